@@ -1,0 +1,399 @@
+/*
+ * mrmd_gb300.h -- C ABI of the GB300-native MRMD hot path.
+ *
+ * One process, one GPU (sm_103a).  Every entry point takes plain pointers and
+ * sizes, returns an int status (MRMD_OK == 0, negative on error) and never
+ * throws.  Device data lives in structs of device pointers that this library
+ * allocates (mrmd_atoms_alloc, mrmd_molecules_alloc, ...); the caller owns the
+ * structs and frees them through the matching *_free call.
+ *
+ * Each declaration names the MRMD (v0.2.0) interface it replaces as
+ * path:line inside the MRMD source tree.  Entry points are synchronous by
+ * default (like the reference's Kokkos::fence() at the end of every action);
+ * mrmd_ctx_set_sync(ctx, 0) turns that off so that a caller can capture a
+ * step into a CUDA graph on the context stream.
+ */
+#ifndef MRMD_GB300_H
+#define MRMD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status -- */
+enum {
+    MRMD_OK = 0,
+    MRMD_ERR_ARG = -1,            /* invalid argument (null, negative size, bad enum)   */
+    MRMD_ERR_OOM = -2,            /* device or pinned allocation failed                 */
+    MRMD_ERR_NLIST_OVERFLOW = -3, /* neighbour list capacity exceeded after retries     */
+    MRMD_ERR_NONFINITE = -4,      /* NaN/Inf detected in positions or forces            */
+    MRMD_ERR_TIMEOUT = -5,        /* a bounded device wait gave up                      */
+    MRMD_ERR_CUDA = -6,           /* CUDA runtime error (see mrmd_ctx_last_error)      */
+    MRMD_ERR_STATE = -7,          /* call order violated (e.g. no ghosts created yet)   */
+    MRMD_ERR_CAPACITY = -8        /* fixed capacity exceeded (no growth allowed here)   */
+};
+
+/* Precision of the pair arithmetic. */
+enum {
+    MRMD_PREC_FP64 = 0,  /* plain FP64 drop-in: all arithmetic in double              */
+    MRMD_PREC_MIXED = 1  /* FP32 pair arithmetic on cell-relative split coordinates,
+                            FP64 positions, velocities, force/energy/virial sums     */
+};
+
+/* Predicate forms used by apply_if-style calls (datatypes.hpp:196-222).  The
+ * slab forms are util::IsInSymmetricSlab (util/IsInSymmetricSlab.hpp:24-64);
+ * the interval form is `lo < x[axis] < hi`. */
+enum {
+    MRMD_PRED_ALWAYS = 0,
+    MRMD_PRED_EITHER_IN_SLAB = 1, /* two positions: slab(p1) || slab(p2) */
+    MRMD_PRED_BOTH_IN_SLAB = 2,   /* two positions: slab(p1) && slab(p2) */
+    MRMD_PRED_IN_SLAB = 3,        /* one position: slab(p)               */
+    MRMD_PRED_IN_OPEN_INTERVAL = 4 /* one position: lo < p[axis] < hi    */
+};
+typedef struct {
+    int32_t kind;
+    int32_t axis;
+    double center;
+    double slabMin; /* or `lo` for the interval form */
+    double slabMax; /* or `hi` for the interval form */
+    double tolerance;
+} mrmd_pred;
+
+/* ------------------------------------------------------------ context -- */
+typedef struct mrmd_ctx mrmd_ctx;
+
+/* Replaces Kokkos::initialize / ScopeGuard (initialization.cpp:23-44) for the
+ * device side: binds `device`, creates the context stream and error word. */
+int mrmd_ctx_create(mrmd_ctx** out, int device);
+int mrmd_ctx_destroy(mrmd_ctx* ctx);
+/* Kokkos::fence() equivalent: waits for the context stream. */
+int mrmd_ctx_sync(mrmd_ctx* ctx);
+/* 1 (default): every entry point synchronises before returning. */
+int mrmd_ctx_set_sync(mrmd_ctx* ctx, int sync);
+/* The CUDA stream (cudaStream_t) all kernels of this context run on. */
+void* mrmd_ctx_stream(mrmd_ctx* ctx);
+const char* mrmd_ctx_last_error(mrmd_ctx* ctx);
+/* Number of kernel launches issued by this context so far. */
+int64_t mrmd_ctx_launch_count(mrmd_ctx* ctx);
+const char* mrmd_version(void);
+
+/* -------------------------------------------------------------- atoms -- */
+/* data::Atoms (data/Atoms.hpp:33-177).  Device layout: pos/vel/force are
+ * [capacity][4] doubles (x, y, z, pad) so that one atom is one 32-byte
+ * sector; scalars are plain arrays.  type is int32 on the device (the
+ * reference's int64 type ids are range-checked at upload). */
+typedef struct {
+    double* pos;
+    double* vel;
+    double* force;
+    int32_t* type;
+    double* mass;
+    double* charge;
+    double* relativeMass;
+    int64_t numLocal;
+    int64_t numGhost;
+    int64_t capacity;
+} mrmd_atoms;
+
+/* GeneralAtoms(numAtoms) constructor (data/Atoms.hpp:123-133): zeroed storage. */
+int mrmd_atoms_alloc(mrmd_ctx* ctx, mrmd_atoms* a, int64_t capacity);
+int mrmd_atoms_free(mrmd_ctx* ctx, mrmd_atoms* a);
+/* GeneralAtoms::resize (data/Atoms.hpp:89-93): grows capacity, keeps content. */
+int mrmd_atoms_reserve(mrmd_ctx* ctx, mrmd_atoms* a, int64_t capacity);
+/* deep_copy host -> device (data/Atoms.hpp:150-159).  Host arrays are the
+ * reference's AoS layout ([n][3] doubles, int64 types); any pointer may be
+ * NULL to leave that field untouched.  Sets numLocal/numGhost. */
+int mrmd_atoms_upload(mrmd_ctx* ctx, mrmd_atoms* a, int64_t numLocal, int64_t numGhost,
+                      const double* pos3, const double* vel3, const double* force3,
+                      const int64_t* type, const double* mass, const double* charge,
+                      const double* relativeMass);
+/* deep_copy device -> host of the first n atoms; NULL pointers are skipped. */
+int mrmd_atoms_download(mrmd_ctx* ctx, const mrmd_atoms* a, int64_t n, double* pos3,
+                        double* vel3, double* force3, int64_t* type, double* mass,
+                        double* charge, double* relativeMass);
+/* GeneralAtoms::setForce(val) / Cabana::deep_copy(force, val) for atoms [0, n). */
+int mrmd_atoms_set_force(mrmd_ctx* ctx, mrmd_atoms* a, int64_t n, double val);
+/* Atoms::permute(LinkedCellList) (data/Atoms.hpp:95): stable counting sort of
+ * the local atoms by cell of the grid [gridMin, gridMax) with cells of edge
+ * >= delta.  perm_out (device, may be NULL) receives old index per new slot. */
+int mrmd_atoms_sort_by_cell(mrmd_ctx* ctx, mrmd_atoms* a, const double* gridMin,
+                            const double* gridMax, double delta, int64_t* perm_out);
+
+/* ---------------------------------------------------------- molecules -- */
+/* data::Molecules (data/Molecules.hpp:27-176).  pos/force/gradLambda are
+ * [capacity][4] doubles on the device. */
+typedef struct {
+    double* pos;
+    double* force;
+    double* lambda;
+    double* modulatedLambda;
+    double* gradLambda;
+    int64_t* atomsOffset;
+    int64_t* numAtoms;
+    int64_t numLocal;
+    int64_t numGhost;
+    int64_t capacity;
+} mrmd_molecules;
+
+int mrmd_molecules_alloc(mrmd_ctx* ctx, mrmd_molecules* m, int64_t capacity);
+int mrmd_molecules_free(mrmd_ctx* ctx, mrmd_molecules* m);
+int mrmd_molecules_reserve(mrmd_ctx* ctx, mrmd_molecules* m, int64_t capacity);
+int mrmd_molecules_upload(mrmd_ctx* ctx, mrmd_molecules* m, int64_t numLocal, int64_t numGhost,
+                          const double* pos3, const double* force3, const double* lambda,
+                          const double* modulatedLambda, const double* gradLambda3,
+                          const int64_t* atomsOffset, const int64_t* numAtoms);
+int mrmd_molecules_download(mrmd_ctx* ctx, const mrmd_molecules* m, int64_t n, double* pos3,
+                            double* force3, double* lambda, double* modulatedLambda,
+                            double* gradLambda3, int64_t* atomsOffset, int64_t* numAtoms);
+/* GeneralMolecules::setForce (data/Molecules.hpp:60). */
+int mrmd_molecules_set_force(mrmd_ctx* ctx, mrmd_molecules* m, int64_t n, double val);
+
+/* ------------------------------------------------------- ghost layer -- */
+/* data::Subdomain corners (data/Subdomain.hpp:41-62); filled by
+ * mrmd_subdomain_init from min/max corner and ghost layer thickness. */
+typedef struct {
+    double minCorner[3];
+    double maxCorner[3];
+    double ghostLayerThickness[3];
+    double minGhostCorner[3];
+    double maxGhostCorner[3];
+    double minInnerCorner[3];
+    double maxInnerCorner[3];
+    double diameter[3];
+    double diameterWithGhostLayer[3];
+} mrmd_subdomain;
+
+int mrmd_subdomain_init(mrmd_subdomain* sd, const double* minCorner, const double* maxCorner,
+                        const double* ghostLayerThickness3);
+
+/* communication::GhostLayer / MultiResGhostLayer state: the
+ * correspondingRealAtom index of every atom (-1 for real atoms). */
+typedef struct {
+    int32_t* correspondingRealAtom; /* device, [capacity] */
+    int64_t capacity;
+    int64_t numLocal; /* atom counts the ghosts were built for */
+    int64_t numGhost;
+    /* real atom -> its ghosts, CSR sorted by ghost index (device); lets the
+     * force fold-back gather in the reference's serial order without atomics */
+    int32_t* ghostStart; /* [localCapacity + 1] */
+    int32_t* ghostList;  /* [capacity]          */
+    int64_t localCapacity;
+} mrmd_ghost_layer;
+
+int mrmd_ghost_layer_alloc(mrmd_ctx* ctx, mrmd_ghost_layer* g, int64_t capacity);
+int mrmd_ghost_layer_free(mrmd_ctx* ctx, mrmd_ghost_layer* g);
+/* GhostLayer::exchangeRealAtoms -> PeriodicMapping::mapIntoDomain
+ * (communication/GhostLayer.hpp:35-38, PeriodicMapping.cpp:30-58). */
+int mrmd_ghost_exchange_real_atoms(mrmd_ctx* ctx, mrmd_atoms* a, const mrmd_subdomain* sd);
+/* GhostLayer::createGhostAtoms -> GhostExchange::createGhostAtomsXYZ
+ * (GhostLayer.hpp:40-43, GhostExchange.cpp:59-181).  Same ghost set and
+ * order as the reference; grows atoms/ghost-layer capacity when needed. */
+int mrmd_ghost_create(mrmd_ctx* ctx, mrmd_ghost_layer* g, mrmd_atoms* a, const mrmd_subdomain* sd);
+/* GhostLayer::updateGhostAtoms -> UpdateGhostAtoms::updateOnlyPos
+ * (GhostLayer.hpp:45-50, UpdateGhostAtoms.cpp:31-68). */
+int mrmd_ghost_update(mrmd_ctx* ctx, const mrmd_ghost_layer* g, mrmd_atoms* a,
+                      const mrmd_subdomain* sd);
+/* GhostLayer::contributeBackGhostToReal -> AccumulateForce::ghostToReal
+ * (GhostLayer.hpp:52-55, AccumulateForce.cpp:25-47). */
+int mrmd_ghost_reduce_force(mrmd_ctx* ctx, const mrmd_ghost_layer* g, mrmd_atoms* a);
+/* MultiResGhostLayer::exchangeRealAtoms -> realAtomsExchange
+ * (MultiResGhostLayer.hpp:36-41, MultiResRealAtomsExchange.cpp:23-73). */
+int mrmd_multires_exchange_real_atoms(mrmd_ctx* ctx, mrmd_molecules* m, mrmd_atoms* a,
+                                      const mrmd_subdomain* sd);
+/* MultiResGhostLayer::createGhostAtoms -> MultiResPeriodicGhostExchange::createGhostAtomsXYZ
+ * (MultiResGhostLayer.hpp:43-48, MultiResPeriodicGhostExchange.cpp:60-277). */
+int mrmd_multires_ghost_create(mrmd_ctx* ctx, mrmd_ghost_layer* g, mrmd_molecules* m,
+                               mrmd_atoms* a, const mrmd_subdomain* sd);
+/* Copy the correspondingRealAtom array (first n entries) to the host. */
+int mrmd_ghost_layer_download(mrmd_ctx* ctx, const mrmd_ghost_layer* g, int64_t n, int64_t* out);
+
+/* ------------------------------------------------- neighbour list -- */
+/* HalfVerletList = Cabana::VerletList<HalfNeighborTag, VerletLayout2D>
+ * (datatypes.hpp:184-187).  Layout: counts[rows], neighbours transposed as
+ * nbrs[k * stride + i] so that a warp reading slot k of 32 consecutive
+ * atoms issues one coalesced 128-byte load. */
+typedef struct {
+    int32_t* counts;   /* device, [rowsCapacity]            */
+    int32_t* nbrs;     /* device, [maxNeighbors * stride]   */
+    int64_t rows;      /* number of list rows (end - begin) */
+    int64_t begin;     /* first particle with a list        */
+    int64_t stride;    /* row stride of nbrs (>= rows, multiple of 32) */
+    int64_t maxNeighbors;
+    int64_t rowsCapacity;
+    int64_t nbrsCapacity; /* allocated int32 entries of nbrs */
+    int64_t totalPairs;   /* sum of counts after the last build */
+    void* cells;          /* opaque cell-grid scratch owned by the list */
+} mrmd_nlist;
+
+int mrmd_nlist_init(mrmd_ctx* ctx, mrmd_nlist* nl);
+int mrmd_nlist_free(mrmd_ctx* ctx, mrmd_nlist* nl);
+/* HalfVerletList::build(pos, begin, end, r, cell_ratio, gridMin, gridMax,
+ * maxNeigh) (call sites examples/02_LennardJones_NVE:156-163,
+ * tests/LennardJones/LennardJones.cpp:112-118).  Candidates are positions
+ * [0, nPos); a pair (i, j) is kept when |x_i - x_j|^2 <= r^2 and x_j is
+ * above x_i in lexicographic (x, y, z) order (Cabana's half-neighbour
+ * discriminator).  Capacity grows (and the build reruns) on overflow. */
+int mrmd_nlist_build(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t nPos,
+                     int64_t begin, int64_t end, double rlist, double cellRatio,
+                     const double* gridMin, const double* gridMax, int64_t maxNeighbors);
+/* Copy counts (rows) and neighbours in row-major [rows][cap] form to the host. */
+int mrmd_nlist_download(mrmd_ctx* ctx, const mrmd_nlist* nl, int32_t* counts, int32_t* nbrs,
+                        int64_t cap);
+/* Cell id of each of the first n positions on the grid the list builder uses
+ * (cell edge >= delta; id = (ix*ny + iy)*nz + iz).  cells_out is host int64[n]. */
+int mrmd_cell_index(mrmd_ctx* ctx, const double* pos4, int64_t n, const double* gridMin,
+                    const double* gridMax, double delta, int64_t* cells_out);
+
+/* ------------------------------------------------------ Lennard-Jones -- */
+/* impl::CappedLennardJonesPotential::PrecomputedValues (action/LennardJones.hpp:27-39). */
+typedef struct {
+    double ff1, ff2, ef1, ef2;
+    double rcSqr;
+    double cappingDistance, cappingDistanceSqr, cappingCoeff;
+    double shift, energyAtCappingPoint;
+} mrmd_lj_params;
+
+typedef struct mrmd_lj mrmd_lj;
+/* LennardJones(cappingDistance, rc, sigma, epsilon, numTypes, isShifted)
+ * (action/LennardJones.hpp:127-132, LennardJones.cpp:254-324): vectors of
+ * numTypes^2 entries.  numTypesIndex is the multiplier of type_i in the
+ * table index (the reference's LennardJones fixes it to 1,
+ * LennardJones.cpp:260; LJ_IdealGas uses numTypes, LJ_IdealGas.cpp:139). */
+int mrmd_lj_create(mrmd_ctx* ctx, mrmd_lj** out, int64_t numTypes, int64_t numTypesIndex,
+                   const double* cappingDistance, const double* rc, const double* sigma,
+                   const double* epsilon, int isShifted);
+int mrmd_lj_destroy(mrmd_ctx* ctx, mrmd_lj* lj);
+int mrmd_lj_get_params(const mrmd_lj* lj, mrmd_lj_params* out, int64_t count);
+/* LennardJones::apply / apply_if (LennardJones.cpp:24-33, LennardJones.hpp:135-206):
+ * half-list pair force over local atoms [0, a->numLocal) with the list's
+ * rows, forces accumulated (i and j, ghosts included), energy and virial
+ * of this call returned (either pointer may be NULL). */
+int mrmd_lj_apply(mrmd_ctx* ctx, mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* nl,
+                  const mrmd_pred* pred, int precision, double* energy, double* virial);
+
+/* ------------------------------------------------------- integrators -- */
+/* VelocityVerlet::preForceIntegrate (action/VelocityVerlet.cpp:26-67);
+ * returns the max displacement in *maxDisplacement (may be NULL). */
+int mrmd_vv_pre(mrmd_ctx* ctx, mrmd_atoms* a, double dt, double* maxDisplacement);
+/* VelocityVerlet::postForceIntegrate (action/VelocityVerlet.cpp:69-90). */
+int mrmd_vv_post(mrmd_ctx* ctx, mrmd_atoms* a, double dt);
+/* VelocityVerletLangevinThermostat::preForceIntegrate(_apply_if)
+ * (action/VelocityVerletLangevinThermostat.hpp:33-121).  The reference's
+ * XorShift1024 pool is replaced by Philox4x32-10 keyed by (seed, step) with
+ * the local atom index as counter, so a run is reproducible. */
+int mrmd_langevin_pre(mrmd_ctx* ctx, mrmd_atoms* a, double dt, double zeta, double temperature,
+                      uint64_t seed, uint64_t step, const mrmd_pred* pred,
+                      double* maxDisplacement);
+
+/* ------------------------------------------------------------ AdResS -- */
+/* weighting_function::Slab (weighting_function/Slab.hpp:189-200): center,
+ * atomistic region diameter, hybrid width, nu (exponent 2*nu), interface
+ * type 0 smooth / 1 abrupt. */
+typedef struct {
+    double center[3];
+    double atomisticRegionDiameter;
+    double hybridRegionDiameter;
+    int64_t nu;
+    int32_t interfaceType;
+    int32_t pad;
+} mrmd_slab;
+
+/* UpdateMolecules::update<Slab> (action/UpdateMolecules.hpp:24-70). */
+int mrmd_update_molecules(mrmd_ctx* ctx, mrmd_molecules* m, const mrmd_atoms* a,
+                          const mrmd_slab* slab);
+/* ContributeMoleculeForceToAtoms::update (action/ContributeMoleculeForceToAtoms.cpp:23-48). */
+int mrmd_contribute_molecule_force(mrmd_ctx* ctx, const mrmd_molecules* m, mrmd_atoms* a);
+
+typedef struct mrmd_ljig mrmd_ljig;
+/* LJ_IdealGas(cappingDistance, rc, sigma, epsilon, numTypes, doShift)
+ * (action/LJ_IdealGas.hpp:92-103, LJ_IdealGas.cpp:262-292). */
+int mrmd_ljig_create(mrmd_ctx* ctx, mrmd_ljig** out, int64_t numTypes,
+                     const double* cappingDistance, const double* rc, const double* sigma,
+                     const double* epsilon, int doShift);
+int mrmd_ljig_destroy(mrmd_ctx* ctx, mrmd_ljig* s);
+/* setCompensationEnergySamplingInterval / setCompensationEnergyUpdateInterval
+ * (LJ_IdealGas.hpp:73-80). */
+int mrmd_ljig_set_intervals(mrmd_ljig* s, int64_t samplingInterval, int64_t updateInterval);
+/* LJ_IdealGas::run (LJ_IdealGas.cpp:227-260). */
+int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nlist* nl,
+                  mrmd_atoms* a, int precision, double* energy);
+/* getMeanCompensationEnergy (LJ_IdealGas.hpp:81) and the two sampling
+ * histograms, each [200][numTypes] (any pointer may be NULL). */
+int mrmd_ljig_get_compensation(mrmd_ctx* ctx, const mrmd_ljig* s, double* mean, double* energy,
+                               double* counter, int64_t* runCounter);
+int mrmd_ljig_set_compensation(mrmd_ctx* ctx, mrmd_ljig* s, const double* mean);
+
+/* ------------------------------------------------ thermodynamic force -- */
+typedef struct mrmd_tf mrmd_tf;
+/* ThermodynamicForce(targetDensity[], subdomain, binWidth, modulation[],
+ * enforceSymmetry, usePeriodicity) (action/ThermodynamicForce.cpp:25-57). */
+int mrmd_tf_create(mrmd_ctx* ctx, mrmd_tf** out, int64_t numTypes, const double* targetDensity,
+                   const mrmd_subdomain* sd, double requestedBinWidth,
+                   const double* modulation, int enforceSymmetry, int usePeriodicity);
+int mrmd_tf_destroy(mrmd_ctx* ctx, mrmd_tf* tf);
+/* numBins, binSize, numTypes of the force/density histograms. */
+int mrmd_tf_shape(const mrmd_tf* tf, int64_t* numBins, double* binSize, int64_t* numTypes);
+/* ThermodynamicForce::sample (ThermodynamicForce.cpp:74-86). */
+int mrmd_tf_sample(mrmd_ctx* ctx, mrmd_tf* tf, const mrmd_atoms* a);
+/* apply / apply_if (ThermodynamicForce.cpp:93-96, .hpp:98-122) and
+ * applyInterpolated_if (.hpp:154-216) when interpolated != 0. */
+int mrmd_tf_apply(mrmd_ctx* ctx, const mrmd_tf* tf, mrmd_atoms* a, const mrmd_pred* pred,
+                  int interpolated);
+/* update / update_if (ThermodynamicForce.cpp:88-91, .hpp:124-152); pred may
+ * be NULL (update).  Returns MRMD_ERR_STATE without samples. */
+int mrmd_tf_update(mrmd_ctx* ctx, mrmd_tf* tf, double smoothingSigma, double smoothingIntensity,
+                   const mrmd_pred* pred);
+/* getForce / setForce / getDensityProfile / getNumberOfDensityProfileSamples
+ * (.hpp:48-63), host arrays [numBins][numTypes]. */
+int mrmd_tf_get_force(mrmd_ctx* ctx, const mrmd_tf* tf, double* out);
+int mrmd_tf_set_force(mrmd_ctx* ctx, mrmd_tf* tf, const double* in);
+int mrmd_tf_get_density(mrmd_ctx* ctx, const mrmd_tf* tf, double* out, int64_t* samples);
+/* getMuLeft / getMuRight (ThermodynamicForce.cpp:98-130), host [numTypes]. */
+int mrmd_tf_mu(mrmd_ctx* ctx, const mrmd_tf* tf, double* muLeft, double* muRight);
+
+/* ---------------------------------------------- fused LJ NVE stepper -- */
+/* The examples/02_LennardJones_NVE time loop (02_LennardJones_NVE.cpp:135-216)
+ * as one device-resident object: cell-sorted atoms, ghost layer, half list
+ * rebuilt every `rebuildInterval` steps, VV integration fused with force
+ * zeroing, and the steps between rebuilds replayed as one CUDA graph. */
+typedef struct mrmd_md mrmd_md;
+typedef struct {
+    double boxMin[3];
+    double boxMax[3];
+    double rc;
+    double skin;
+    double sigma;
+    double epsilon;
+    double cappingDistance;
+    int32_t shifted;
+    int32_t precision;       /* MRMD_PREC_FP64 or MRMD_PREC_MIXED */
+    double dt;
+    int64_t rebuildInterval; /* steps between list rebuilds (>= 1) */
+    int32_t useGraph;        /* capture the steps between rebuilds as a CUDA graph */
+    int32_t sortAtoms;       /* permute atoms by cell at every rebuild */
+    int64_t maxNeighbors;    /* initial list capacity (grown on overflow) */
+} mrmd_md_config;
+
+int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int64_t n,
+                   const double* pos3, const double* vel3, const double* mass);
+int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md);
+/* Advance nsteps; energies (may be NULL) receives the LJ energy and virial
+ * of every step as [nsteps][2] (read back from pinned memory at the end). */
+int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies);
+/* Current state in the ORIGINAL atom order (host [n][3] arrays, NULL skips). */
+int mrmd_md_get_state(mrmd_ctx* ctx, mrmd_md* md, double* pos3, double* vel3, double* force3);
+/* Replace positions/velocities (original order) and force a rebuild. */
+int mrmd_md_set_state(mrmd_ctx* ctx, mrmd_md* md, const double* pos3, const double* vel3);
+/* Counters: [0] steps, [1] rebuilds, [2] list pairs, [3] ghosts, [4] list capacity. */
+int mrmd_md_stats(const mrmd_md* md, int64_t* out5);
+/* Access to the internal atoms / list for profiling and tests. */
+const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md);
+const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

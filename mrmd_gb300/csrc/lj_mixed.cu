@@ -1,0 +1,243 @@
+// Mixed-precision Lennard-Jones pair force.
+//
+// Positions stay FP64 in the atoms; before the pair kernel each coordinate
+// c = x - origin (origin = the list's cell-grid corner) is split into
+//   hi = c rounded to a multiple of 2^-q, q = 24 - ceil(log2(extent)),
+//   lo = float(c - hi),
+// so every hi is an integer multiple of 2^-q below 2^24 * 2^-q: the FP32
+// difference hi_i - hi_j is exact, and dx = (hi_i - hi_j) + (lo_i - lo_j)
+// carries ~2^-40 absolute accuracy.  r^2, 1/r^2 and the force factor are
+// evaluated in double-float (pairs of FP32) because the LJ force factor
+// amplifies a relative error of r^2 sevenfold (F ~ r^-14); the result is
+// rounded once to FP32.  All of this runs on the FP32 pipe.  Energy and
+// virial use FP32 terms, summed with compensated FP32 per thread and FP64
+// across threads; the i-force is a compensated FP32 sum added to the FP64
+// force array, and the j-force of the half list goes out as FP64 atomics.
+#include <cmath>
+
+#include "common.cuh"
+#include "lj_impl.cuh"
+#include "lj_mixed.cuh"
+#include "nlist_impl.cuh"
+
+using namespace mrmd_impl;
+
+namespace mrmd_impl
+{
+SplitParams split_params(const double* origin, double extent)
+{
+    SplitParams s{};
+    int e = 0;
+    std::frexp(extent > 1.0 ? extent : 1.0, &e);  // extent < 2^e
+    const int q = 24 - e;
+    s.origin = make_double3(origin[0], origin[1], origin[2]);
+    s.scale = std::ldexp(1.0, q);
+    s.invScale = std::ldexp(1.0, -q);
+    return s;
+}
+
+__global__ void k_split_coords(const double4* __restrict__ pos, int64_t n, SplitParams sp,
+                               float4* __restrict__ hi, float4* __restrict__ lo)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const double4 p = pos[i];
+        float4 h, l;
+        split_one(p.x - sp.origin.x, sp, h.x, l.x);
+        split_one(p.y - sp.origin.y, sp, h.y, l.y);
+        split_one(p.z - sp.origin.z, sp, h.z, l.z);
+        h.w = 0.0f;
+        l.w = 0.0f;
+        hi[i] = h;
+        lo[i] = l;
+    }
+}
+
+int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo)
+{
+    if (n == 0) return MRMD_OK;
+    k_split_coords<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n, sp,
+                                                                   hi, lo);
+    return after_launch(ctx, "split_coords");
+}
+
+namespace
+{
+constexpr int MX_TB = 128;
+
+template <bool PRED>
+__global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
+    const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
+    double* __restrict__ force, const LJDev p, float rcSqrf, const int32_t* __restrict__ counts,
+    const int32_t* __restrict__ nbrs, int64_t stride, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
+{
+    __shared__ double red[64];
+    df eAcc{0.f, 0.f}, wAcc{0.f, 0.f};
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const float4 hi_i = hi[i], lo_i = lo[i];
+        double4 pi;
+        if (PRED) pi = pos[i];
+        df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
+        const int32_t cnt = counts[i];
+        const int32_t* __restrict__ col = nbrs + i;
+        for (int32_t k = 0; k < cnt; ++k)
+        {
+            const int32_t j = __ldg(col + (int64_t)k * stride);
+            if (PRED)
+            {
+                const double4 pj = mrmd_dev::ldg4(pos + j);
+                if (!mrmd_dev::pred2(pred, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z)) continue;
+            }
+            const float4 hj = __ldg(hi + j), lj = __ldg(lo + j);
+            float ff, e, r2h;
+            float3 d;
+            if (!pair_mixed(hi_i, lo_i, hj, lj, p, rcSqrf, ff, e, r2h, d)) continue;
+            df_acc(eAcc, e);
+            df_acc(wAcc, -0.5f * ff * r2h);
+            const float gx = d.x * ff, gy = d.y * ff, gz = d.z * ff;
+            df_acc(fx, gx);
+            df_acc(fy, gy);
+            df_acc(fz, gz);
+            atomicAdd(force + 4 * (int64_t)j + 0, -(double)gx);
+            atomicAdd(force + 4 * (int64_t)j + 1, -(double)gy);
+            atomicAdd(force + 4 * (int64_t)j + 2, -(double)gz);
+        }
+        atomicAdd(force + 4 * i + 0, (double)fx.h + (double)fx.l);
+        atomicAdd(force + 4 * i + 1, (double)fy.h + (double)fy.l);
+        atomicAdd(force + 4 * i + 2, (double)fz.h + (double)fz.l);
+    }
+    double e = (double)eAcc.h + (double)eAcc.l, w = (double)wAcc.h + (double)wAcc.l;
+    mrmd_dev::block_sum2(e, w, red);
+    if (threadIdx.x == 0)
+    {
+        atomicAdd(ev + 0, e);
+        atomicAdd(ev + 1, w);
+    }
+}
+// Full-list form: every pair is evaluated from both sides, each thread owns
+// its atom's force (no atomics, deterministic) and ghosts receive nothing,
+// so no ghost force fold-back is needed.  Energy and virial are halved.
+template <bool ACCUM>
+__global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
+    const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
+    float rcSqrf, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t stride, int64_t n,
+    double* __restrict__ ev)
+{
+    __shared__ double red[64];
+    df eAcc{0.f, 0.f}, wAcc{0.f, 0.f};
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const float4 hi_i = hi[i], lo_i = lo[i];
+        df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
+        const int32_t cnt = counts[i];
+        const int32_t* __restrict__ col = nbrs + i;
+        int32_t k = 0;
+        for (; k + 1 < cnt; k += 2)
+        {
+            const int32_t j0 = __ldg(col + (int64_t)k * stride);
+            const int32_t j1 = __ldg(col + (int64_t)(k + 1) * stride);
+            const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
+            const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
+            float ff, e, r2h;
+            float3 d;
+            if (pair_mixed(hi_i, lo_i, h0, l0, p, rcSqrf, ff, e, r2h, d))
+            {
+                df_acc(eAcc, e);
+                df_acc(wAcc, -0.5f * ff * r2h);
+                df_acc(fx, d.x * ff);
+                df_acc(fy, d.y * ff);
+                df_acc(fz, d.z * ff);
+            }
+            if (pair_mixed(hi_i, lo_i, h1, l1, p, rcSqrf, ff, e, r2h, d))
+            {
+                df_acc(eAcc, e);
+                df_acc(wAcc, -0.5f * ff * r2h);
+                df_acc(fx, d.x * ff);
+                df_acc(fy, d.y * ff);
+                df_acc(fz, d.z * ff);
+            }
+        }
+        if (k < cnt)
+        {
+            const int32_t j0 = __ldg(col + (int64_t)k * stride);
+            float ff, e, r2h;
+            float3 d;
+            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rcSqrf, ff, e, r2h, d))
+            {
+                df_acc(eAcc, e);
+                df_acc(wAcc, -0.5f * ff * r2h);
+                df_acc(fx, d.x * ff);
+                df_acc(fy, d.y * ff);
+                df_acc(fz, d.z * ff);
+            }
+        }
+        double4 f = make_double4((double)fx.h + (double)fx.l, (double)fy.h + (double)fy.l,
+                                 (double)fz.h + (double)fz.l, 0.0);
+        if (ACCUM)
+        {
+            const double4 o = force[i];
+            f.x += o.x;
+            f.y += o.y;
+            f.z += o.z;
+        }
+        force[i] = f;
+    }
+    double e = 0.5 * ((double)eAcc.h + (double)eAcc.l), w = 0.5 * ((double)wAcc.h + (double)wAcc.l);
+    mrmd_dev::block_sum2(e, w, red);
+    if (threadIdx.x == 0)
+    {
+        atomicAdd(ev + 0, e);
+        atomicAdd(ev + 1, w);
+    }
+}
+}  // namespace
+
+int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
+                  const mrmd_nlist* nl, double* ev, bool accumulate)
+{
+    const int64_t n = nl->rows;
+    if (n == 0) return MRMD_OK;
+    const unsigned grid = (unsigned)div_up(n, MX_TB);
+    if (accumulate)
+        k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
+                                                              (float)rcSqr, nl->counts, nl->nbrs, nl->stride, n, ev);
+    else
+        k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
+                                                               (float)rcSqr, nl->counts, nl->nbrs, nl->stride, n, ev);
+    return after_launch(ctx, "lj_mixed_full");
+}
+
+int lj_apply_mixed(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* nl, const mrmd_pred* pred,
+                   double* ev)
+{
+    if (lj->numTypes > 1)
+        return set_error(ctx, MRMD_ERR_ARG, "mixed precision supports one atom type");
+    const int64_t n = nl->rows;
+    if (n == 0) return MRMD_OK;
+    const CellList* cl = static_cast<const CellList*>(nl->cells);
+    const double origin[3] = {cl->g.mn.x, cl->g.mn.y, cl->g.mn.z};
+    const SplitParams sp = split_params(origin, cl->g.extent * 1.25 + 8.0);
+    const int64_t nAll = a->numLocal + a->numGhost;
+    float4* hi = static_cast<float4*>(scratch(ctx, sizeof(float4) * 2 * (size_t)nAll));
+    if (!hi) return MRMD_ERR_OOM;
+    float4* lo = hi + nAll;
+    MRMD_TRY(split_coords(ctx, a->pos, nAll, sp, hi, lo));
+    const bool usePred = pred != nullptr && pred->kind != MRMD_PRED_ALWAYS;
+    const unsigned grid = (unsigned)div_up(n, MX_TB);
+    const mrmd_dev::Pred dp = to_dev_pred(pred);
+    const float rcSqrf = (float)lj->rcSqr;
+    if (usePred)
+        k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
+                                                               a->force, lj->p0, rcSqrf, nl->counts, nl->nbrs,
+                                                               nl->stride, n, dp, ev);
+    else
+        k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
+                                                                a->force, lj->p0, rcSqrf, nl->counts, nl->nbrs,
+                                                                nl->stride, n, dp, ev);
+    return after_launch(ctx, "lj_mixed_half");
+}
+}  // namespace mrmd_impl

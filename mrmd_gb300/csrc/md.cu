@@ -1,0 +1,504 @@
+// Fused LJ NVE stepper: the examples/02_LennardJones_NVE time loop
+// (02_LennardJones_NVE.cpp:135-216) as one device-resident object.
+//
+// Per step:
+//   [post-kick of step s-1 + pre-kick/drift of step s + force zeroing]  one kernel
+//   rebuild (every K steps): mapIntoDomain, cell sort, ghosts, list
+//   or ghost position update
+//   (mixed) FP32 split coordinates of local + ghost atoms
+//   pair force (FP64: half list + atomics; mixed: full list, no atomics)
+//   (FP64) ghost force fold-back
+// and the final post-kick when a run ends.  The kick arithmetic is the
+// reference's (two kicks with the same force, then the drift), so fusing
+// post(s-1) with pre(s) changes no bit.  The K-1 steps between rebuilds
+// are captured once per rebuild and replayed as one CUDA graph.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "integrate_impl.cuh"
+#include "lj_impl.cuh"
+#include "lj_mixed.cuh"
+#include "nlist_impl.cuh"
+
+using namespace mrmd_impl;
+
+namespace
+{
+constexpr int TB = 256;
+
+__global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
+                                   const double* __restrict__ mass, int64_t n, double dtHalf, double dt, int postKick)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        double4 v = vel[i], x = pos[i];
+        const double4 f = force[i];
+        const double dtfm = __ddiv_rn(dtHalf, mass[i]);
+        if (postKick) kick(v, f, dtfm);  // VelocityVerlet::postForceIntegrate of the previous step
+        kick(v, f, dtfm);                // preForceIntegrate
+        drift(x, v, dt);
+        pos[i] = x;
+        vel[i] = v;
+        force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    }
+}
+
+__global__ void k_post_kick(double4* __restrict__ vel, const double4* __restrict__ force,
+                            const double* __restrict__ mass, int64_t n, double dtHalf)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        double4 v = vel[i];
+        kick(v, force[i], __ddiv_rn(dtHalf, mass[i]));
+        vel[i] = v;
+    }
+}
+
+__global__ void k_gather_i32(const int32_t* __restrict__ src, int32_t* __restrict__ dst,
+                             const int32_t* __restrict__ perm, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+__global__ void k_iota(int32_t* p, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (int32_t)i;
+}
+
+// out[orig[i]] = v[i] (three components) for the first n atoms
+__global__ void k_unpermute3(const double4* __restrict__ v, const int32_t* __restrict__ orig, int64_t n,
+                             double* __restrict__ out3)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const double4 x = v[i];
+        const int64_t o = orig[i];
+        out3[3 * o] = x.x;
+        out3[3 * o + 1] = x.y;
+        out3[3 * o + 2] = x.z;
+    }
+}
+
+// v[i] = in[orig[i]]
+__global__ void k_permute_in3(const double* __restrict__ in3, const int32_t* __restrict__ orig, int64_t n,
+                              double4* __restrict__ v)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t o = orig[i];
+        v[i] = make_double4(in3[3 * o], in3[3 * o + 1], in3[3 * o + 2], 0.0);
+    }
+}
+}  // namespace
+
+struct mrmd_md
+{
+    mrmd_md_config cfg{};
+    mrmd_subdomain sd{};
+    mrmd_atoms atoms{};
+    mrmd_atoms shadow{};
+    mrmd_ghost_layer ghosts{};
+    mrmd_nlist list{};
+    mrmd_lj* lj = nullptr;
+    CellList sortCells;
+    CellGrid grid{};
+    int32_t* orig = nullptr;     // original index of each local atom
+    int32_t* origTmp = nullptr;
+    float4* split = nullptr;     // [2][capacity] hi, lo
+    int64_t splitCap = 0;
+    SplitParams sp{};
+    double* dEnergy = nullptr;   // [energyCap][2]
+    int64_t energyCap = 0;
+    double* hEnergy = nullptr;   // pinned
+    int64_t n = 0;
+    int64_t steps = 0, rebuilds = 0;
+    bool forceValid = false;     // force array holds F(x) of the current positions
+    bool needRebuild = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t graphSteps = 0;      // steps captured in exec
+    int64_t graphFirstSlot = -1; // energy slot of the first captured step
+};
+
+namespace
+{
+int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
+{
+    mrmd_atoms* a = &md->atoms;
+    MRMD_TRY(mrmd_ghost_exchange_real_atoms(ctx, a, &md->sd));
+    if (md->cfg.sortAtoms)
+    {
+        MRMD_TRY(md->sortCells.build(ctx, a->pos, md->n, md->grid));
+        if (md->shadow.capacity < a->capacity)
+        {
+            mrmd_atoms_free(ctx, &md->shadow);
+            MRMD_TRY(mrmd_atoms_alloc(ctx, &md->shadow, a->capacity));
+        }
+        a->numGhost = 0;
+        MRMD_TRY(permute_atoms(ctx, a, &md->shadow, md->sortCells.sorted, md->n));
+        k_gather_i32<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(md->orig, md->origTmp, md->sortCells.sorted,
+                                                                        md->n);
+        MRMD_TRY(after_launch(ctx, "gather_orig"));
+        std::swap(md->orig, md->origTmp);
+    }
+    MRMD_TRY(mrmd_ghost_create(ctx, &md->ghosts, a, &md->sd));
+    const int64_t nAll = a->numLocal + a->numGhost;
+    const bool full = md->cfg.precision == MRMD_PREC_MIXED;
+    const double rlist = md->cfg.rc + md->cfg.skin;
+    MRMD_TRY(build_half_list(ctx, &md->list, a->pos, nAll, 0, a->numLocal, rlist, md->grid,
+                             md->list.maxNeighbors > 0 ? md->list.maxNeighbors : md->cfg.maxNeighbors, full));
+    if (full && nAll > md->splitCap)
+    {
+        dfree(md->split);
+        md->split = nullptr;
+        const int64_t c = nAll + nAll / 8 + 64;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->split), sizeof(float4) * 2 * (size_t)c));
+        md->splitCap = c;
+    }
+    md->rebuilds++;
+    md->needRebuild = false;
+    return MRMD_OK;
+}
+
+// Force evaluation of the current positions into atoms.force (zeroed by the
+// caller), energy/virial added into ev.
+int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
+{
+    mrmd_atoms* a = &md->atoms;
+    if (md->cfg.precision == MRMD_PREC_MIXED)
+    {
+        const int64_t nAll = a->numLocal + a->numGhost;
+        MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + md->splitCap));
+        return lj_mixed_full(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
+                             &md->list, ev, false);
+    }
+    MRMD_TRY(lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev));
+    return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
+}
+
+// One step without rebuild, for capture: kick/drift, ghost update, forces.
+int md_plain_step(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool postKick)
+{
+    mrmd_atoms* a = &md->atoms;
+    k_fused_kick_drift<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(
+        reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel), reinterpret_cast<double4*>(a->force),
+        a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0);
+    MRMD_TRY(after_launch(ctx, "fused_kick_drift"));
+    MRMD_TRY(mrmd_ghost_update(ctx, &md->ghosts, a, &md->sd));
+    return md_forces(ctx, md, ev);
+}
+
+int ensure_energy(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps)
+{
+    if (nsteps + 1 <= md->energyCap) return MRMD_OK;
+    cudaStreamSynchronize(ctx->stream);
+    dfree(md->dEnergy);
+    if (md->hEnergy) cudaFreeHost(md->hEnergy);
+    md->dEnergy = nullptr;
+    md->hEnergy = nullptr;
+    const int64_t c = nsteps + 64;
+    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->dEnergy), sizeof(double) * 2 * (size_t)c));
+    MRMD_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&md->hEnergy), sizeof(double) * 2 * (size_t)c));
+    md->energyCap = c;
+    // any captured graph referenced the old buffer
+    if (md->exec)
+    {
+        cudaGraphExecDestroy(md->exec);
+        md->exec = nullptr;
+    }
+    return MRMD_OK;
+}
+
+void drop_graph(mrmd_md* md)
+{
+    if (md->exec) cudaGraphExecDestroy(md->exec);
+    if (md->graph) cudaGraphDestroy(md->graph);
+    md->exec = nullptr;
+    md->graph = nullptr;
+    md->graphSteps = 0;
+}
+
+// Capture `count` plain steps writing energies into slots [slot0, slot0+count).
+int capture_steps(mrmd_ctx* ctx, mrmd_md* md, int64_t count, int64_t slot0)
+{
+    cudaGraph_t g = nullptr;
+    const int oldSync = ctx->sync;
+    ctx->sync = 0;
+    MRMD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = MRMD_OK;
+    for (int64_t k = 0; k < count && rc == MRMD_OK; ++k) rc = md_plain_step(ctx, md, md->dEnergy + 2 * (slot0 + k), true);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->sync = oldSync;
+    if (rc != MRMD_OK)
+    {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    MRMD_TRY(check_cuda(ctx, e, "end capture"));
+    if (md->exec && md->graphSteps == count)
+    {
+        cudaGraphExecUpdateResultInfo info{};
+        if (cudaGraphExecUpdate(md->exec, g, &info) == cudaSuccess)
+        {
+            if (md->graph) cudaGraphDestroy(md->graph);
+            md->graph = g;
+            md->graphFirstSlot = slot0;
+            return MRMD_OK;
+        }
+        cudaGetLastError();
+    }
+    drop_graph(md);
+    md->graph = g;
+    MRMD_CUDA(ctx, cudaGraphInstantiate(&md->exec, g, 0));
+    md->graphSteps = count;
+    md->graphFirstSlot = slot0;
+    return MRMD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int64_t n, const double* pos3,
+                   const double* vel3, const double* mass)
+{
+    if (!ctx || !out || !cfg || !pos3 || !vel3 || n <= 0) return MRMD_ERR_ARG;
+    MRMD_CHECK_ARG(cfg->rc > 0 && cfg->skin >= 0 && cfg->dt > 0 && cfg->rebuildInterval >= 1, ctx, "bad config");
+    MRMD_CHECK_ARG(cfg->precision == MRMD_PREC_FP64 || cfg->precision == MRMD_PREC_MIXED, ctx, "bad precision");
+    MRMD_CHECK_ARG(n < INT32_MAX / 2, ctx, "too many atoms");
+    *out = nullptr;
+    mrmd_md* md = new mrmd_md();
+    md->cfg = *cfg;
+    if (md->cfg.maxNeighbors <= 0) md->cfg.maxNeighbors = md->cfg.precision == MRMD_PREC_MIXED ? 112 : 64;
+    md->n = n;
+    const double rlist = cfg->rc + cfg->skin;
+    const double ghost3[3] = {rlist, rlist, rlist};
+    int rc = mrmd_subdomain_init(&md->sd, cfg->boxMin, cfg->boxMax, ghost3);
+    for (int d = 0; d < 3 && rc == MRMD_OK; ++d)
+        if (!(md->sd.diameter[d] > rlist)) rc = set_error(ctx, MRMD_ERR_ARG, "box must exceed the list radius");
+    if (rc == MRMD_OK)
+    {
+        md->grid = make_grid(md->sd.minGhostCorner, md->sd.maxGhostCorner, rlist);
+        md->sp = split_params(md->sd.minGhostCorner, md->grid.extent * 1.25 + 8.0);
+    }
+    std::vector<double> m((size_t)n, 1.0);
+    if (mass)
+        for (int64_t i = 0; i < n; ++i) m[(size_t)i] = mass[i];
+    std::vector<int64_t> type((size_t)n, 0);
+    std::vector<double> rel((size_t)n, 1.0);
+    const int64_t cap = n + n / 2 + 1024;
+    if (rc == MRMD_OK) rc = mrmd_atoms_alloc(ctx, &md->atoms, cap);
+    if (rc == MRMD_OK)
+        rc = mrmd_atoms_upload(ctx, &md->atoms, n, 0, pos3, vel3, nullptr, type.data(), m.data(), nullptr, rel.data());
+    if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, &md->atoms, cap, 0.0);
+    if (rc == MRMD_OK) rc = mrmd_atoms_alloc(ctx, &md->shadow, cap);
+    if (rc == MRMD_OK) rc = mrmd_ghost_layer_alloc(ctx, &md->ghosts, cap);
+    if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->list);
+    if (rc == MRMD_OK)
+    {
+        const double c = cfg->cappingDistance, r = cfg->rc, s = cfg->sigma, e = cfg->epsilon;
+        rc = mrmd_lj_create(ctx, &md->lj, 1, 1, &c, &r, &s, &e, cfg->shifted);
+    }
+    if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->orig), sizeof(int32_t) * (size_t)n);
+    if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->origTmp), sizeof(int32_t) * (size_t)n);
+    if (rc == MRMD_OK)
+    {
+        k_iota<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(md->orig, n);
+        rc = after_launch(ctx, "iota");
+    }
+    if (rc == MRMD_OK) rc = ensure_energy(ctx, md, 1024);
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "md_create");
+    if (rc != MRMD_OK)
+    {
+        mrmd_md_destroy(ctx, md);
+        return rc;
+    }
+    *out = md;
+    return MRMD_OK;
+}
+
+int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md)
+{
+    if (!md) return MRMD_OK;
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    drop_graph(md);
+    mrmd_atoms_free(ctx, &md->atoms);
+    mrmd_atoms_free(ctx, &md->shadow);
+    mrmd_ghost_layer_free(ctx, &md->ghosts);
+    mrmd_nlist_free(ctx, &md->list);
+    mrmd_lj_destroy(ctx, md->lj);
+    md->sortCells.release();
+    dfree(md->orig);
+    dfree(md->origTmp);
+    dfree(md->split);
+    dfree(md->dEnergy);
+    if (md->hEnergy) cudaFreeHost(md->hEnergy);
+    delete md;
+    return MRMD_OK;
+}
+
+int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
+{
+    if (!ctx || !md || nsteps < 0) return MRMD_ERR_ARG;
+    if (nsteps == 0) return MRMD_OK;
+    MRMD_TRY(ensure_energy(ctx, md, nsteps));
+    const int oldSync = ctx->sync;
+    ctx->sync = 0;
+    int rc = check_cuda(ctx, cudaMemsetAsync(md->dEnergy, 0, sizeof(double) * 2 * (size_t)(nsteps + 1), ctx->stream),
+                        "energy clear");
+    mrmd_atoms* a = &md->atoms;
+    const int64_t K = md->cfg.rebuildInterval;
+    // make sure the force array holds F(x) before the first kick
+    if (rc == MRMD_OK && !md->forceValid)
+    {
+        rc = md_rebuild(ctx, md);
+        if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, a, a->numLocal + a->numGhost, 0.0);
+        if (rc == MRMD_OK) rc = md_forces(ctx, md, md->dEnergy + 2 * nsteps);  // scratch slot
+        md->forceValid = true;
+    }
+    int64_t s = 0;
+    while (rc == MRMD_OK && s < nsteps)
+    {
+        const int64_t global = md->steps + s;
+        if (md->needRebuild || global % K == 0)
+        {
+            // rebuild step, eager: kick/drift, rebuild, forces
+            k_fused_kick_drift<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(
+                reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
+                reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt,
+                global > 0 ? 1 : 0);
+            rc = after_launch(ctx, "fused_kick_drift");
+            if (rc == MRMD_OK) rc = md_rebuild(ctx, md);
+            if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, a, a->numLocal + a->numGhost, 0.0);
+            if (rc == MRMD_OK) rc = md_forces(ctx, md, md->dEnergy + 2 * s);
+            ++s;
+            // the steps up to the next rebuild, as one graph (or eagerly)
+            const int64_t nextRebuild = ((md->steps + s + K - 1) / K) * K;
+            int64_t count = nextRebuild - (md->steps + s);
+            if (count > nsteps - s) count = nsteps - s;
+            if (rc == MRMD_OK && count > 0)
+            {
+                if (md->cfg.useGraph && count == K - 1)
+                {
+                    rc = capture_steps(ctx, md, count, s);
+                    if (rc == MRMD_OK)
+                    {
+                        if (md->graphFirstSlot != s)
+                            rc = set_error(ctx, MRMD_ERR_STATE, "graph slot mismatch");
+                        else
+                            rc = check_cuda(ctx, cudaGraphLaunch(md->exec, ctx->stream), "graph launch");
+                        ctx->launches += count * 4;
+                    }
+                }
+                else
+                {
+                    for (int64_t k = 0; k < count && rc == MRMD_OK; ++k)
+                        rc = md_plain_step(ctx, md, md->dEnergy + 2 * (s + k), true);
+                }
+                s += count;
+            }
+        }
+        else
+        {
+            rc = md_plain_step(ctx, md, md->dEnergy + 2 * s, true);
+            ++s;
+        }
+    }
+    md->steps += s;
+    ctx->sync = oldSync;
+    if (rc != MRMD_OK) return rc;
+    // The stored velocities stay half-kicked: the post-kick of the last step
+    // is applied by the first fused kernel of the next run (and to a copy by
+    // mrmd_md_get_state).
+    if (energies)
+    {
+        MRMD_CUDA(ctx, cudaMemcpyAsync(md->hEnergy, md->dEnergy, sizeof(double) * 2 * (size_t)nsteps,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        std::memcpy(energies, md->hEnergy, sizeof(double) * 2 * (size_t)nsteps);
+    }
+    return finish(ctx, "md_run");
+}
+
+int mrmd_md_get_state(mrmd_ctx* ctx, mrmd_md* md, double* pos3, double* vel3, double* force3)
+{
+    // Velocities are reported at the end of the last full step: the pending
+    // post-kick of the last step is applied to a copy.
+    if (!ctx || !md) return MRMD_ERR_ARG;
+    mrmd_atoms* a = &md->atoms;
+    const int64_t n = md->n;
+    double* stage = static_cast<double*>(scratch(ctx, sizeof(double) * 3 * (size_t)n));
+    if (!stage) return MRMD_ERR_OOM;
+    double* hostOut[3] = {pos3, vel3, force3};
+    for (int w = 0; w < 3; ++w)
+    {
+        if (!hostOut[w]) continue;
+        const double* src = w == 0 ? a->pos : (w == 1 ? a->vel : a->force);
+        if (w == 1 && md->steps > 0)
+        {
+            // v(t) = v_half + dt/2 F(t)/m on the shadow velocity buffer
+            MRMD_CUDA(ctx, cudaMemcpyAsync(md->shadow.vel, a->vel, sizeof(double) * 4 * (size_t)n,
+                                           cudaMemcpyDeviceToDevice, ctx->stream));
+            k_post_kick<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<double4*>(md->shadow.vel),
+                                                                       reinterpret_cast<const double4*>(a->force),
+                                                                       a->mass, n, 0.5 * md->cfg.dt);
+            MRMD_TRY(after_launch(ctx, "post_kick"));
+            src = md->shadow.vel;
+        }
+        k_unpermute3<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(src), md->orig, n,
+                                                                    stage);
+        MRMD_TRY(after_launch(ctx, "unpermute"));
+        MRMD_CUDA(ctx, cudaMemcpyAsync(hostOut[w], stage, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return MRMD_OK;
+}
+
+int mrmd_md_set_state(mrmd_ctx* ctx, mrmd_md* md, const double* pos3, const double* vel3)
+{
+    if (!ctx || !md) return MRMD_ERR_ARG;
+    mrmd_atoms* a = &md->atoms;
+    const int64_t n = md->n;
+    double* stage = static_cast<double*>(scratch(ctx, sizeof(double) * 3 * (size_t)n));
+    if (!stage) return MRMD_ERR_OOM;
+    const double* in[2] = {pos3, vel3};
+    for (int w = 0; w < 2; ++w)
+    {
+        if (!in[w]) continue;
+        MRMD_CUDA(ctx, cudaMemcpyAsync(stage, in[w], sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        k_permute_in3<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(stage, md->orig, n,
+                                                                     reinterpret_cast<double4*>(w == 0 ? a->pos : a->vel));
+        MRMD_TRY(after_launch(ctx, "permute_in"));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    md->needRebuild = true;
+    md->forceValid = false;
+    md->steps = 0;
+    return MRMD_OK;
+}
+
+int mrmd_md_stats(const mrmd_md* md, int64_t* out5)
+{
+    if (!md || !out5) return MRMD_ERR_ARG;
+    out5[0] = md->steps;
+    out5[1] = md->rebuilds;
+    out5[2] = md->list.totalPairs;
+    out5[3] = md->atoms.numGhost;
+    out5[4] = md->list.maxNeighbors;
+    return MRMD_OK;
+}
+
+const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md) { return md ? &md->atoms : nullptr; }
+const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md) { return md ? &md->list : nullptr; }
+
+}  // extern "C"

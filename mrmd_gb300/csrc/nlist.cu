@@ -1,0 +1,516 @@
+// Linked cells and the half Verlet list (Cabana::LinkedCellList +
+// Cabana::VerletList<HalfNeighborTag, VerletLayout2D> as used by MRMD).
+//
+// Pair rule (Cabana 0.7, NeighborDiscriminator<HalfNeighborTag>): particle
+// j is a neighbour of i when j != i, |x_i - x_j|^2 <= r^2 and x_j is above
+// x_i in lexicographic (x, y, z) order.  Every test below decides exactly
+// the FP64 predicate: an FP32 prefilter settles the clear cases and the
+// FP64 positions decide everything inside the FP32 error band, so the pair
+// set is bit-identical to an all-FP64 build.
+//
+// Because x_j >= x_i implies cell_x(j) >= cell_x(i) (floor is monotone),
+// only the 9 + 9 cells with cell_x >= cell_x(i) can hold neighbours.
+#include <cmath>
+
+#include "common.cuh"
+#include "nlist_impl.cuh"
+
+using namespace mrmd_impl;
+
+namespace mrmd_impl
+{
+CellGrid make_grid(const double* gridMin, const double* gridMax, double delta)
+{
+    // n = max(1, floor(L / delta)) cells per axis, edge L / n >= delta
+    CellGrid g{};
+    double mn[3], rdx[3];
+    int n[3];
+    double extent = 0.0;
+    for (int d = 0; d < 3; ++d)
+    {
+        const double L = gridMax[d] - gridMin[d];
+        int64_t c = (int64_t)std::floor(L / delta);
+        if (c < 1) c = 1;
+        n[d] = (int)c;
+        mn[d] = gridMin[d];
+        rdx[d] = (double)c / L;
+        extent = std::fmax(extent, std::fmax(std::fabs(gridMin[d]), std::fabs(gridMax[d])));
+        extent = std::fmax(extent, L);
+    }
+    g.mn = make_double3(mn[0], mn[1], mn[2]);
+    g.rdx = make_double3(rdx[0], rdx[1], rdx[2]);
+    g.n = make_int3(n[0], n[1], n[2]);
+    g.ncell = (int64_t)n[0] * n[1] * n[2];
+    g.extent = extent;
+    return g;
+}
+
+__global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGrid g,
+                             int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int32_t c = cell_of(pos[i], g);
+        cellOf[i] = c;
+        atomicAdd(&cellCount[c], 1);
+    }
+}
+
+__global__ void k_cell_scatter(const int32_t* __restrict__ cellOf, int64_t n,
+                               const int32_t* __restrict__ cellStart, int32_t* __restrict__ cursor,
+                               int32_t* __restrict__ sorted)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int32_t c = cellOf[i];
+        sorted[cellStart[c] + atomicAdd(&cursor[c], 1)] = (int32_t)i;
+    }
+}
+
+// ascending particle index inside each cell (stable counting sort)
+__global__ void k_cell_sort(const int32_t* __restrict__ cellStart, int64_t ncell,
+                            int32_t* __restrict__ sorted)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
+         c += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int32_t s = cellStart[c], e = cellStart[c + 1];
+        for (int32_t a = s + 1; a < e; ++a)
+        {
+            const int32_t v = sorted[a];
+            int32_t b = a - 1;
+            while (b >= s && sorted[b] > v)
+            {
+                sorted[b + 1] = sorted[b];
+                --b;
+            }
+            sorted[b + 1] = v;
+        }
+    }
+}
+
+__global__ void k_cell_gather(const double4* __restrict__ pos, const int32_t* __restrict__ sorted,
+                              int64_t n, double3 origin, float4* __restrict__ spos)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int32_t j = sorted[s];
+        const double4 p = pos[j];
+        spos[s] = make_float4((float)(p.x - origin.x), (float)(p.y - origin.y), (float)(p.z - origin.z),
+                              __int_as_float(j));
+    }
+}
+
+__device__ __forceinline__ bool lex_above(const double4& pi, const double4& pj)
+{
+    return (pj.x > pi.x) || ((pj.x == pi.x) && ((pj.y > pi.y) || ((pj.y == pi.y) && (pj.z > pi.z))));
+}
+
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_build_list(
+    const double4* __restrict__ pos, const int32_t* __restrict__ cellOf,
+    const int32_t* __restrict__ cellStart, const float4* __restrict__ spos, CellGrid g,
+    int64_t begin, int64_t end, double rsq, float rsqLo, float rsqHi, int64_t stride, int64_t cap,
+    int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount)
+{
+    for (int64_t i = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < end;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const double4 pi = pos[i];
+        const float xi = (float)(pi.x - g.mn.x), yi = (float)(pi.y - g.mn.y), zi = (float)(pi.z - g.mn.z);
+        const int32_t ci = cellOf[i];
+        const int cz = ci % g.n.z;
+        const int cy = (ci / g.n.z) % g.n.y;
+        const int cx = ci / (g.n.z * g.n.y);
+        int32_t cnt = 0;
+        const int64_t row = i - begin;
+        const int axEnd = min(cx + 1, g.n.x - 1);
+        for (int ax = FULL ? max(cx - 1, 0) : cx; ax <= axEnd; ++ax)
+        {
+            for (int ay = max(cy - 1, 0); ay <= min(cy + 1, g.n.y - 1); ++ay)
+            {
+                for (int az = max(cz - 1, 0); az <= min(cz + 1, g.n.z - 1); ++az)
+                {
+                    const int32_t c = (ax * g.n.y + ay) * g.n.z + az;
+                    const int32_t s0 = cellStart[c], s1 = cellStart[c + 1];
+                    for (int32_t s = s0; s < s1; ++s)
+                    {
+                        const float4 q = spos[s];
+                        const int32_t j = __float_as_int(q.w);
+                        if (j == (int32_t)i) continue;
+                        // lexicographic (x, y, z): float order is exact unless equal
+                        if (!FULL && q.x < xi) continue;
+                        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                        const float d2f = dx * dx + dy * dy + dz * dz;
+                        if (d2f > rsqHi) continue;
+                        bool keep;
+                        if ((FULL || q.x > xi) && d2f < rsqLo)
+                        {
+                            keep = true;
+                        }
+                        else
+                        {
+                            const double4 pj = pos[j];
+                            const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+                            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
+                                                        __dmul_rn(ddz, ddz));
+                            keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
+                        }
+                        if (!keep) continue;
+                        if (cnt < cap) nbrs[(int64_t)cnt * stride + row] = j;
+                        ++cnt;
+                    }
+                }
+            }
+        }
+        counts[row] = cnt < cap ? cnt : (int32_t)cap;
+        if (cnt > cap) atomicMax(maxCount, cnt);
+    }
+}
+
+int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid)
+{
+    g = grid;
+    if (n > INT32_MAX || g.ncell > INT32_MAX) return set_error(ctx, MRMD_ERR_CAPACITY, "too many particles or cells");
+    if (n + 1 > capN)
+    {
+        dfree(cellOf);
+        dfree(sorted);
+        dfree(spos);
+        cellOf = sorted = nullptr;
+        spos = nullptr;
+        const int64_t c = n + n / 4 + 64;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&cellOf), sizeof(int32_t) * (size_t)c));
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&sorted), sizeof(int32_t) * (size_t)c));
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&spos), sizeof(float4) * (size_t)c));
+        capN = c;
+    }
+    if (g.ncell + 1 > capCells)
+    {
+        dfree(cellStart);
+        dfree(cursor);
+        cellStart = cursor = nullptr;
+        const int64_t c = g.ncell + 1;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&cellStart), sizeof(int32_t) * (size_t)c));
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&cursor), sizeof(int32_t) * (size_t)c));
+        capCells = c;
+    }
+    numParticles = n;
+    constexpr int TB = 256;
+    MRMD_CUDA(ctx, cudaMemsetAsync(cellStart, 0, sizeof(int32_t) * (size_t)(g.ncell + 1), ctx->stream));
+    MRMD_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)(g.ncell + 1), ctx->stream));
+    if (n > 0)
+    {
+        k_cell_count<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n,
+                                                                   g, cellOf, cellStart);
+        MRMD_TRY(after_launch(ctx, "cell_count"));
+    }
+    MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, g.ncell + 1, nullptr));
+    if (n > 0)
+    {
+        k_cell_scatter<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, n, cellStart, cursor, sorted);
+        MRMD_TRY(after_launch(ctx, "cell_scatter"));
+        k_cell_sort<<<grid_for(ctx, g.ncell, TB), TB, 0, ctx->stream>>>(cellStart, g.ncell, sorted);
+        MRMD_TRY(after_launch(ctx, "cell_sort"));
+        k_cell_gather<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4),
+                                                                    sorted, n, g.mn, spos);
+        MRMD_TRY(after_launch(ctx, "cell_gather"));
+    }
+    return MRMD_OK;
+}
+
+void CellList::release()
+{
+    dfree(cellOf);
+    dfree(sorted);
+    dfree(spos);
+    dfree(cellStart);
+    dfree(cursor);
+    cellOf = sorted = cellStart = cursor = nullptr;
+    spos = nullptr;
+    capN = capCells = 0;
+}
+
+static int ensure_list_storage(mrmd_ctx* ctx, mrmd_nlist* nl, int64_t rows, int64_t maxNeighbors)
+{
+    const int64_t stride = div_up(rows > 0 ? rows : 1, 32) * 32;
+    if (rows + 1 > nl->rowsCapacity)
+    {
+        dfree(nl->counts);
+        nl->counts = nullptr;
+        const int64_t c = rows + rows / 8 + 64;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&nl->counts), sizeof(int32_t) * (size_t)c));
+        nl->rowsCapacity = c;
+    }
+    const int64_t need = stride * maxNeighbors;
+    if (need > nl->nbrsCapacity)
+    {
+        dfree(nl->nbrs);
+        nl->nbrs = nullptr;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&nl->nbrs), sizeof(int32_t) * (size_t)need));
+        nl->nbrsCapacity = need;
+    }
+    nl->stride = stride;
+    nl->maxNeighbors = maxNeighbors;
+    return MRMD_OK;
+}
+
+int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t nPos, int64_t begin,
+                    int64_t end, double rlist, const CellGrid& grid, int64_t maxNeighbors, bool full)
+{
+    CellList* cl = static_cast<CellList*>(nl->cells);
+    MRMD_TRY(cl->build(ctx, pos4, nPos, grid));
+    const int64_t rows = end - begin;
+    // FP32 error band: coordinates are stored relative to the grid origin
+    // (|c| <= extent), each rounding error <= 2^-24 |c|, so |dx_f - dx| <=
+    // delta := 2^-22 extent and |d2_f - d2| <= 6 r delta + 3 delta^2 plus the
+    // FP32 rounding of the sum (< 2^-21 d2).
+    const double delta = std::ldexp(grid.extent, -22);
+    const double band = 6.0 * rlist * delta + 3.0 * delta * delta + std::ldexp(rlist * rlist, -20);
+    const double rsq = rlist * rlist;
+    const float rsqLo = (float)std::fmax(0.0, (rsq - 2.0 * band) * (1.0 - 1e-6));
+    const float rsqHi = (float)((rsq + 2.0 * band) * (1.0 + 1e-6));
+    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
+    int64_t cap = maxNeighbors > 0 ? maxNeighbors : 64;
+    for (int attempt = 0; attempt < 4; ++attempt)
+    {
+        MRMD_TRY(ensure_list_storage(ctx, nl, rows, cap));
+        MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, sizeof(int32_t), ctx->stream));
+        if (rows > 0)
+        {
+            if (full)
+                k_build_list<true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
+                    reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
+                    end, rsq, rsqLo, rsqHi, nl->stride, cap, nl->counts, nl->nbrs, maxCount);
+            else
+                k_build_list<false><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
+                    reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
+                    end, rsq, rsqLo, rsqHi, nl->stride, cap, nl->counts, nl->nbrs, maxCount);
+            MRMD_TRY(after_launch(ctx, "build_list"));
+        }
+        int32_t hMax = 0;
+        MRMD_CUDA(ctx, cudaMemcpyAsync(&hMax, maxCount, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hMax <= cap)
+        {
+            nl->rows = rows;
+            nl->begin = begin;
+            return MRMD_OK;
+        }
+        cap = hMax + hMax / 8 + 4;  // Cabana grows and rebuilds the same way
+    }
+    return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+}
+
+__global__ void k_count_sum(const int32_t* __restrict__ counts, int64_t n, unsigned long long* out)
+{
+    unsigned long long s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s += (unsigned long long)counts[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl)
+{
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(ctx->devScalars + 8);
+    MRMD_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+    if (nl->rows > 0)
+    {
+        k_count_sum<<<grid_for(ctx, nl->rows, 256, 4), 256, 0, ctx->stream>>>(nl->counts, nl->rows, d);
+        MRMD_TRY(after_launch(ctx, "count_sum"));
+    }
+    unsigned long long h = 0;
+    MRMD_CUDA(ctx, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    nl->totalPairs = (int64_t)h;
+    return MRMD_OK;
+}
+
+// ----------------------------------------------------------- permutation --
+
+template <typename T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const int32_t* __restrict__ perm,
+                         int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+__global__ void k_perm_out(const int32_t* __restrict__ perm, int64_t n, int64_t* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = perm[i];
+}
+
+int permute_atoms(mrmd_ctx* ctx, mrmd_atoms* a, mrmd_atoms* shadow, const int32_t* perm, int64_t n)
+{
+    // gather every field through perm into `shadow`, then swap storage
+    constexpr int TB = 256;
+    const unsigned gr = grid_for(ctx, n, TB);
+    k_gather<double4><<<gr, TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(a->pos),
+                                                  reinterpret_cast<double4*>(shadow->pos), perm, n);
+    k_gather<double4><<<gr, TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(a->vel),
+                                                  reinterpret_cast<double4*>(shadow->vel), perm, n);
+    k_gather<double4><<<gr, TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(a->force),
+                                                  reinterpret_cast<double4*>(shadow->force), perm, n);
+    k_gather<int32_t><<<gr, TB, 0, ctx->stream>>>(a->type, shadow->type, perm, n);
+    k_gather<double><<<gr, TB, 0, ctx->stream>>>(a->mass, shadow->mass, perm, n);
+    k_gather<double><<<gr, TB, 0, ctx->stream>>>(a->charge, shadow->charge, perm, n);
+    k_gather<double><<<gr, TB, 0, ctx->stream>>>(a->relativeMass, shadow->relativeMass, perm, n);
+    ctx->launches += 6;
+    MRMD_TRY(after_launch(ctx, "permute_gather"));
+    std::swap(a->pos, shadow->pos);
+    std::swap(a->vel, shadow->vel);
+    std::swap(a->force, shadow->force);
+    std::swap(a->type, shadow->type);
+    std::swap(a->mass, shadow->mass);
+    std::swap(a->charge, shadow->charge);
+    std::swap(a->relativeMass, shadow->relativeMass);
+    return MRMD_OK;
+}
+}  // namespace mrmd_impl
+
+extern "C" {
+
+int mrmd_nlist_init(mrmd_ctx* ctx, mrmd_nlist* nl)
+{
+    if (!ctx || !nl) return MRMD_ERR_ARG;
+    std::memset(nl, 0, sizeof(*nl));
+    nl->cells = new CellList();
+    return MRMD_OK;
+}
+
+int mrmd_nlist_free(mrmd_ctx* ctx, mrmd_nlist* nl)
+{
+    if (!nl) return MRMD_ERR_ARG;
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    dfree(nl->counts);
+    dfree(nl->nbrs);
+    if (nl->cells)
+    {
+        CellList* cl = static_cast<CellList*>(nl->cells);
+        cl->release();
+        delete cl;
+    }
+    std::memset(nl, 0, sizeof(*nl));
+    return MRMD_OK;
+}
+
+int mrmd_nlist_build(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t nPos, int64_t begin,
+                     int64_t end, double rlist, double cellRatio, const double* gridMin,
+                     const double* gridMax, int64_t maxNeighbors)
+{
+    if (!ctx || !nl || !nl->cells || !gridMin || !gridMax) return MRMD_ERR_ARG;
+    MRMD_CHECK_ARG(nPos >= 0 && begin >= 0 && begin <= end && end <= nPos, ctx, "bad particle range");
+    MRMD_CHECK_ARG(rlist > 0.0 && cellRatio > 0.0 && cellRatio <= 1.0, ctx, "bad cutoff or cell ratio");
+    if (nPos > 0) MRMD_CHECK_ARG(pos4 != nullptr, ctx, "null positions");
+    for (int d = 0; d < 3; ++d) MRMD_CHECK_ARG(gridMax[d] > gridMin[d], ctx, "empty grid");
+    // cells of edge >= rlist (cellRatio < 1 is accepted and rounded up to one
+    // list radius per cell, which keeps the 3-cell stencil exact)
+    CellGrid g = make_grid(gridMin, gridMax, rlist);
+    (void)cellRatio;
+    MRMD_TRY(build_half_list(ctx, nl, pos4, nPos, begin, end, rlist, g, maxNeighbors, false));
+    MRMD_TRY(list_total_pairs(ctx, nl));
+    return finish(ctx, "nlist_build");
+}
+
+int mrmd_nlist_download(mrmd_ctx* ctx, const mrmd_nlist* nl, int32_t* counts, int32_t* nbrs, int64_t cap)
+{
+    if (!ctx || !nl) return MRMD_ERR_ARG;
+    const int64_t rows = nl->rows;
+    if (rows == 0) return MRMD_OK;
+    std::vector<int32_t> c((size_t)rows);
+    MRMD_CUDA(ctx, cudaMemcpyAsync(c.data(), nl->counts, sizeof(int32_t) * (size_t)rows,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int32_t mx = 0;
+    for (auto v : c) mx = v > mx ? v : mx;
+    if (counts) std::memcpy(counts, c.data(), sizeof(int32_t) * (size_t)rows);
+    if (!nbrs) return MRMD_OK;
+    if (mx > cap) return set_error(ctx, MRMD_ERR_CAPACITY, "download capacity %lld < %d", (long long)cap, mx);
+    std::vector<int32_t> t((size_t)(nl->stride * mx));
+    if (mx > 0)
+    {
+        MRMD_CUDA(ctx, cudaMemcpyAsync(t.data(), nl->nbrs, sizeof(int32_t) * t.size(), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t k = 0; k < c[(size_t)i]; ++k) nbrs[i * cap + k] = t[(size_t)(k * nl->stride + i)];
+    return MRMD_OK;
+}
+
+int mrmd_cell_index(mrmd_ctx* ctx, const double* pos4, int64_t n, const double* gridMin,
+                    const double* gridMax, double delta, int64_t* cells_out)
+{
+    if (!ctx || !gridMin || !gridMax || !cells_out || delta <= 0) return MRMD_ERR_ARG;
+    if (n == 0) return MRMD_OK;
+    CellGrid g = make_grid(gridMin, gridMax, delta);
+    CellList cl;
+    int rc = cl.build(ctx, pos4, n, g);
+    std::vector<int32_t> c((size_t)n);
+    if (rc == MRMD_OK)
+        rc = check_cuda(ctx, cudaMemcpyAsync(c.data(), cl.cellOf, sizeof(int32_t) * (size_t)n,
+                                             cudaMemcpyDeviceToHost, ctx->stream), "cells");
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "cells");
+    cl.release();
+    if (rc != MRMD_OK) return rc;
+    for (int64_t i = 0; i < n; ++i) cells_out[i] = c[(size_t)i];
+    return MRMD_OK;
+}
+
+int mrmd_atoms_sort_by_cell(mrmd_ctx* ctx, mrmd_atoms* a, const double* gridMin, const double* gridMax,
+                            double delta, int64_t* perm_out)
+{
+    if (!ctx || !a || !gridMin || !gridMax || delta <= 0) return MRMD_ERR_ARG;
+    const int64_t n = a->numLocal;
+    if (n == 0) return MRMD_OK;
+    CellGrid g = make_grid(gridMin, gridMax, delta);
+    CellList cl;
+    int rc = cl.build(ctx, a->pos, n, g);
+    mrmd_atoms shadow{};
+    if (rc == MRMD_OK) rc = mrmd_atoms_alloc(ctx, &shadow, a->capacity);
+    if (rc == MRMD_OK)
+    {
+        // ghosts (if any) keep their slots: copy the tail unchanged
+        const int64_t tail = a->numGhost;
+        if (tail > 0)
+        {
+            cudaMemcpyAsync(shadow.pos + 4 * n, a->pos + 4 * n, sizeof(double) * 4 * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.vel + 4 * n, a->vel + 4 * n, sizeof(double) * 4 * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.force + 4 * n, a->force + 4 * n, sizeof(double) * 4 * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.type + n, a->type + n, sizeof(int32_t) * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.mass + n, a->mass + n, sizeof(double) * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.charge + n, a->charge + n, sizeof(double) * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(shadow.relativeMass + n, a->relativeMass + n, sizeof(double) * tail, cudaMemcpyDeviceToDevice, ctx->stream);
+        }
+        rc = permute_atoms(ctx, a, &shadow, cl.sorted, n);
+    }
+    if (rc == MRMD_OK && perm_out)
+    {
+        int64_t* d = nullptr;
+        rc = dmalloc(ctx, reinterpret_cast<void**>(&d), sizeof(int64_t) * (size_t)n);
+        if (rc == MRMD_OK)
+        {
+            k_perm_out<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(cl.sorted, n, d);
+            rc = after_launch(ctx, "perm_out");
+            if (rc == MRMD_OK)
+                rc = check_cuda(ctx, cudaMemcpyAsync(perm_out, d, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream), "perm");
+            cudaStreamSynchronize(ctx->stream);
+            dfree(d);
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    mrmd_atoms_free(ctx, &shadow);  // frees the old storage after the swap
+    cl.release();
+    return rc;
+}
+
+}  // extern "C"
