@@ -1,0 +1,420 @@
+"""Benchmark: atom-steps/s of the LJ NVE hot path on one GB300.
+
+Workload: 4,000,000-atom LJ fluid (fcc 100^3 cells, reduced density 0.8442,
+T* = 0.728 Maxwell-Boltzmann velocities from a seed, rc = 2.5 sigma shifted,
+skin 0.3 sigma, half/full Verlet list rebuilt every 10 steps, dt = 0.005),
+run in the plain FP64 form and in the mixed form.  `value` is the mixed
+form's atom-steps/s with the state resident in HBM; the FP64 form, the force
+error of the mixed form against FP64 on identical positions and the NVE
+drift of both are reported beside it.  `e2e` runs the same workload through
+the public stepper API from pinned host buffers (state upload, per-step
+energy read-back, final state download inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica (replicas
+only: the hot path has no exchange step) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s"
+WORKLOAD = "LJ fluid 4,000,000 atoms (fcc 100^3, rho 0.8442, T 0.728, rc 2.5 shifted, skin 0.3, rebuild/10, dt 0.005)"
+
+
+def fcc(cells, rho=0.8442):
+    a = (4.0 / rho) ** (1.0 / 3.0)
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(*[np.arange(cells)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pos = ((g[:, None, :] + base[None, :, :]).reshape(-1, 3) + 0.25) * a
+    return pos, a * cells
+
+
+def mb_velocities(n, T, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(0.0, np.sqrt(T), (n, 3))
+    v -= v.mean(0)
+    return v
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    """Bytes per atom of one pair-kernel launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
+            if parts.get("kernel") == kernel and "dram_bytes_per_atom" in parts:
+                return float(parts["dram_bytes_per_atom"])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    mx.append(float(c[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, c[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def kinetic(v, m=1.0):
+    return 0.5 * m * float((v * v).sum())
+
+
+def run_cpu(pos, vel, L, steps, warmup, budget_s, threads):
+    """The oracle (CPU restatement of the reference loop, OpenMP) on the same
+    workload: examples/02_LennardJones_NVE.cpp:135-216 with rebuild every 10."""
+    from oracle import oracle as O
+
+    O.set_threads(threads)
+    rc, skin, dt, K = 2.5, 0.3, 0.005, 10
+    n = len(pos)
+    sd = O.subdomain([0, 0, 0], [L] * 3, rc + skin)
+    a = O.Atoms.from_positions(pos, capacity=int(n * 1.3) + 1024)
+    a.vel[:n] = vel
+    tab = O.lj_table(0.0, rc, 1.0, 1.0, 1, True)
+    state = {}
+
+    def rebuild():
+        a.numGhost = 0
+        O.map_into_domain(a, sd)
+        state["corr"] = O.create_ghosts(a, sd)
+        state["list"] = O.build_half_list(a.pos, a.n, 0, a.numLocal, rc + skin, sd.minGhostCorner,
+                                          sd.maxGhostCorner, 1.0, 64)
+
+    def forces():
+        a.force[: a.n] = 0.0
+        co, no = state["list"]
+        E, W = O.lj_apply(tab, rc * rc, a, co, no)
+        O.ghost_to_real(a, state["corr"])
+        return E
+
+    rebuild()
+    forces()
+
+    def step(s):
+        O.vv_pre(a, dt)
+        if s % K == 0:
+            rebuild()
+        else:
+            O.update_ghosts(a, state["corr"], sd)
+        forces()
+        O.vv_post(a, dt)
+
+    t0 = time.perf_counter()
+    s = 0
+    while s < warmup and time.perf_counter() - t0 < budget_s / 4:
+        step(s)
+        s += 1
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        step(s)
+        s += 1
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dtime = time.perf_counter() - t0
+    return n * done / dtime, done, dtime
+
+
+def cpu_info():
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                model = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return os.cpu_count() or 1, model
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build()
+    cells = args.cells
+    pos, L = fcc(cells)
+    vel = mb_velocities(len(pos), 0.728, 0)
+    ncores, model = cpu_info()
+    value, done, dtime = run_cpu(pos, vel, L, args.steps, args.warmup, args.cpu_budget, ncores)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * dtime / max(done, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
+        "config": {"workload": WORKLOAD, "atoms": len(pos), "form": "FP64 half list, OpenMP atomics",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": ncores, "kind": "port",
+                         "sample": f"{done} steps of the {len(pos)}-atom system on {ncores} threads ({model}); "
+                                   "CPU restatement of the reference (Kokkos/Cabana not buildable here)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_run(torch, M, sysm, steps, stream):
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sysm.ctx.sync()
+    l0 = sysm.ctx.launches
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    e = sysm.run(steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    wall = time.perf_counter() - t0
+    return ev0.elapsed_time(ev1), wall, e, sysm.ctx.launches - l0
+
+
+def time_pair_kernel(torch, sysm, stream, reps=20):
+    sysm.eval_forces()
+    for _ in range(3):
+        sysm.launch_pair_kernel()
+    sysm.ctx.sync()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        sysm.launch_pair_kernel()
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1) / reps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")
+    ap.add_argument("--forms", default="fp64,mixed")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    import mrmd_gb300 as M
+
+    ctx = M.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    pos, L = fcc(args.cells)
+    n = len(pos)
+    vel = mb_velocities(n, 0.728, 1000 + rank)
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    res = {}
+    systems = {}
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for form in forms:
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        sysm = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, ctx=ctx)
+        sysm.run(args.warmup)
+        barrier()
+        _, v0, _ = sysm.state()
+        with ClockSampler(local_rank) as clk:
+            ms, wall, e, launches = time_run(torch, M, sysm, args.steps, stream)
+        _, v1, _ = sysm.state()
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        # NVE drift: total energy at the end of the first and last timed step
+        e_start = e[0, 0] + kinetic(v0)
+        e_end = e[-1, 0] + kinetic(v1)
+        tau = args.steps * 0.005
+        res[form] = dict(ms=ms, wall=wall, launches=launches,
+                         value=n * args.steps * world / (ms * 1e-3),
+                         drift=(e_end - e_start) / n / tau * 1000.0,
+                         clocks=clk.summary(), stats=sysm.stats())
+        systems[form] = sysm
+
+    head = "mixed" if "mixed" in res else forms[0]
+    sysm = systems[head]
+
+    # force error of the mixed form against FP64 on identical positions
+    ferr = None
+    if "mixed" in systems and "fp64" in systems:
+        p, v, _ = systems["fp64"].state()
+        systems["mixed"].set_state(p, v)
+        systems["fp64"].set_state(p, v)
+        systems["mixed"].eval_forces()
+        systems["fp64"].eval_forces()
+        _, _, fm = systems["mixed"].state()
+        _, _, fr = systems["fp64"].state()
+        d = np.linalg.norm(fm - fr, axis=1)
+        mag = np.linalg.norm(fr, axis=1)
+        rms = float(np.sqrt((mag ** 2).mean()))
+        ferr = {"max_abs_over_rms": float(d.max() / rms), "rms_over_rms": float(np.sqrt((d ** 2).mean()) / rms),
+                "max_per_atom_relative": float((d / np.maximum(mag, 1e-300)).max()),
+                "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
+
+    # the pair kernel alone (dominant kernel) for the roofline
+    kern_ms = time_pair_kernel(torch, sysm, stream)
+    st = sysm.stats()
+    nbar = st["pairs"] / n
+    if head == "mixed":
+        bytes_per_atom = 32 + 24 + 4 * (1 + nbar)  # split coords read, F written, full list
+        kname = "lj_mixed_full"
+    else:
+        bytes_per_atom = 24 + 24 + 4 * (1 + nbar)  # SURVEY 8(d) pair formula
+        kname = "lj_fp64"
+    peak, peak_kind = load_peaks()
+    achieved = bytes_per_atom * n / (kern_ms * 1e-3) / 1e9
+    tpa = load_traffic(kname)
+
+    # end to end through the public API with pinned host buffers
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hp, hv = pin(pos), pin(vel)
+    outs = [pin(np.zeros((n, 3))) for _ in range(3)]
+    prec = M.PREC_MIXED if head == "mixed" else M.PREC_FP64
+    e2e_sys = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, ctx=ctx)
+    e2e_sys.run(args.warmup)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_sys.set_state(hp, hv)
+    e2e_sys.run(args.steps)
+    e2e_sys.state(out=outs)
+    e2e_wall = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_wall], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_wall = float(t.item())
+    e2e_value = n * args.steps * world / e2e_wall
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ncores, model = cpu_info()
+        cv, done, ctime = run_cpu(pos, vel, L, 10 ** 6, 3, args.cpu_budget, ncores)
+        cpu = {"value": cv, "unit": METRIC, "cores": ncores, "kind": "port",
+               "sample": f"{done} steps of the {n}-atom system after 3 warm-up steps, {ncores} OpenMP threads "
+                         f"({model}); CPU restatement of the reference loop"}
+
+    if rank != 0:
+        return
+    r = res[head]
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 state, f32 double-float pair arithmetic" if head == "mixed" else "f64",
+        "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
+        "config": {"workload": WORKLOAD, "atoms": n, "form": head, "l2": "inputs larger than L2 (no flush needed)",
+                   "list_pairs": st["pairs"], "ghosts": st["ghosts"],
+                   "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
+                                 "nve_drift_per_atom_per_1000tau": res[f]["drift"],
+                                 "kernel_launches": res[f]["launches"]} for f in res},
+                   "mixed_over_fp64": (res["mixed"]["value"] / res["fp64"]["value"]) if {"mixed", "fp64"} <= res.keys() else None,
+                   "force_error_mixed_vs_fp64": ferr},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(48 * n / args.steps),
+                "d2h_bytes_per_step": int(16 + 72 * n / args.steps)},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "kernel_ms": kern_ms,
+                     "algorithmic_bytes_per_atom": bytes_per_atom,
+                     "traffic": (tpa * n) if tpa is not None else None},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

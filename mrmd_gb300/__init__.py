@@ -651,8 +651,12 @@ class LJSystem:
         self.ctx.check(self.ctx.lib.mrmd_md_run(self.ctx.h, self.h, int(nsteps), _dp(e)), "run")
         return e[:nsteps] if energies else None
 
-    def state(self):
-        p, v, f = (np.zeros((self.n, 3)) for _ in range(3))
+    def state(self, out=None):
+        """(pos, vel, force) in the original atom order; `out` may supply three
+        C-contiguous float64 [n, 3] arrays (e.g. pinned) to fill."""
+        p, v, f = out if out is not None else (np.zeros((self.n, 3)) for _ in range(3))
+        for a in (p, v, f):
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == (self.n, 3)
         self.ctx.check(self.ctx.lib.mrmd_md_get_state(self.ctx.h, self.h, _dp(p), _dp(v), _dp(f)),
                        "state")
         return p, v, f
@@ -660,6 +664,16 @@ class LJSystem:
     def set_state(self, pos, vel):
         self.ctx.check(self.ctx.lib.mrmd_md_set_state(self.ctx.h, self.h, _dp(_f64(pos)),
                                                       _dp(_f64(vel))), "set_state")
+
+    def eval_forces(self):
+        """Forces of the current positions; returns (energy, virial)."""
+        ev = np.zeros(2)
+        self.ctx.check(self.ctx.lib.mrmd_md_eval(self.ctx.h, self.h, 0, _dp(ev)), "eval")
+        return float(ev[0]), float(ev[1])
+
+    def launch_pair_kernel(self):
+        """Enqueue the pair-force kernel alone (asynchronous; for timing)."""
+        self.ctx.check(self.ctx.lib.mrmd_md_eval(self.ctx.h, self.h, 1, None), "pair kernel")
 
     def stats(self):
         out = np.zeros(5, dtype=np.int64)

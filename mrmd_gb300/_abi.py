@@ -173,6 +173,7 @@ SIGNATURES = {
     "mrmd_md_get_state": (_i, [_v, _v, c_double_p, c_double_p, c_double_p]),
     "mrmd_md_set_state": (_i, [_v, _v, c_double_p, c_double_p]),
     "mrmd_md_stats": (_i, [_v, c_int64_p]),
+    "mrmd_md_eval": (_i, [_v, _v, _i, c_double_p]),
     "mrmd_md_atoms": (P(AtomsS), [_v]),
     "mrmd_md_nlist": (P(NListS), [_v]),
 }

@@ -54,22 +54,44 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
+CPP_INCLUDE = os.path.join(PKG, "cpp", "include")
+CPP_EXAMPLES = os.path.join(PKG, "cpp", "examples")
+
+
+def build_examples() -> list[str]:
+    """Compile the C++ drivers written against the drop-in headers."""
+    outs = []
+    for src in sorted(glob.glob(os.path.join(CPP_EXAMPLES, "*.cpp"))):
+        exe = os.path.join(OBJ, os.path.basename(src)[:-4])
+        deps = [src, LIB] + glob.glob(os.path.join(CPP_INCLUDE, "**", "*.hpp"), recursive=True)
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+            outs.append(exe)
+            continue
+        cmd = ["g++", "-O2", "-std=c++20", "-Wall", f"-I{INCLUDE}", f"-I{CPP_INCLUDE}", src, "-o", exe,
+               f"-L{PKG}", "-lmrmd_gb300", f"-Wl,-rpath,{PKG}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed for {src}:\n{r.stdout}\n{r.stderr}")
+        outs.append(exe)
+    return outs
+
+
 def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     os.makedirs(OBJ, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     extra = list(extra or [])
     with cf.ThreadPoolExecutor(max_workers=min(16, len(sources))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), sources))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs) and not extra:
-        return LIB
-    tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    if verbose:
-        print(f"built {LIB}")
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)) or extra:
+        tmp = LIB + ".tmp"
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+        if verbose:
+            print(f"built {LIB}")
+    build_examples()
     return LIB
 
 

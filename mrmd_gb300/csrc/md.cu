@@ -126,6 +126,7 @@ struct mrmd_md
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t graphSteps = 0;      // steps captured in exec
+    int64_t graphLaunches = 0;   // kernels per graph replay
     int64_t graphFirstSlot = -1; // energy slot of the first captured step
 };
 
@@ -235,8 +236,12 @@ int capture_steps(mrmd_ctx* ctx, mrmd_md* md, int64_t count, int64_t slot0)
     ctx->sync = 0;
     MRMD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = MRMD_OK;
+    const int64_t launches0 = ctx->launches;
     for (int64_t k = 0; k < count && rc == MRMD_OK; ++k) rc = md_plain_step(ctx, md, md->dEnergy + 2 * (slot0 + k), true);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    // captured kernels run when the graph is launched: count them there
+    md->graphLaunches = ctx->launches - launches0;
+    ctx->launches = launches0;
     ctx->sync = oldSync;
     if (rc != MRMD_OK)
     {
@@ -395,7 +400,7 @@ int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
                             rc = set_error(ctx, MRMD_ERR_STATE, "graph slot mismatch");
                         else
                             rc = check_cuda(ctx, cudaGraphLaunch(md->exec, ctx->stream), "graph launch");
-                        ctx->launches += count * 4;
+                        ctx->launches += md->graphLaunches;
                     }
                 }
                 else
@@ -495,6 +500,40 @@ int mrmd_md_stats(const mrmd_md* md, int64_t* out5)
     out5[2] = md->list.totalPairs;
     out5[3] = md->atoms.numGhost;
     out5[4] = md->list.maxNeighbors;
+    return MRMD_OK;
+}
+
+int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
+{
+    if (!ctx || !md || (what != 0 && what != 1)) return MRMD_ERR_ARG;
+    mrmd_atoms* a = &md->atoms;
+    MRMD_TRY(ensure_energy(ctx, md, 1));
+    double* ev = md->dEnergy + 2 * (md->energyCap - 1);
+    if (what == 1)
+    {
+        if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
+        if (md->cfg.precision == MRMD_PREC_MIXED)
+            return lj_mixed_full(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
+                                 &md->list, ev, false);
+        return lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev);
+    }
+    const int oldSync = ctx->sync;
+    ctx->sync = 0;
+    int rc = MRMD_OK;
+    if (md->needRebuild || !md->forceValid) rc = md_rebuild(ctx, md);
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaMemsetAsync(ev, 0, 2 * sizeof(double), ctx->stream), "ev");
+    if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, a, a->numLocal + a->numGhost, 0.0);
+    if (rc == MRMD_OK) rc = md_forces(ctx, md, ev);
+    ctx->sync = oldSync;
+    MRMD_TRY(rc);
+    md->forceValid = true;
+    MRMD_CUDA(ctx, cudaMemcpyAsync(ctx->hostScalars + 40, ev, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ev2)
+    {
+        ev2[0] = ctx->hostScalars[40];
+        ev2[1] = ctx->hostScalars[41];
+    }
     return MRMD_OK;
 }
 
