@@ -304,7 +304,7 @@ def main():
     for form in forms:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
         sysm = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, ctx=ctx)
-        sysm.run(args.warmup)
+        ew = sysm.run(args.warmup)
         barrier()
         _, v0, _ = sysm.state()
         with ClockSampler(local_rank) as clk:
@@ -314,8 +314,9 @@ def main():
             t = torch.tensor([ms], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
-        # NVE drift: total energy at the end of the first and last timed step
-        e_start = e[0, 0] + kinetic(v0)
+        # NVE drift over the timed steps: potential energy of the last step of
+        # each run with the full-step velocities of the same positions
+        e_start = ew[-1, 0] + kinetic(v0)
         e_end = e[-1, 0] + kinetic(v1)
         tau = args.steps * 0.005
         res[form] = dict(ms=ms, wall=wall, launches=launches,

@@ -148,7 +148,7 @@ struct LJIGArgs
     const LJDev* table;
     int32_t numTypes;
     double rcSqr;
-    float rcSqrf;
+    RcSq rc2;
     int32_t sampling;
     double* compEnergy;   // [200][numTypes]
     double* compCounter;  // [200][numTypes]
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(128) k_ljig(LJIGArgs A)
                     {
                         float fff, ef, r2h;
                         float3 d;
-                        if (!pair_mixed(A.hi[idx], A.lo[idx], A.hi[jdx], A.lo[jdx], p, A.rcSqrf, fff, ef, r2h, d))
+                        if (!pair_mixed(A.hi[idx], A.lo[idx], A.hi[jdx], A.lo[jdx], p, A.rc2, fff, ef, r2h, d))
                             continue;
                         ff = fff;
                         e = ef;
@@ -408,7 +408,7 @@ int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nli
     A.table = s->dTable;
     A.numTypes = (int32_t)s->numTypes;
     A.rcSqr = s->rcSqr;
-    A.rcSqrf = (float)s->rcSqr;
+    A.rc2 = make_rcsq(s->rcSqr);
     A.sampling = sampling;
     A.compEnergy = s->comp;
     A.compCounter = s->comp + nb;

@@ -69,7 +69,7 @@ constexpr int MX_TB = 128;
 template <bool PRED>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
-    double* __restrict__ force, const LJDev p, float rcSqrf, const int32_t* __restrict__ counts,
+    double* __restrict__ force, const LJDev p, RcSq rc2, const int32_t* __restrict__ counts,
     const int32_t* __restrict__ nbrs, int64_t stride, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
             const float4 hj = __ldg(hi + j), lj = __ldg(lo + j);
             float ff, e, r2h;
             float3 d;
-            if (!pair_mixed(hi_i, lo_i, hj, lj, p, rcSqrf, ff, e, r2h, d)) continue;
+            if (!pair_mixed(hi_i, lo_i, hj, lj, p, rc2, ff, e, r2h, d)) continue;
             df_acc(eAcc, e);
             df_acc(wAcc, -0.5f * ff * r2h);
             const float gx = d.x * ff, gy = d.y * ff, gz = d.z * ff;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
 template <bool ACCUM>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
     const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
-    float rcSqrf, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t stride, int64_t n,
+    RcSq rc2, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t stride, int64_t n,
     double* __restrict__ ev)
 {
     __shared__ double red[64];
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
             const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
             float ff, e, r2h;
             float3 d;
-            if (pair_mixed(hi_i, lo_i, h0, l0, p, rcSqrf, ff, e, r2h, d))
+            if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, ff, e, r2h, d))
             {
                 df_acc(eAcc, e);
                 df_acc(wAcc, -0.5f * ff * r2h);
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
                 df_acc(fy, d.y * ff);
                 df_acc(fz, d.z * ff);
             }
-            if (pair_mixed(hi_i, lo_i, h1, l1, p, rcSqrf, ff, e, r2h, d))
+            if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, ff, e, r2h, d))
             {
                 df_acc(eAcc, e);
                 df_acc(wAcc, -0.5f * ff * r2h);
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
             const int32_t j0 = __ldg(col + (int64_t)k * stride);
             float ff, e, r2h;
             float3 d;
-            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rcSqrf, ff, e, r2h, d))
+            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rc2, ff, e, r2h, d))
             {
                 df_acc(eAcc, e);
                 df_acc(wAcc, -0.5f * ff * r2h);
@@ -204,10 +204,10 @@ int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* for
     const unsigned grid = (unsigned)div_up(n, MX_TB);
     if (accumulate)
         k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
-                                                              (float)rcSqr, nl->counts, nl->nbrs, nl->stride, n, ev);
+                                                              make_rcsq(rcSqr), nl->counts, nl->nbrs, nl->stride, n, ev);
     else
         k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
-                                                               (float)rcSqr, nl->counts, nl->nbrs, nl->stride, n, ev);
+                                                               make_rcsq(rcSqr), nl->counts, nl->nbrs, nl->stride, n, ev);
     return after_launch(ctx, "lj_mixed_full");
 }
 
@@ -229,14 +229,14 @@ int lj_apply_mixed(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_n
     const bool usePred = pred != nullptr && pred->kind != MRMD_PRED_ALWAYS;
     const unsigned grid = (unsigned)div_up(n, MX_TB);
     const mrmd_dev::Pred dp = to_dev_pred(pred);
-    const float rcSqrf = (float)lj->rcSqr;
+    const RcSq rc2 = make_rcsq(lj->rcSqr);
     if (usePred)
         k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
-                                                               a->force, lj->p0, rcSqrf, nl->counts, nl->nbrs,
+                                                               a->force, lj->p0, rc2, nl->counts, nl->nbrs,
                                                                nl->stride, n, dp, ev);
     else
         k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
-                                                                a->force, lj->p0, rcSqrf, nl->counts, nl->nbrs,
+                                                                a->force, lj->p0, rc2, nl->counts, nl->nbrs,
                                                                 nl->stride, n, dp, ev);
     return after_launch(ctx, "lj_mixed_half");
 }

@@ -29,16 +29,33 @@ int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams
 int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
                   const mrmd_nlist* nl, double* ev, bool accumulate);
 
+// rc^2 as a double-float, so that the cutoff test decides on the full
+// ~2^-48 accurate r^2: the LJ force jumps at rc (the shifted potential is
+// continuous, its force is not), and an FP32-rounded test would misplace
+// the pairs within 2^-24 of rc^2.
+struct RcSq
+{
+    float h, l;
+};
+
+inline RcSq make_rcsq(double rcSqr)
+{
+    RcSq r;
+    r.h = (float)rcSqr;
+    r.l = (float)(rcSqr - (double)r.h);
+    return r;
+}
+
 // One pair in the mixed form.  Returns false when outside the cutoff.
 // ff: force factor (F_i = d * ff), e: pair energy, r2h: FP32 r^2, d: FP32 dx.
 __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_i, const float4& hj, const float4& lj,
-                                           const LJDev& p, float rcSqrf, float& ff, float& e, float& r2h, float3& d)
+                                           const LJDev& p, RcSq rc2, float& ff, float& e, float& r2h, float3& d)
 {
     const df dx = fast_two_sum(hi_i.x - hj.x, lo_i.x - lj.x);
     const df dy = fast_two_sum(hi_i.y - hj.y, lo_i.y - lj.y);
     const df dz = fast_two_sum(hi_i.z - hj.z, lo_i.z - lj.z);
     const df r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-    if (r2.h > rcSqrf) return false;
+    if (r2.h > rc2.h || (r2.h == rc2.h && r2.l > rc2.l)) return false;  // distSqr > rcSqr
     r2h = r2.h;
     d = make_float3(dx.h, dy.h, dz.h);
     if (r2.h >= p.capSqrf)

@@ -157,6 +157,7 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
     const double rlist = md->cfg.rc + md->cfg.skin;
     MRMD_TRY(build_half_list(ctx, &md->list, a->pos, nAll, 0, a->numLocal, rlist, md->grid,
                              md->list.maxNeighbors > 0 ? md->list.maxNeighbors : md->cfg.maxNeighbors, full));
+    MRMD_TRY(list_total_pairs(ctx, &md->list));
     if (full && nAll > md->splitCap)
     {
         dfree(md->split);

@@ -136,6 +136,8 @@ def test_multires_ghosts_bit_exact(M, orc):
         sdg = M.Subdomain([0, 0, 0], list(box), rc + skin)
         gl.createGhostAtoms(m, a, sdg)
         assert m.numGhostMolecules == mo.numGhost and a.numGhostAtoms == ao.numGhost
+        # the oracle fixture recomputes every centre of mass after ghost creation
+        M.UpdateMolecules.update(m, a, M.Slab([box[0] / 2, box[1] / 2, box[2] / 2], 10.0, 5.0, 1))
         d = m.download()
         np.testing.assert_array_equal(d["pos"], mo.pos[: mo.numLocal + mo.numGhost])
         np.testing.assert_array_equal(d["atomsOffset"], mo.atomsOffset[: mo.numLocal + mo.numGhost])

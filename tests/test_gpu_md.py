@@ -104,6 +104,25 @@ def test_mixed_stepper_is_deterministic_and_graph_invariant(M):
         np.testing.assert_allclose(e, runs[0][0], rtol=1e-13)
 
 
+def test_mixed_cutoff_decision_at_scale(M):
+    """256,000 atoms (~20M list pairs): the mixed form must place pairs at the
+    cutoff exactly as FP64 does (the shifted LJ force jumps at rc)."""
+    pos, L = fcc(40)
+    rng = np.random.default_rng(7)
+    pos = pos + rng.normal(0, 0.1, pos.shape)
+    vel = mb_velocities(len(pos), 0.728, 4)
+    ref = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64)
+    mix = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED)
+    ref.eval_forces()
+    mix.eval_forces()
+    fr = ref.state()[2]
+    fm = mix.state()[2]
+    rms = np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean())
+    err = np.linalg.norm(fm - fr, axis=1).max() / rms
+    assert err < 1e-6, err
+    assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
+
+
 def test_mixed_vs_fp64_forces_and_drift(M):
     pos, L = fcc(8)  # 2048 atoms
     vel = mb_velocities(len(pos), 0.728, 3)
