@@ -196,15 +196,13 @@ __global__ void __launch_bounds__(128) k_ljig(LJIGArgs A)
                     double ff, e, dx, dy, dz;
                     if (MIXED)
                     {
-                        float fff, ef, r2h;
-                        float3 d;
-                        if (!pair_mixed(A.hi[idx], A.lo[idx], A.hi[jdx], A.lo[jdx], p, A.rc2, fff, ef, r2h, d))
-                            continue;
-                        ff = fff;
-                        e = ef;
-                        dx = d.x;
-                        dy = d.y;
-                        dz = d.z;
+                        PairMixed q;
+                        if (!pair_mixed(A.hi[idx], A.lo[idx], A.hi[jdx], A.lo[jdx], p, A.rc2, q)) continue;
+                        ff = (double)q.ff.h + (double)q.ff.l;
+                        e = q.e;
+                        dx = (double)q.dh.x + (double)q.dl.x;
+                        dy = (double)q.dh.y + (double)q.dl.y;
+                        dz = (double)q.dh.z + (double)q.dl.z;
                     }
                     else
                     {

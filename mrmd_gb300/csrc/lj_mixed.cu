@@ -6,13 +6,13 @@
 //   lo = float(c - hi),
 // so every hi is an integer multiple of 2^-q below 2^24 * 2^-q: the FP32
 // difference hi_i - hi_j is exact, and dx = (hi_i - hi_j) + (lo_i - lo_j)
-// carries ~2^-40 absolute accuracy.  r^2, 1/r^2 and the force factor are
-// evaluated in double-float (pairs of FP32) because the LJ force factor
-// amplifies a relative error of r^2 sevenfold (F ~ r^-14); the result is
-// rounded once to FP32.  All of this runs on the FP32 pipe.  Energy and
-// virial use FP32 terms, summed with compensated FP32 per thread and FP64
-// across threads; the i-force is a compensated FP32 sum added to the FP64
-// force array, and the j-force of the half list goes out as FP64 atomics.
+// carries ~2^-40 absolute accuracy.  r^2, 1/r^2, the force factor and the
+// force products are evaluated in double-float (pairs of FP32), because the
+// LJ force factor amplifies a relative error of r^2 sevenfold (F ~ r^-14) and
+// single pair forces can exceed the atom's net force by orders of magnitude;
+// the per-atom sums are compensated double-float.  All of this runs on the
+// FP32 pipe.  Energy and virial use FP32 terms, summed with compensated FP32
+// per thread and FP64 across threads.
 #include <cmath>
 
 #include "common.cuh"
@@ -66,6 +66,20 @@ namespace
 {
 constexpr int MX_TB = 128;
 
+struct Acc
+{
+    df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, e{0.f, 0.f}, w{0.f, 0.f};
+
+    __device__ __forceinline__ void add(const PairMixed& q)
+    {
+        df_acc_prod(fx, q.dh.x, q.dl.x, q.ff);
+        df_acc_prod(fy, q.dh.y, q.dl.y, q.ff);
+        df_acc_prod(fz, q.dh.z, q.dl.z, q.ff);
+        df_acc(e, q.e);
+        df_acc(w, -0.5f * q.ff.h * q.r2h);
+    }
+};
+
 template <bool PRED>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
@@ -73,14 +87,13 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const int32_t* __restrict__ nbrs, int64_t stride, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
-    df eAcc{0.f, 0.f}, wAcc{0.f, 0.f};
+    Acc acc;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n)
     {
         const float4 hi_i = hi[i], lo_i = lo[i];
         double4 pi;
         if (PRED) pi = pos[i];
-        df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
         const int32_t cnt = counts[i];
         const int32_t* __restrict__ col = nbrs + i;
         for (int32_t k = 0; k < cnt; ++k)
@@ -91,25 +104,18 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
                 const double4 pj = mrmd_dev::ldg4(pos + j);
                 if (!mrmd_dev::pred2(pred, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z)) continue;
             }
-            const float4 hj = __ldg(hi + j), lj = __ldg(lo + j);
-            float ff, e, r2h;
-            float3 d;
-            if (!pair_mixed(hi_i, lo_i, hj, lj, p, rc2, ff, e, r2h, d)) continue;
-            df_acc(eAcc, e);
-            df_acc(wAcc, -0.5f * ff * r2h);
-            const float gx = d.x * ff, gy = d.y * ff, gz = d.z * ff;
-            df_acc(fx, gx);
-            df_acc(fy, gy);
-            df_acc(fz, gz);
-            atomicAdd(force + 4 * (int64_t)j + 0, -(double)gx);
-            atomicAdd(force + 4 * (int64_t)j + 1, -(double)gy);
-            atomicAdd(force + 4 * (int64_t)j + 2, -(double)gz);
+            PairMixed q;
+            if (!pair_mixed(hi_i, lo_i, __ldg(hi + j), __ldg(lo + j), p, rc2, q)) continue;
+            acc.add(q);
+            atomicAdd(force + 4 * (int64_t)j + 0, -prod_d(q.dh.x, q.dl.x, q.ff));
+            atomicAdd(force + 4 * (int64_t)j + 1, -prod_d(q.dh.y, q.dl.y, q.ff));
+            atomicAdd(force + 4 * (int64_t)j + 2, -prod_d(q.dh.z, q.dl.z, q.ff));
         }
-        atomicAdd(force + 4 * i + 0, (double)fx.h + (double)fx.l);
-        atomicAdd(force + 4 * i + 1, (double)fy.h + (double)fy.l);
-        atomicAdd(force + 4 * i + 2, (double)fz.h + (double)fz.l);
+        atomicAdd(force + 4 * i + 0, (double)acc.fx.h + (double)acc.fx.l);
+        atomicAdd(force + 4 * i + 1, (double)acc.fy.h + (double)acc.fy.l);
+        atomicAdd(force + 4 * i + 2, (double)acc.fz.h + (double)acc.fz.l);
     }
-    double e = (double)eAcc.h + (double)eAcc.l, w = (double)wAcc.h + (double)wAcc.l;
+    double e = (double)acc.e.h + (double)acc.e.l, w = (double)acc.w.h + (double)acc.w.l;
     mrmd_dev::block_sum2(e, w, red);
     if (threadIdx.x == 0)
     {
@@ -117,6 +123,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
         atomicAdd(ev + 1, w);
     }
 }
+
 // Full-list form: every pair is evaluated from both sides, each thread owns
 // its atom's force (no atomics, deterministic) and ghosts receive nothing,
 // so no ghost force fold-back is needed.  Energy and virial are halved.
@@ -127,12 +134,11 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
     double* __restrict__ ev)
 {
     __shared__ double red[64];
-    df eAcc{0.f, 0.f}, wAcc{0.f, 0.f};
+    Acc acc;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n)
     {
         const float4 hi_i = hi[i], lo_i = lo[i];
-        df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
         const int32_t cnt = counts[i];
         const int32_t* __restrict__ col = nbrs + i;
         int32_t k = 0;
@@ -142,41 +148,18 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
             const int32_t j1 = __ldg(col + (int64_t)(k + 1) * stride);
             const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
             const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
-            float ff, e, r2h;
-            float3 d;
-            if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, ff, e, r2h, d))
-            {
-                df_acc(eAcc, e);
-                df_acc(wAcc, -0.5f * ff * r2h);
-                df_acc(fx, d.x * ff);
-                df_acc(fy, d.y * ff);
-                df_acc(fz, d.z * ff);
-            }
-            if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, ff, e, r2h, d))
-            {
-                df_acc(eAcc, e);
-                df_acc(wAcc, -0.5f * ff * r2h);
-                df_acc(fx, d.x * ff);
-                df_acc(fy, d.y * ff);
-                df_acc(fz, d.z * ff);
-            }
+            PairMixed q;
+            if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
+            if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, q)) acc.add(q);
         }
         if (k < cnt)
         {
             const int32_t j0 = __ldg(col + (int64_t)k * stride);
-            float ff, e, r2h;
-            float3 d;
-            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rc2, ff, e, r2h, d))
-            {
-                df_acc(eAcc, e);
-                df_acc(wAcc, -0.5f * ff * r2h);
-                df_acc(fx, d.x * ff);
-                df_acc(fy, d.y * ff);
-                df_acc(fz, d.z * ff);
-            }
+            PairMixed q;
+            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rc2, q)) acc.add(q);
         }
-        double4 f = make_double4((double)fx.h + (double)fx.l, (double)fy.h + (double)fy.l,
-                                 (double)fz.h + (double)fz.l, 0.0);
+        double4 f = make_double4((double)acc.fx.h + (double)acc.fx.l, (double)acc.fy.h + (double)acc.fy.l,
+                                 (double)acc.fz.h + (double)acc.fz.l, 0.0);
         if (ACCUM)
         {
             const double4 o = force[i];
@@ -186,7 +169,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
         }
         force[i] = f;
     }
-    double e = 0.5 * ((double)eAcc.h + (double)eAcc.l), w = 0.5 * ((double)wAcc.h + (double)wAcc.l);
+    double e = 0.5 * ((double)acc.e.h + (double)acc.e.l), w = 0.5 * ((double)acc.w.h + (double)acc.w.l);
     mrmd_dev::block_sum2(e, w, red);
     if (threadIdx.x == 0)
     {
@@ -202,42 +185,53 @@ int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* for
     const int64_t n = nl->rows;
     if (n == 0) return MRMD_OK;
     const unsigned grid = (unsigned)div_up(n, MX_TB);
+    const RcSq rc2 = make_rcsq(rcSqr);
     if (accumulate)
-        k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
-                                                              make_rcsq(rcSqr), nl->counts, nl->nbrs, nl->stride, n, ev);
+        k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
+                                                              nl->counts, nl->nbrs, nl->stride, n, ev);
     else
-        k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p,
-                                                               make_rcsq(rcSqr), nl->counts, nl->nbrs, nl->stride, n, ev);
+        k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
+                                                               nl->counts, nl->nbrs, nl->stride, n, ev);
     return after_launch(ctx, "lj_mixed_full");
+}
+
+int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_lj* lj, mrmd_atoms* a,
+                  const mrmd_nlist* nl, const mrmd_pred* pred, double* ev)
+{
+    const int64_t n = nl->rows;
+    if (n == 0) return MRMD_OK;
+    const bool usePred = pred != nullptr && pred->kind != MRMD_PRED_ALWAYS;
+    const unsigned grid = (unsigned)div_up(n, MX_TB);
+    const mrmd_dev::Pred dp = to_dev_pred(pred);
+    const RcSq rc2 = make_rcsq(lj->rcSqr);
+    const double4* pos = reinterpret_cast<const double4*>(a->pos);
+    if (usePred)
+        k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
+                                                               nl->nbrs, nl->stride, n, dp, ev);
+    else
+        k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
+                                                                nl->nbrs, nl->stride, n, dp, ev);
+    return after_launch(ctx, "lj_mixed_half");
+}
+
+SplitParams split_params_for(const mrmd_nlist* nl)
+{
+    const CellList* cl = static_cast<const CellList*>(nl->cells);
+    const double origin[3] = {cl->g.mn.x, cl->g.mn.y, cl->g.mn.z};
+    return split_params(origin, cl->g.extent * 1.25 + 8.0);
 }
 
 int lj_apply_mixed(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* nl, const mrmd_pred* pred,
                    double* ev)
 {
-    if (lj->numTypes > 1)
-        return set_error(ctx, MRMD_ERR_ARG, "mixed precision supports one atom type");
-    const int64_t n = nl->rows;
-    if (n == 0) return MRMD_OK;
-    const CellList* cl = static_cast<const CellList*>(nl->cells);
-    const double origin[3] = {cl->g.mn.x, cl->g.mn.y, cl->g.mn.z};
-    const SplitParams sp = split_params(origin, cl->g.extent * 1.25 + 8.0);
+    if (lj->numTypes > 1) return set_error(ctx, MRMD_ERR_ARG, "mixed precision supports one atom type");
+    if (nl->rows == 0) return MRMD_OK;
+    const SplitParams sp = split_params_for(nl);
     const int64_t nAll = a->numLocal + a->numGhost;
     float4* hi = static_cast<float4*>(scratch(ctx, sizeof(float4) * 2 * (size_t)nAll));
     if (!hi) return MRMD_ERR_OOM;
     float4* lo = hi + nAll;
     MRMD_TRY(split_coords(ctx, a->pos, nAll, sp, hi, lo));
-    const bool usePred = pred != nullptr && pred->kind != MRMD_PRED_ALWAYS;
-    const unsigned grid = (unsigned)div_up(n, MX_TB);
-    const mrmd_dev::Pred dp = to_dev_pred(pred);
-    const RcSq rc2 = make_rcsq(lj->rcSqr);
-    if (usePred)
-        k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
-                                                               a->force, lj->p0, rc2, nl->counts, nl->nbrs,
-                                                               nl->stride, n, dp, ev);
-    else
-        k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<const double4*>(a->pos),
-                                                                a->force, lj->p0, rc2, nl->counts, nl->nbrs,
-                                                                nl->stride, n, dp, ev);
-    return after_launch(ctx, "lj_mixed_half");
+    return lj_mixed_half(ctx, hi, lo, lj, a, nl, pred, ev);
 }
 }  // namespace mrmd_impl

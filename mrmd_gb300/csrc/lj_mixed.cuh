@@ -29,6 +29,14 @@ int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams
 int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
                   const mrmd_nlist* nl, double* ev, bool accumulate);
 
+// Half-list mixed pair force on given split coordinates (i and j forces
+// accumulated into the FP64 force array with atomics).
+int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_lj* lj, mrmd_atoms* a,
+                  const mrmd_nlist* nl, const mrmd_pred* pred, double* ev);
+
+// Split parameters matching the cell grid the list was built on.
+SplitParams split_params_for(const mrmd_nlist* nl);
+
 // rc^2 as a double-float, so that the cutoff test decides on the full
 // ~2^-48 accurate r^2: the LJ force jumps at rc (the shifted potential is
 // continuous, its force is not), and an FP32-rounded test would misplace
@@ -46,18 +54,40 @@ inline RcSq make_rcsq(double rcSqr)
     return r;
 }
 
-// One pair in the mixed form.  Returns false when outside the cutoff.
-// ff: force factor (F_i = d * ff), e: pair energy, r2h: FP32 r^2, d: FP32 dx.
-__device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_i, const float4& hj, const float4& lj,
-                                           const LJDev& p, RcSq rc2, float& ff, float& e, float& r2h, float3& d)
+// Result of one pair in the mixed form.  dx = dh + dl exactly (the split
+// coordinates make hi_i - hi_j exact), ff is the double-float force factor
+// (F_i += dx * ff), e the FP32 pair energy, r2h the FP32 head of r^2.
+struct PairMixed
 {
-    const df dx = fast_two_sum(hi_i.x - hj.x, lo_i.x - lj.x);
-    const df dy = fast_two_sum(hi_i.y - hj.y, lo_i.y - lj.y);
-    const df dz = fast_two_sum(hi_i.z - hj.z, lo_i.z - lj.z);
-    const df r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-    if (r2.h > rc2.h || (r2.h == rc2.h && r2.l > rc2.l)) return false;  // distSqr > rcSqr
-    r2h = r2.h;
-    d = make_float3(dx.h, dy.h, dz.h);
+    float3 dh, dl;
+    df ff;
+    float e, r2h;
+};
+
+// One pair in the mixed form; false when outside the cutoff (distSqr > rcSqr).
+__device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_i, const float4& hj, const float4& lj,
+                                           const LJDev& p, RcSq rc2, PairMixed& o)
+{
+    o.dh = make_float3(hi_i.x - hj.x, hi_i.y - hj.y, hi_i.z - hj.z);  // exact
+    o.dl = make_float3(lo_i.x - lj.x, lo_i.y - lj.y, lo_i.z - lj.z);  // |dl| <= 2^-q
+    // FP32 early reject, far outside the FP32 error of r^2
+    const float fx = o.dh.x + o.dl.x, fy = o.dh.y + o.dl.y, fz = o.dh.z + o.dl.z;
+    const float r2f = __fmaf_rn(fx, fx, __fmaf_rn(fy, fy, fz * fz));
+    if (r2f > rc2.h * 1.0000005f) return false;
+    // r^2 = sum (dh + dl)^2 as double-float: exact squares of the heads
+    // (FMA TwoProd), the 2*dh*dl cross terms in the low part
+    const float px = o.dh.x * o.dh.x, py = o.dh.y * o.dh.y, pz = o.dh.z * o.dh.z;
+    float lo = __fmaf_rn(o.dh.x, o.dh.x, -px);
+    lo += __fmaf_rn(o.dh.y, o.dh.y, -py);
+    lo += __fmaf_rn(o.dh.z, o.dh.z, -pz);
+    lo = __fmaf_rn(2.0f * o.dh.x, o.dl.x, lo);
+    lo = __fmaf_rn(2.0f * o.dh.y, o.dl.y, lo);
+    lo = __fmaf_rn(2.0f * o.dh.z, o.dl.z, lo);
+    const df s1 = two_sum(px, py);
+    const df s2 = two_sum(s1.h, pz);
+    const df r2 = fast_two_sum(s2.h, s2.l + s1.l + lo);
+    if (r2.h > rc2.h || (r2.h == rc2.h && r2.l > rc2.l)) return false;
+    o.r2h = r2.h;
     if (r2.h >= p.capSqrf)
     {
         const df u = df_rcp(r2);
@@ -65,18 +95,40 @@ __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_
         const df u3 = df_mul(u2, u);
         const df u4 = df_sqr(u2);
         const df t = df_add(df_mul(df{p.ff1h, p.ff1l}, u3), df{-p.ff2h, -p.ff2l});
-        const df f = df_mul(u4, t);
-        ff = f.h + f.l;
-        e = __fmaf_rn(u3.h, __fmaf_rn(p.ef1f, u3.h, -p.ef2f), -p.shiftf);
+        o.ff = df_mul(u4, t);
+        o.e = __fmaf_rn(u3.h, __fmaf_rn(p.ef1f, u3.h, -p.ef2f), -p.shiftf);
     }
     else
     {
         // capped branch (action/LennardJones.hpp:70-77): |F| constant, no
         // amplification of the r^2 error
         const float dist = sqrtf(r2.h);
-        ff = p.capCoeff_f / dist;
-        e = p.eCapf - (dist - p.capDistf) * p.capCoeff_f - p.shiftf;
+        o.ff = df{p.capCoeff_f / dist, 0.0f};
+        o.e = p.eCapf - (dist - p.capDistf) * p.capCoeff_f - p.shiftf;
     }
     return true;
+}
+
+// s += (dh + dl) * ff in double-float (FMA TwoProd of the heads, first-order
+// cross terms), so no pair force is ever rounded to FP32.
+__device__ __forceinline__ void df_acc_prod(df& s, float dh, float dl, const df& ff)
+{
+    const float p = dh * ff.h;
+    float e = __fmaf_rn(dh, ff.h, -p);
+    e = __fmaf_rn(dh, ff.l, e);
+    e = __fmaf_rn(dl, ff.h, e);
+    const df t = two_sum(s.h, p);
+    s.h = t.h;
+    s.l += t.l + e;
+}
+
+// The same product as a double (for FP64 atomics of the j-force).
+__device__ __forceinline__ double prod_d(float dh, float dl, const df& ff)
+{
+    const float p = dh * ff.h;
+    float e = __fmaf_rn(dh, ff.h, -p);
+    e = __fmaf_rn(dh, ff.l, e);
+    e = __fmaf_rn(dl, ff.h, e);
+    return (double)p + (double)e;
 }
 }  // namespace mrmd_impl
