@@ -274,6 +274,22 @@ int mrmd_lj_get_params(const mrmd_lj* lj, mrmd_lj_params* out, int64_t count);
 int mrmd_lj_apply(mrmd_ctx* ctx, mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* nl,
                   const mrmd_pred* pred, int precision, double* energy, double* virial);
 
+/* Largest atom count (local + ghost) mrmd_lj_apply_mixed_noalloc accepts. */
+#define MRMD_LJ_NOALLOC_MAX_ATOMS 262144
+
+/* No counterpart in the reference.  The mixed-form mrmd_lj_apply for callers
+ * that cannot allocate device memory during their step loop (all free
+ * memory already belongs to another allocator, or a cudaMalloc and its
+ * implied synchronisation are not allowed there): same arguments and
+ * results as mrmd_lj_apply(..., MRMD_PREC_MIXED, ...), but its scratch is a
+ * fixed array inside the library (8 MiB per GPU, held until exit) and it
+ * calls no allocator.  Rejects more than MRMD_LJ_NOALLOC_MAX_ATOMS atoms
+ * with MRMD_ERR_CAPACITY.  The first call on a device looks up the array's
+ * device address (make it before any stream capture); calls that overlap
+ * on the GPU share the array and race. */
+int mrmd_lj_apply_mixed_noalloc(mrmd_ctx* ctx, mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* nl,
+                                const mrmd_pred* pred, double* energy, double* virial);
+
 /* ------------------------------------------------------- integrators -- */
 /* VelocityVerlet::preForceIntegrate (action/VelocityVerlet.cpp:26-67);
  * returns the max displacement in *maxDisplacement (may be NULL). */

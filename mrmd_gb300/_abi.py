@@ -145,6 +145,7 @@ SIGNATURES = {
     "mrmd_lj_destroy": (_i, [_v, _v]),
     "mrmd_lj_get_params": (_i, [_v, P(LJParamsS), _i64]),
     "mrmd_lj_apply": (_i, [_v, _v, P(AtomsS), P(NListS), P(Pred), _i, c_double_p, c_double_p]),
+    "mrmd_lj_apply_mixed_noalloc": (_i, [_v, _v, P(AtomsS), P(NListS), P(Pred), c_double_p, c_double_p]),
     "mrmd_vv_pre": (_i, [_v, P(AtomsS), _d, c_double_p]),
     "mrmd_vv_post": (_i, [_v, P(AtomsS), _d]),
     "mrmd_langevin_pre": (_i, [_v, P(AtomsS), _d, _d, _d, _u64, _u64, P(Pred), c_double_p]),
