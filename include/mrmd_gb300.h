@@ -212,15 +212,16 @@ int mrmd_ghost_layer_download(mrmd_ctx* ctx, const mrmd_ghost_layer* g, int64_t 
 
 /* ------------------------------------------------- neighbour list -- */
 /* HalfVerletList = Cabana::VerletList<HalfNeighborTag, VerletLayout2D>
- * (datatypes.hpp:184-187).  Layout: counts[rows], neighbours transposed as
- * nbrs[k * stride + i] so that a warp reading slot k of 32 consecutive
- * atoms issues one coalesced 128-byte load. */
+ * (datatypes.hpp:184-187).  Layout: counts[rows]; neighbours in tiles of 32
+ * rows, entry k of row i at (i / 32) * 32 * maxNeighbors + 32 * k + i % 32,
+ * so a warp reading slot k of its 32 rows issues one 128-byte load and a
+ * warp's whole list is one compact tile (written without partial sectors). */
 typedef struct {
-    int32_t* counts;   /* device, [rowsCapacity]            */
-    int32_t* nbrs;     /* device, [maxNeighbors * stride]   */
-    int64_t rows;      /* number of list rows (end - begin) */
-    int64_t begin;     /* first particle with a list        */
-    int64_t stride;    /* row stride of nbrs (>= rows, multiple of 32) */
+    int32_t* counts;   /* device, [rowsCapacity]                          */
+    int32_t* nbrs;     /* device, [ceil(rows / 32) * 32 * maxNeighbors]   */
+    int64_t rows;      /* number of list rows (end - begin)               */
+    int64_t begin;     /* first particle with a list                      */
+    int64_t stride;    /* step between consecutive slots of a row (32)    */
     int64_t maxNeighbors;
     int64_t rowsCapacity;
     int64_t nbrsCapacity; /* allocated int32 entries of nbrs */
@@ -389,7 +390,7 @@ typedef struct {
     double dt;
     int64_t rebuildInterval; /* steps between list rebuilds (>= 1) */
     int32_t useGraph;        /* capture the steps between rebuilds as a CUDA graph */
-    int32_t sortAtoms;       /* permute atoms by cell at every rebuild */
+    int32_t sortAtoms;       /* k > 0: permute atoms into cell order at every k-th rebuild; 0: never */
     int64_t maxNeighbors;    /* initial list capacity (grown on overflow) */
 } mrmd_md_config;
 

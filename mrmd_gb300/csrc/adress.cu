@@ -143,7 +143,7 @@ struct LJIGArgs
     mrmd_molecules m;
     const int32_t* counts;
     const int32_t* nbrs;
-    int64_t stride;
+    int64_t cap;
     int64_t nMol;
     const LJDev* table;
     int32_t numTypes;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(128) k_ljig(LJIGArgs A)
         const int32_t cnt = A.counts[alpha];
         for (int32_t k = 0; k < cnt; ++k)
         {
-            const int64_t beta = A.nbrs[(int64_t)k * A.stride + alpha];
+            const int64_t beta = A.nbrs[mrmd_dev::nbr_row(alpha, A.cap) + 32 * (int64_t)k];
             double fB[3] = {0.0, 0.0, 0.0};
             const double modB = A.m.modulatedLambda[beta];
             if (is_cg(modA) && is_cg(modB)) continue;
@@ -401,7 +401,7 @@ int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nli
     A.m = *m;
     A.counts = nl->counts;
     A.nbrs = nl->nbrs;
-    A.stride = nl->stride;
+    A.cap = nl->maxNeighbors;
     A.nMol = nl->rows;
     A.table = s->dTable;
     A.numTypes = (int32_t)s->numTypes;

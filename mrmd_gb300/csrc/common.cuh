@@ -86,6 +86,11 @@ int scan_exclusive_i32(mrmd_ctx* ctx, const int32_t* in, int32_t* out, int64_t n
 
 namespace mrmd_dev
 {
+// Neighbour lists are stored in tiles of 32 rows: entry k of row i lives at
+// (i / 32) * 32 * cap + 32 * k + i % 32, so slot k of a warp's 32 rows is one
+// 128-byte line and a warp's whole list is one compact 32 x cap tile.
+__device__ __forceinline__ int64_t nbr_row(int64_t i, int64_t cap) { return (i >> 5) * (cap << 5) + (i & 31); }
+
 // read-only 32-byte load of one atom sector as two 128-bit loads
 __device__ __forceinline__ double4 ldg4(const double4* p)
 {

@@ -74,7 +74,7 @@ template <bool PRED, bool MULTI>
 __global__ void __launch_bounds__(LJ_TB) k_lj_fp64(
     const double4* __restrict__ pos, double* __restrict__ force, const int32_t* __restrict__ type,
     const LJDev p0, const LJDev* __restrict__ table, int32_t numTypesIndex, double rcSqr,
-    const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t stride, int64_t n,
+    const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
     mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
@@ -86,10 +86,10 @@ __global__ void __launch_bounds__(LJ_TB) k_lj_fp64(
         double fx = 0.0, fy = 0.0, fz = 0.0;
         const int32_t cnt = counts[i];
         const int32_t ti = MULTI ? type[i] * numTypesIndex : 0;
-        const int32_t* __restrict__ col = nbrs + i;
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
         for (int32_t k = 0; k < cnt; ++k)
         {
-            const int32_t j = __ldg(col + (int64_t)k * stride);
+            const int32_t j = __ldg(col + 32 * (int64_t)k);
             const double4 pj = mrmd_dev::ldg4(pos + j);
             if (PRED && !mrmd_dev::pred2(pred, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z)) continue;
             const double dx = pi.x - pj.x;
@@ -136,7 +136,7 @@ int lj_apply_fp64(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_nl
 #define LJ_LAUNCH(P, M)                                                                                \
     k_lj_fp64<P, M><<<grid, LJ_TB, 0, ctx->stream>>>(pos, a->force, a->type, lj->p0, lj->dTable,         \
                                                      (int32_t)lj->numTypesIndex, lj->rcSqr, nl->counts, \
-                                                     nl->nbrs, nl->stride, n, dp, ev)
+                                                     nl->nbrs, nl->maxNeighbors, n, dp, ev)
     if (usePred && multi) LJ_LAUNCH(true, true);
     else if (usePred) LJ_LAUNCH(true, false);
     else if (multi) LJ_LAUNCH(false, true);

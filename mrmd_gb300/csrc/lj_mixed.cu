@@ -84,7 +84,7 @@ template <bool PRED>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
     double* __restrict__ force, const LJDev p, RcSq rc2, const int32_t* __restrict__ counts,
-    const int32_t* __restrict__ nbrs, int64_t stride, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
+    const int32_t* __restrict__ nbrs, int64_t cap, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
     Acc acc;
@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
         double4 pi;
         if (PRED) pi = pos[i];
         const int32_t cnt = counts[i];
-        const int32_t* __restrict__ col = nbrs + i;
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
         for (int32_t k = 0; k < cnt; ++k)
         {
-            const int32_t j = __ldg(col + (int64_t)k * stride);
+            const int32_t j = __ldg(col + 32 * (int64_t)k);
             if (PRED)
             {
                 const double4 pj = mrmd_dev::ldg4(pos + j);
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
 template <bool ACCUM>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
     const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
-    RcSq rc2, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t stride, int64_t n,
+    RcSq rc2, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
     double* __restrict__ ev)
 {
     __shared__ double red[64];
@@ -140,12 +140,12 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
     {
         const float4 hi_i = hi[i], lo_i = lo[i];
         const int32_t cnt = counts[i];
-        const int32_t* __restrict__ col = nbrs + i;
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
         int32_t k = 0;
         for (; k + 1 < cnt; k += 2)
         {
-            const int32_t j0 = __ldg(col + (int64_t)k * stride);
-            const int32_t j1 = __ldg(col + (int64_t)(k + 1) * stride);
+            const int32_t j0 = __ldg(col + 32 * (int64_t)k);
+            const int32_t j1 = __ldg(col + 32 * (int64_t)(k + 1));
             const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
             const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
             PairMixed q;
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
         }
         if (k < cnt)
         {
-            const int32_t j0 = __ldg(col + (int64_t)k * stride);
+            const int32_t j0 = __ldg(col + 32 * (int64_t)k);
             PairMixed q;
             if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rc2, q)) acc.add(q);
         }
@@ -188,10 +188,10 @@ int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* for
     const RcSq rc2 = make_rcsq(rcSqr);
     if (accumulate)
         k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
-                                                              nl->counts, nl->nbrs, nl->stride, n, ev);
+                                                              nl->counts, nl->nbrs, nl->maxNeighbors, n, ev);
     else
         k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
-                                                               nl->counts, nl->nbrs, nl->stride, n, ev);
+                                                               nl->counts, nl->nbrs, nl->maxNeighbors, n, ev);
     return after_launch(ctx, "lj_mixed_full");
 }
 
@@ -207,10 +207,10 @@ int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_
     const double4* pos = reinterpret_cast<const double4*>(a->pos);
     if (usePred)
         k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                               nl->nbrs, nl->stride, n, dp, ev);
+                                                               nl->nbrs, nl->maxNeighbors, n, dp, ev);
     else
         k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                                nl->nbrs, nl->stride, n, dp, ev);
+                                                                nl->nbrs, nl->maxNeighbors, n, dp, ev);
     return after_launch(ctx, "lj_mixed_half");
 }
 

@@ -136,7 +136,7 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
 {
     mrmd_atoms* a = &md->atoms;
     MRMD_TRY(mrmd_ghost_exchange_real_atoms(ctx, a, &md->sd));
-    if (md->cfg.sortAtoms)
+    if (md->cfg.sortAtoms > 0 && md->rebuilds % md->cfg.sortAtoms == 0)
     {
         MRMD_TRY(md->sortCells.build(ctx, a->pos, md->n, md->grid));
         if (md->shadow.capacity < a->capacity)

@@ -69,25 +69,20 @@ __global__ void k_cell_scatter(const int32_t* __restrict__ cellOf, int64_t n,
     }
 }
 
-// ascending particle index inside each cell (stable counting sort)
-__global__ void k_cell_sort(const int32_t* __restrict__ cellStart, int64_t ncell,
-                            int32_t* __restrict__ sorted)
+// Stable order inside each cell: every slot of the (unordered) scatter
+// output counts the smaller ids of its cell and moves its id to that rank.
+__global__ void k_cell_rank(const int32_t* __restrict__ cellOf, const int32_t* __restrict__ cellStart,
+                            const int32_t* __restrict__ unordered, int64_t n, int32_t* __restrict__ sorted)
 {
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell;
-         c += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x)
     {
-        const int32_t s = cellStart[c], e = cellStart[c + 1];
-        for (int32_t a = s + 1; a < e; ++a)
-        {
-            const int32_t v = sorted[a];
-            int32_t b = a - 1;
-            while (b >= s && sorted[b] > v)
-            {
-                sorted[b + 1] = sorted[b];
-                --b;
-            }
-            sorted[b + 1] = v;
-        }
+        const int32_t v = unordered[s];
+        const int32_t c = cellOf[v];
+        const int32_t b = cellStart[c], e = cellStart[c + 1];
+        int32_t rank = 0;
+        for (int32_t t = b; t < e; ++t) rank += unordered[t] < v;
+        sorted[b + rank] = v;
     }
 }
 
@@ -113,7 +108,7 @@ template <bool FULL>
 __global__ void __launch_bounds__(128) k_build_list(
     const double4* __restrict__ pos, const int32_t* __restrict__ cellOf,
     const int32_t* __restrict__ cellStart, const float4* __restrict__ spos, CellGrid g,
-    int64_t begin, int64_t end, double rsq, float rsqLo, float rsqHi, int64_t stride, int64_t cap,
+    int64_t begin, int64_t end, double rsq, float rsqLo, float rsqHi, int64_t cap,
     int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount)
 {
     for (int64_t i = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < end;
@@ -128,14 +123,16 @@ __global__ void __launch_bounds__(128) k_build_list(
         int32_t cnt = 0;
         const int64_t row = i - begin;
         const int axEnd = min(cx + 1, g.n.x - 1);
+        const int az0 = max(cz - 1, 0), az1 = min(cz + 1, g.n.z - 1);
         for (int ax = FULL ? max(cx - 1, 0) : cx; ax <= axEnd; ++ax)
         {
             for (int ay = max(cy - 1, 0); ay <= min(cy + 1, g.n.y - 1); ++ay)
             {
-                for (int az = max(cz - 1, 0); az <= min(cz + 1, g.n.z - 1); ++az)
+                // cells (ax, ay, az0..az1) are adjacent in the cell order, so
+                // their particles form one contiguous span of `spos`
                 {
-                    const int32_t c = (ax * g.n.y + ay) * g.n.z + az;
-                    const int32_t s0 = cellStart[c], s1 = cellStart[c + 1];
+                    const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
+                    const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
                     for (int32_t s = s0; s < s1; ++s)
                     {
                         const float4 q = spos[s];
@@ -160,7 +157,7 @@ __global__ void __launch_bounds__(128) k_build_list(
                             keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
                         }
                         if (!keep) continue;
-                        if (cnt < cap) nbrs[(int64_t)cnt * stride + row] = j;
+                        if (cnt < cap) nbrs[mrmd_dev::nbr_row(row, cap) + 32 * (int64_t)cnt] = j;
                         ++cnt;
                     }
                 }
@@ -211,10 +208,13 @@ int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid
     MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, g.ncell + 1, nullptr));
     if (n > 0)
     {
-        k_cell_scatter<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, n, cellStart, cursor, sorted);
+        // unordered scatter into `spos` storage (reused as int32 scratch), then
+        // stable ranks into `sorted`
+        int32_t* unordered = reinterpret_cast<int32_t*>(spos);
+        k_cell_scatter<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, n, cellStart, cursor, unordered);
         MRMD_TRY(after_launch(ctx, "cell_scatter"));
-        k_cell_sort<<<grid_for(ctx, g.ncell, TB), TB, 0, ctx->stream>>>(cellStart, g.ncell, sorted);
-        MRMD_TRY(after_launch(ctx, "cell_sort"));
+        k_cell_rank<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, cellStart, unordered, n, sorted);
+        MRMD_TRY(after_launch(ctx, "cell_rank"));
         k_cell_gather<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4),
                                                                     sorted, n, g.mn, spos);
         MRMD_TRY(after_launch(ctx, "cell_gather"));
@@ -253,7 +253,7 @@ static int ensure_list_storage(mrmd_ctx* ctx, mrmd_nlist* nl, int64_t rows, int6
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&nl->nbrs), sizeof(int32_t) * (size_t)need));
         nl->nbrsCapacity = need;
     }
-    nl->stride = stride;
+    nl->stride = 32;  // slot step inside a 32-row tile
     nl->maxNeighbors = maxNeighbors;
     return MRMD_OK;
 }
@@ -284,11 +284,11 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
             if (full)
                 k_build_list<true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                     reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
-                    end, rsq, rsqLo, rsqHi, nl->stride, cap, nl->counts, nl->nbrs, maxCount);
+                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount);
             else
                 k_build_list<false><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                     reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
-                    end, rsq, rsqLo, rsqHi, nl->stride, cap, nl->counts, nl->nbrs, maxCount);
+                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount);
             MRMD_TRY(after_launch(ctx, "build_list"));
         }
         int32_t hMax = 0;
@@ -435,7 +435,8 @@ int mrmd_nlist_download(mrmd_ctx* ctx, const mrmd_nlist* nl, int32_t* counts, in
     if (counts) std::memcpy(counts, c.data(), sizeof(int32_t) * (size_t)rows);
     if (!nbrs) return MRMD_OK;
     if (mx > cap) return set_error(ctx, MRMD_ERR_CAPACITY, "download capacity %lld < %d", (long long)cap, mx);
-    std::vector<int32_t> t((size_t)(nl->stride * mx));
+    const int64_t tiles = div_up(rows, 32), lcap = nl->maxNeighbors;
+    std::vector<int32_t> t((size_t)(tiles * 32 * lcap));
     if (mx > 0)
     {
         MRMD_CUDA(ctx, cudaMemcpyAsync(t.data(), nl->nbrs, sizeof(int32_t) * t.size(), cudaMemcpyDeviceToHost,
@@ -443,7 +444,7 @@ int mrmd_nlist_download(mrmd_ctx* ctx, const mrmd_nlist* nl, int32_t* counts, in
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     for (int64_t i = 0; i < rows; ++i)
-        for (int64_t k = 0; k < c[(size_t)i]; ++k) nbrs[i * cap + k] = t[(size_t)(k * nl->stride + i)];
+        for (int64_t k = 0; k < c[(size_t)i]; ++k) nbrs[i * cap + k] = t[(size_t)((i >> 5) * (lcap << 5) + (k << 5) + (i & 31))];
     return MRMD_OK;
 }
 
