@@ -415,6 +415,48 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2);
 const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md);
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
 
+/* ------------------------------------------ fused AdResS stepper -- */
+/* The AdResS LJ <-> ideal-gas step composed from LJ_IdealGas::run
+ * (LJ_IdealGas.cpp:227-260), VelocityVerletLangevinThermostat
+ * (VelocityVerletLangevinThermostat.hpp:48-121), UpdateMolecules with a Slab
+ * (UpdateMolecules.hpp:24-70), ContributeMoleculeForceToAtoms
+ * (ContributeMoleculeForceToAtoms.cpp:23-48), MultiResGhostLayer and
+ * ThermodynamicForce sample/apply/update (ThermodynamicForce.cpp:74-96),
+ * for single-site molecules; the reference has no driver for this step. */
+typedef struct mrmd_adress mrmd_adress;
+typedef struct {
+    double boxMin[3];
+    double boxMax[3];
+    double rc, skin, sigma, epsilon, cappingDistance;
+    int32_t shifted;
+    int32_t precision;
+    double dt;
+    int64_t rebuildInterval;
+    double slabCenter[3];
+    double atomisticDiameter; /* Slab(center, atomisticRegionDiameter, hybridRegionDiameter, nu) */
+    double hybridDiameter;
+    int64_t nu;
+    double gamma;             /* Langevin friction (zeta) and temperature */
+    double temperature;
+    uint64_t seed;
+    int32_t tfEnabled;
+    int32_t useGraph;
+    double tfBinWidth, tfTargetDensity, tfModulation, tfSmoothingSigma, tfSmoothingRange;
+    int64_t tfSampleInterval, tfUpdateInterval;
+    int64_t maxNeighbors;
+} mrmd_adress_config;
+
+int mrmd_adress_create(mrmd_ctx* ctx, mrmd_adress** out, const mrmd_adress_config* cfg, int64_t n,
+                       const double* pos3, const double* vel3, const double* mass);
+int mrmd_adress_destroy(mrmd_ctx* ctx, mrmd_adress* s);
+/* Advance nsteps; energies (may be NULL): LJ_IdealGas energy of every step. */
+int mrmd_adress_run(mrmd_ctx* ctx, mrmd_adress* s, int64_t nsteps, double* energies);
+int mrmd_adress_get_state(mrmd_ctx* ctx, mrmd_adress* s, double* pos3, double* vel3, double* force3);
+int mrmd_adress_get_tf(mrmd_ctx* ctx, mrmd_adress* s, double* force, double* density, int64_t* numBins);
+int mrmd_adress_set_tf(mrmd_ctx* ctx, mrmd_adress* s, const double* force);
+/* [0] steps, [1] rebuilds, [2] molecule list pairs, [3] ghost molecules */
+int mrmd_adress_stats(const mrmd_adress* s, int64_t* out4);
+
 #ifdef __cplusplus
 }
 #endif

@@ -693,5 +693,82 @@ class LJSystem:
             pass
 
 
+class AdResSSystem:
+    """Fused AdResS LJ <-> ideal-gas stepper for single-site molecules (mrmd_adress_*)."""
+
+    def __init__(self, pos, vel, box_min, box_max, slab_center, atomistic_diameter,
+                 hybrid_diameter, nu=1, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
+                 capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
+                 rebuild_interval=10, gamma=1.0, temperature=1.0, seed=1234, tf=True,
+                 tf_bin_width=1.2, tf_target_density=0.5, tf_modulation=1.0, tf_sigma=2.4,
+                 tf_range=3.0, tf_sample_interval=1, tf_update_interval=1000, use_graph=True,
+                 max_neighbors=0, mass=None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        pos = _f64(pos)
+        vel = _f64(vel)
+        self.n = len(pos)
+        c = _abi.AdResSConfigS()
+        c.boxMin = (C.c_double * 3)(*box_min)
+        c.boxMax = (C.c_double * 3)(*box_max)
+        c.rc, c.skin, c.sigma, c.epsilon = rc, skin, sigma, epsilon
+        c.cappingDistance = capping_distance
+        c.shifted = int(bool(shifted))
+        c.precision = int(precision)
+        c.dt = dt
+        c.rebuildInterval = int(rebuild_interval)
+        c.slabCenter = (C.c_double * 3)(*slab_center)
+        c.atomisticDiameter, c.hybridDiameter, c.nu = atomistic_diameter, hybrid_diameter, int(nu)
+        c.gamma, c.temperature, c.seed = gamma, temperature, int(seed)
+        c.tfEnabled = int(bool(tf))
+        c.useGraph = int(bool(use_graph))
+        c.tfBinWidth, c.tfTargetDensity, c.tfModulation = tf_bin_width, tf_target_density, tf_modulation
+        c.tfSmoothingSigma, c.tfSmoothingRange = tf_sigma, tf_range
+        c.tfSampleInterval, c.tfUpdateInterval = int(tf_sample_interval), int(tf_update_interval)
+        c.maxNeighbors = int(max_neighbors)
+        self.cfg = c
+        h = C.c_void_p()
+        m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())
+        self.ctx.check(self.ctx.lib.mrmd_adress_create(self.ctx.h, C.byref(h), C.byref(c), self.n,
+                                                       _dp(pos), _dp(vel), _dp(m)), "AdResSSystem")
+        self.h = h
+
+    def run(self, nsteps: int, energies: bool = True):
+        e = np.zeros(max(nsteps, 1)) if energies else None
+        self.ctx.check(self.ctx.lib.mrmd_adress_run(self.ctx.h, self.h, int(nsteps), _dp(e)), "run")
+        return e[:nsteps] if energies else None
+
+    def state(self):
+        p, v, f = (np.zeros((self.n, 3)) for _ in range(3))
+        self.ctx.check(self.ctx.lib.mrmd_adress_get_state(self.ctx.h, self.h, _dp(p), _dp(v), _dp(f)),
+                       "state")
+        return p, v, f
+
+    def thermodynamic_force(self):
+        nb = C.c_int64()
+        self.ctx.check(self.ctx.lib.mrmd_adress_get_tf(self.ctx.h, self.h, None, None, C.byref(nb)), "tf")
+        f, d = np.zeros(nb.value), np.zeros(nb.value)
+        self.ctx.check(self.ctx.lib.mrmd_adress_get_tf(self.ctx.h, self.h, _dp(f), _dp(d), None), "tf")
+        return f, d
+
+    def set_thermodynamic_force(self, f):
+        self.ctx.check(self.ctx.lib.mrmd_adress_set_tf(self.ctx.h, self.h, _dp(_f64(f))), "set tf")
+
+    def stats(self):
+        out = np.zeros(4, dtype=np.int64)
+        self.ctx.lib.mrmd_adress_stats(self.h, _ip(out))
+        return dict(steps=int(out[0]), rebuilds=int(out[1]), pairs=int(out[2]), ghost_molecules=int(out[3]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.mrmd_adress_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def version() -> str:
     return _abi.lib().mrmd_version().decode()

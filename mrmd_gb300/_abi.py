@@ -89,6 +89,20 @@ class MDConfigS(C.Structure):
                 ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64)]
 
 
+class AdResSConfigS(C.Structure):
+    _fields_ = [("boxMin", C.c_double * 3), ("boxMax", C.c_double * 3), ("rc", C.c_double),
+                ("skin", C.c_double), ("sigma", C.c_double), ("epsilon", C.c_double),
+                ("cappingDistance", C.c_double), ("shifted", C.c_int32), ("precision", C.c_int32),
+                ("dt", C.c_double), ("rebuildInterval", C.c_int64), ("slabCenter", C.c_double * 3),
+                ("atomisticDiameter", C.c_double), ("hybridDiameter", C.c_double), ("nu", C.c_int64),
+                ("gamma", C.c_double), ("temperature", C.c_double), ("seed", C.c_uint64),
+                ("tfEnabled", C.c_int32), ("useGraph", C.c_int32), ("tfBinWidth", C.c_double),
+                ("tfTargetDensity", C.c_double), ("tfModulation", C.c_double),
+                ("tfSmoothingSigma", C.c_double), ("tfSmoothingRange", C.c_double),
+                ("tfSampleInterval", C.c_int64), ("tfUpdateInterval", C.c_int64),
+                ("maxNeighbors", C.c_int64)]
+
+
 P = C.POINTER
 _v = C.c_void_p
 _i = C.c_int
@@ -175,6 +189,14 @@ SIGNATURES = {
     "mrmd_md_set_state": (_i, [_v, _v, c_double_p, c_double_p]),
     "mrmd_md_stats": (_i, [_v, c_int64_p]),
     "mrmd_md_eval": (_i, [_v, _v, _i, c_double_p]),
+    "mrmd_adress_create": (_i, [_v, P(_v), P(AdResSConfigS), _i64, c_double_p, c_double_p,
+                                c_double_p]),
+    "mrmd_adress_destroy": (_i, [_v, _v]),
+    "mrmd_adress_run": (_i, [_v, _v, _i64, c_double_p]),
+    "mrmd_adress_get_state": (_i, [_v, _v, c_double_p, c_double_p, c_double_p]),
+    "mrmd_adress_get_tf": (_i, [_v, _v, c_double_p, c_double_p, c_int64_p]),
+    "mrmd_adress_set_tf": (_i, [_v, _v, c_double_p]),
+    "mrmd_adress_stats": (_i, [_v, c_int64_p]),
     "mrmd_md_atoms": (P(AtomsS), [_v]),
     "mrmd_md_nlist": (P(NListS), [_v]),
 }

@@ -383,17 +383,19 @@ int mrmd_ljig_set_intervals(mrmd_ljig* s, int64_t samplingInterval, int64_t upda
     return MRMD_OK;
 }
 
-int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nlist* nl, mrmd_atoms* a,
-                  int precision, double* energy)
+}  // extern "C"
+
+namespace mrmd_impl
 {
-    // action/LJ_IdealGas.cpp:227-260
-    if (!ctx || !s || !m || !nl || !a) return MRMD_ERR_ARG;
-    MRMD_CHECK_ARG(precision == MRMD_PREC_FP64 || precision == MRMD_PREC_MIXED, ctx, "bad precision");
-    MRMD_CHECK_ARG(nl->rows <= m->numLocal, ctx, "list has more rows than local molecules");
+// LJ_IdealGas::run (LJ_IdealGas.cpp:227-260) without any host read-back:
+// the energy is added to *ev (device, zeroed by the caller).  For the mixed
+// form `hi`/`lo` may hold split coordinates already computed for the list's
+// grid (else they are computed into context scratch).
+int ljig_run_async(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nlist* nl, mrmd_atoms* a,
+                   int precision, double* ev, const float4* hiIn, const float4* loIn)
+{
     const int sampling = (s->runCounter % s->samplingInterval) == 0;
     const int64_t nb = COMP_BINS * s->numTypes;
-    double* ev = ctx->devScalars + 32;
-    MRMD_CUDA(ctx, cudaMemsetAsync(ev, 0, sizeof(double), ctx->stream));
     LJIGArgs A{};
     A.apos = reinterpret_cast<const double4*>(a->pos);
     A.aforce = a->force;
@@ -417,15 +419,20 @@ int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nli
         const unsigned grid = (unsigned)div_up(A.nMol, 128);
         if (precision == MRMD_PREC_MIXED)
         {
-            const CellList* cl = static_cast<const CellList*>(nl->cells);
-            const double origin[3] = {cl->g.mn.x, cl->g.mn.y, cl->g.mn.z};
-            const SplitParams sp = split_params(origin, cl->g.extent * 1.25 + 8.0);
-            const int64_t nAll = a->numLocal + a->numGhost;
-            float4* hi = static_cast<float4*>(scratch(ctx, sizeof(float4) * 2 * (size_t)nAll));
-            if (!hi) return MRMD_ERR_OOM;
-            MRMD_TRY(split_coords(ctx, a->pos, nAll, sp, hi, hi + nAll));
-            A.hi = hi;
-            A.lo = hi + nAll;
+            if (hiIn && loIn)
+            {
+                A.hi = hiIn;
+                A.lo = loIn;
+            }
+            else
+            {
+                const int64_t nAll = a->numLocal + a->numGhost;
+                float4* hi = static_cast<float4*>(scratch(ctx, sizeof(float4) * 2 * (size_t)nAll));
+                if (!hi) return MRMD_ERR_OOM;
+                MRMD_TRY(split_coords(ctx, a->pos, nAll, split_params_for(nl), hi, hi + nAll));
+                A.hi = hi;
+                A.lo = hi + nAll;
+            }
             k_ljig<true><<<grid, 128, 0, ctx->stream>>>(A);
         }
         else
@@ -441,6 +448,22 @@ int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nli
         MRMD_TRY(after_launch(ctx, "update_mean_comp"));
     }
     ++s->runCounter;
+    return MRMD_OK;
+}
+}  // namespace mrmd_impl
+
+extern "C" {
+
+int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nlist* nl, mrmd_atoms* a,
+                  int precision, double* energy)
+{
+    // action/LJ_IdealGas.cpp:227-260
+    if (!ctx || !s || !m || !nl || !a) return MRMD_ERR_ARG;
+    MRMD_CHECK_ARG(precision == MRMD_PREC_FP64 || precision == MRMD_PREC_MIXED, ctx, "bad precision");
+    MRMD_CHECK_ARG(nl->rows <= m->numLocal, ctx, "list has more rows than local molecules");
+    double* ev = ctx->devScalars + 32;
+    MRMD_CUDA(ctx, cudaMemsetAsync(ev, 0, sizeof(double), ctx->stream));
+    MRMD_TRY(ljig_run_async(ctx, s, m, nl, a, precision, ev, nullptr, nullptr));
     MRMD_CUDA(ctx, cudaMemcpyAsync(ctx->hostScalars + 32, ev, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (energy) *energy = ctx->hostScalars[32];

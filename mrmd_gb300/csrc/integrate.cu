@@ -66,6 +66,23 @@ __global__ void k_langevin_pre(double4* __restrict__ pos, double4* __restrict__ 
 }
 }  // namespace mrmd_impl
 
+namespace mrmd_impl
+{
+// Langevin pre-force step without reading the displacement back; dMax
+// (device) receives the max |dx|^2 via atomicMax (caller zeroes it).
+int langevin_pre_async(mrmd_ctx* ctx, mrmd_atoms* a, double dt, double zeta, double temperature, uint64_t seed,
+                       uint64_t step, const mrmd_pred* pred, double* dMax)
+{
+    const int64_t n = a->numLocal;
+    if (n == 0) return MRMD_OK;
+    k_langevin_pre<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+        reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
+        reinterpret_cast<const double4*>(a->force), a->mass, n, 0.5 * dt, dt, zeta, temperature, seed, step,
+        to_dev_pred(pred), dMax);
+    return after_launch(ctx, "langevin_pre");
+}
+}  // namespace mrmd_impl
+
 static int read_max_disp(mrmd_ctx* ctx, double* dMax, double* out)
 {
     if (!out) return finish(ctx, "integrate");

@@ -1,0 +1,114 @@
+"""The fused AdResS stepper against an oracle-driven loop of the same actions
+(LJ_IdealGas, Langevin, UpdateMolecules/Slab, ContributeMoleculeForceToAtoms,
+MultiResGhostLayer, ThermodynamicForce sample/apply/update)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    import mrmd_gb300 as M
+
+    M.default_context()
+    return M
+
+
+P = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=5, gamma=1.0, T=1.0, seed=77,
+         at=10.0, hy=5.0, nu=1, binw=1.2, rho=0.5, mod=1.0, tfs=2.4, tfr=3.0, S=2, U=6)
+
+
+def system(n, box, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0, 1, (n, 3)) * np.asarray(box)
+    vel = rng.normal(0, 1, (n, 3))
+    return pos, vel
+
+
+def oracle_loop(orc, pos, vel, box, nsteps, p):
+    n = len(pos)
+    rlist = p["rc"] + p["skin"]
+    sd = orc.subdomain([0, 0, 0], box, rlist)
+    a = orc.Atoms.from_positions(pos, capacity=4 * n)
+    a.vel[:n] = vel
+    m = orc.Molecules(4 * n)
+    m.atomsOffset[:n] = np.arange(n)
+    m.numAtoms[:n] = 1
+    m.numLocal = n
+    slab = orc.slab([box[0] / 2, box[1] / 2, box[2] / 2], p["at"], p["hy"], p["nu"])
+    ljig = orc.LJIdealGas(p["cap"], p["rc"], p["sigma"], p["epsilon"], True)
+    tf = orc.ThermodynamicForce([p["rho"]], sd, p["binw"], [p["mod"]], False, True)
+    energies = []
+    corr = co = no = None
+    for st in range(nsteps):
+        orc.langevin_pre(a, p["dt"], p["gamma"], p["T"], p["seed"], st)
+        if st % p["K"] == 0:
+            a.numGhost = 0
+            m.numGhost = 0
+            orc.update_molecules(m, a, slab)
+            orc.multires_map_into_domain(sd, m, a)
+            corr = orc.multires_create_ghosts(m, a, sd)
+            co, no = orc.build_half_list(m.pos, m.numLocal + m.numGhost, 0, m.numLocal, rlist,
+                                         sd.minGhostCorner, sd.maxGhostCorner, 1.0, 96)
+        else:
+            orc.update_ghosts(a, corr, sd)
+        orc.update_molecules(m, a, slab)
+        a.force[:] = 0
+        m.force[:] = 0
+        energies.append(ljig.run(m, co, no, a))
+        orc.contribute_molecule_force(m, a)
+        tf.apply(a)
+        orc.ghost_to_real(a, corr)
+        orc.vv_post(a, p["dt"])
+        if st % p["S"] == 0:
+            tf.sample(a)
+        if (st + 1) % p["U"] == 0:
+            tf.update(p["tfs"], p["tfr"])
+    return a.pos[:n].copy(), a.vel[:n].copy(), np.array(energies), tf.force[:, 0].copy()
+
+
+def gpu_system(M, pos, vel, box, p, precision, graph=True):
+    return M.AdResSSystem(pos, vel, [0, 0, 0], box, [box[0] / 2, box[1] / 2, box[2] / 2], p["at"], p["hy"],
+                          p["nu"], rc=p["rc"], skin=p["skin"], sigma=p["sigma"], epsilon=p["epsilon"],
+                          capping_distance=p["cap"], precision=precision, dt=p["dt"], rebuild_interval=p["K"],
+                          gamma=p["gamma"], temperature=p["T"], seed=p["seed"], tf=True, tf_bin_width=p["binw"],
+                          tf_target_density=p["rho"], tf_modulation=p["mod"], tf_sigma=p["tfs"],
+                          tf_range=p["tfr"], tf_sample_interval=p["S"], tf_update_interval=p["U"],
+                          use_graph=graph)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_adress_trajectory_matches_oracle(M, orc, graph):
+    box = [36.0, 10.0, 10.0]
+    pos, vel = system(1800, box, 5)
+    steps = 13
+    po, vo, eo, fo = oracle_loop(orc, pos, vel, box, steps, P)
+    s = gpu_system(M, pos, vel, box, P, M.PREC_FP64, graph)
+    eg = s.run(steps)
+    pg, vg, _ = s.state()
+    # Langevin noise and the Slab weights go through exp/log/cos/sin, which may
+    # differ by ulps between host and device libraries
+    np.testing.assert_allclose(pg, po, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(vg, vo, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(eg, eo, rtol=1e-9)
+    fg, _ = s.thermodynamic_force()
+    np.testing.assert_allclose(fg, fo, rtol=1e-9, atol=1e-12)
+    st = s.stats()
+    assert st["steps"] == steps and st["rebuilds"] == 3 and st["ghost_molecules"] > 0
+
+
+def test_adress_mixed_close_to_fp64(M):
+    box = [36.0, 10.0, 10.0]
+    pos, vel = system(1800, box, 6)
+    a = gpu_system(M, pos, vel, box, P, M.PREC_FP64)
+    b = gpu_system(M, pos, vel, box, P, M.PREC_MIXED)
+    ea = a.run(6)
+    eb = b.run(6)
+    pa, va, _ = a.state()
+    pb, vb, _ = b.state()
+    np.testing.assert_allclose(eb, ea, rtol=1e-6)
+    # the mixed form evaluates pair energies in FP32 and the AdResS drift force
+    # (-V_ij/2 grad lambda) uses them; on this random start (capped forces of
+    # 1000 sigma/eps) six steps move positions by < 1e-7
+    assert np.abs(pa - pb).max() < 1e-7
