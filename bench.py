@@ -257,12 +257,137 @@ def time_pair_kernel(torch, sysm, stream, reps=20):
     return ev0.elapsed_time(ev1) / reps
 
 
+ADRESS = dict(n=34560, box=(120.0, 24.0, 24.0), center=(60.0, 12.0, 12.0), at=30.0, hy=10.0, nu=1, rc=2.5,
+              skin=0.3, cap=0.78420, gamma=1.0, T=1.0, binw=1.2, rho=0.5, mod=1.0, tfs=2.4, tfr=3.0, S=1,
+              U=1000, dt=0.005, K=10)
+ADRESS_WORKLOAD = ("AdResS LJ<->ideal gas, 34,560 single-site molecules in 120x24x24, atomistic slab 30, hybrid 10, "
+                   "cos^2, rc 2.5 with force cap 1000 (r_cap 0.7842), Langevin T=1 gamma=1, thermodynamic force "
+                   "100 bins sampled every step / updated every 1000, rebuild/10, dt 0.005")
+
+
+def adress_initial(seed=0):
+    c = ADRESS
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0.0, 1.0, (c["n"], 3)) * np.asarray(c["box"])
+    vel = mb_velocities(c["n"], c["T"], seed + 1)
+    return pos, vel
+
+
+def run_adress_cpu(pos, vel, steps, warmup, budget_s, threads):
+    """Oracle loop of the AdResS step (the composition in mrmd_gb300/csrc/adress_md.cu)."""
+    from oracle import oracle as O
+
+    O.set_threads(threads)
+    c = ADRESS
+    n = len(pos)
+    rlist = c["rc"] + c["skin"]
+    sd = O.subdomain([0, 0, 0], list(c["box"]), rlist)
+    a = O.Atoms.from_positions(pos, capacity=3 * n)
+    a.vel[:n] = vel
+    m = O.Molecules(3 * n)
+    m.atomsOffset[:n] = np.arange(n)
+    m.numAtoms[:n] = 1
+    m.numLocal = n
+    slab = O.slab(list(c["center"]), c["at"], c["hy"], c["nu"])
+    ljig = O.LJIdealGas(c["cap"], c["rc"], 1.0, 1.0, True)
+    tf = O.ThermodynamicForce([c["rho"]], sd, c["binw"], [c["mod"]], False, True)
+    st = {"corr": None, "list": None}
+
+    def step(s):
+        O.langevin_pre(a, c["dt"], c["gamma"], c["T"], 1234, s)
+        if s % c["K"] == 0:
+            a.numGhost = 0
+            m.numGhost = 0
+            O.update_molecules(m, a, slab)
+            O.multires_map_into_domain(sd, m, a)
+            st["corr"] = O.multires_create_ghosts(m, a, sd)
+            st["list"] = O.build_half_list(m.pos, m.numLocal + m.numGhost, 0, m.numLocal, rlist,
+                                           sd.minGhostCorner, sd.maxGhostCorner, 1.0, 64)
+        else:
+            O.update_ghosts(a, st["corr"], sd)
+        O.update_molecules(m, a, slab)
+        a.force[: a.n] = 0.0
+        m.force[: m.numLocal + m.numGhost] = 0.0
+        ljig.run(m, st["list"][0], st["list"][1], a)
+        O.contribute_molecule_force(m, a)
+        tf.apply(a)
+        O.ghost_to_real(a, st["corr"])
+        O.vv_post(a, c["dt"])
+        if s % c["S"] == 0:
+            tf.sample(a)
+        if (s + 1) % c["U"] == 0:
+            tf.update(c["tfs"], c["tfr"])
+
+    s = 0
+    for _ in range(warmup):
+        step(s)
+        s += 1
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        step(s)
+        s += 1
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dtime = time.perf_counter() - t0
+    return n * done / dtime, done, dtime
+
+
+def adress_main(args, rank, world, local_rank):
+    """Config-2 AdResS step, FP64 and mixed forms (a separate measurement line)."""
+    import torch
+
+    import mrmd_gb300 as M
+
+    torch.cuda.set_device(local_rank)
+    ctx = M.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    c = ADRESS
+    pos, vel = adress_initial(100 + rank)
+    n = len(pos)
+    res = {}
+    for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        s = M.AdResSSystem(pos, vel, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], c["hy"], c["nu"],
+                           rc=c["rc"], skin=c["skin"], capping_distance=c["cap"], precision=prec, dt=c["dt"],
+                           rebuild_interval=c["K"], gamma=c["gamma"], temperature=c["T"], tf=True,
+                           tf_bin_width=c["binw"], tf_target_density=c["rho"], tf_modulation=c["mod"],
+                           tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
+                           tf_update_interval=c["U"], ctx=ctx)
+        s.run(args.warmup)
+        with ClockSampler(local_rank) as clk:
+            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream)
+        res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
+                         stats=s.stats())
+        s.close()
+    cpu = None
+    if not args.no_cpu:
+        ncores, model = cpu_info()
+        cv, done, ctime = run_adress_cpu(pos, vel, 10 ** 6, 3, args.cpu_budget, ncores)
+        cpu = {"value": cv, "unit": METRIC, "cores": ncores, "kind": "port",
+               "sample": f"{done} steps of the {n}-molecule system, {ncores} OpenMP threads ({model})"}
+    head = "mixed" if "mixed" in res else next(iter(res))
+    r = res[head]
+    print(json.dumps({
+        "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f64 state, f32 double-float pair arithmetic",
+        "data": "synthetic (seeded uniform positions, Maxwell-Boltzmann velocities)",
+        "config": {"workload": ADRESS_WORKLOAD, "molecules": n, "form": head,
+                   "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
+                                 "kernel_launches": res[f]["launches"], "list_pairs": res[f]["stats"]["pairs"],
+                                 "ghost_molecules": res[f]["stats"]["ghost_molecules"]} for f in res}},
+        "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--workload", choices=["lj", "adress"], default="lj")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")
@@ -276,6 +401,9 @@ def main():
 
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "adress":
+        adress_main(args, rank, world, local_rank)
         return
 
     import torch

@@ -821,6 +821,9 @@ double orc_ljig_run(orc_ljig* s, orc_molecules* mol, const int32_t* counts, cons
     const int64_t* atype = atoms->type;
     double sumEnergy = 0.0;
 
+    /* one task per local molecule (parallel_reduce); shared updates are
+     * atomic as the reference's atomic_access_slice / ScatterView */
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : sumEnergy) if (g_threads > 1)
     for (int64_t alpha = 0; alpha < mol->numLocal; ++alpha)
     {
         double forceTmpAlpha[3] = {0.0, 0.0, 0.0};
@@ -861,9 +864,13 @@ double orc_ljig_run(orc_ljig* s, orc_molecules* mol, const int32_t* counts, cons
                     forceTmpIdx[0] += dx * ffactor;
                     forceTmpIdx[1] += dy * ffactor;
                     forceTmpIdx[2] += dz * ffactor;
-                    afor[3 * jdx + 0] -= dx * ffactor;
-                    afor[3 * jdx + 1] -= dy * ffactor;
-                    afor[3 * jdx + 2] -= dz * ffactor;
+                    const double fjx = dx * ffactor, fjy = dy * ffactor, fjz = dz * ffactor;
+#pragma omp atomic
+                    afor[3 * jdx + 0] -= fjx;
+#pragma omp atomic
+                    afor[3 * jdx + 1] -= fjy;
+#pragma omp atomic
+                    afor[3 * jdx + 2] -= fjz;
                     sumEnergy += e * weighting;
                     double Vij = 0.5 * e;
                     if (is_hy(modLamA) || is_hy(modLamB))
@@ -879,25 +886,40 @@ double orc_ljig_run(orc_ljig* s, orc_molecules* mol, const int32_t* counts, cons
                             int64_t binBeta = -1;
                             if (is_hy(modLamB)) binBeta = comp_bin(mol->lambda[beta]);
                             if (is_hy(modLamA) && binAlpha != -1)
+                            {
+#pragma omp atomic
                                 s->compensationEnergy[binAlpha * nt + atype[idx]] += Vij;
+                            }
                             if (is_hy(modLamB) && binBeta != -1)
+                            {
+#pragma omp atomic
                                 s->compensationEnergy[binBeta * nt + atype[jdx]] += Vij;
+                            }
                         }
                     }
                 }
+#pragma omp atomic
                 afor[3 * idx + 0] += forceTmpIdx[0];
+#pragma omp atomic
                 afor[3 * idx + 1] += forceTmpIdx[1];
+#pragma omp atomic
                 afor[3 * idx + 2] += forceTmpIdx[2];
             }
+#pragma omp atomic
             mol->force[3 * beta + 0] += forceTmpBeta[0];
+#pragma omp atomic
             mol->force[3 * beta + 1] += forceTmpBeta[1];
+#pragma omp atomic
             mol->force[3 * beta + 2] += forceTmpBeta[2];
         }
         if (sampling)
         {
             for (int64_t a = sA; a < eA; ++a)
                 if (is_hy(modLamA) && binAlpha != -1)
+                {
+#pragma omp atomic
                     s->compensationEnergyCounter[binAlpha * nt + atype[a]] += 1.0;
+                }
         }
         if (is_hy(modLamA) && binAlpha != -1)
         {
@@ -906,8 +928,11 @@ double orc_ljig_run(orc_ljig* s, orc_molecules* mol, const int32_t* counts, cons
             forceTmpAlpha[1] += me * gA[1];
             forceTmpAlpha[2] += me * gA[2];
         }
+#pragma omp atomic
         mol->force[3 * alpha + 0] += forceTmpAlpha[0];
+#pragma omp atomic
         mol->force[3 * alpha + 1] += forceTmpAlpha[1];
+#pragma omp atomic
         mol->force[3 * alpha + 2] += forceTmpAlpha[2];
     }
 
