@@ -65,6 +65,8 @@ def load_traffic(kernel):
         return None
     with open(p) as f:
         for line in f:
+            if line.lstrip().startswith("#"):
+                continue
             parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
             if parts.get("kernel") == kernel and "dram_bytes_per_atom" in parts:
                 return float(parts["dram_bytes_per_atom"])
@@ -481,7 +483,7 @@ def main():
         bytes_per_atom = 32 + 24 + 4 * (1 + nbar)  # split coords read, F written, full list
         kname = "lj_mixed_full"
     else:
-        bytes_per_atom = 24 + 24 + 4 * (1 + nbar)  # SURVEY 8(d) pair formula
+        bytes_per_atom = 24 + 24 + 4 * (1 + nbar)  # positions read, F written, half list
         kname = "lj_fp64"
     peak, peak_kind = load_peaks()
     achieved = bytes_per_atom * n / (kern_ms * 1e-3) / 1e9
