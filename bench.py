@@ -275,18 +275,19 @@ def adress_initial(seed=0):
     return pos, vel
 
 
-def run_adress_cpu(pos, vel, steps, warmup, budget_s, threads):
-    """Oracle loop of the AdResS step (the composition in mrmd_gb300/csrc/adress_md.cu)."""
+def run_adress_cpu(pos, vel, steps, warmup, budget_s, threads, geometry=None):
+    """Oracle loop of the AdResS step (the composition in mrmd_gb300/csrc/adress_md.cu).
+    geometry overrides box, center, at and hy of the AdResS workload."""
     from oracle import oracle as O
 
     O.set_threads(threads)
-    c = ADRESS
+    c = dict(ADRESS, **(geometry or {}))
     n = len(pos)
     rlist = c["rc"] + c["skin"]
     sd = O.subdomain([0, 0, 0], list(c["box"]), rlist)
-    a = O.Atoms.from_positions(pos, capacity=3 * n)
+    a = O.Atoms.from_positions(pos, capacity=8 * n + 64)
     a.vel[:n] = vel
-    m = O.Molecules(3 * n)
+    m = O.Molecules(8 * n + 64)
     m.atomsOffset[:n] = np.arange(n)
     m.numAtoms[:n] = 1
     m.numLocal = n
@@ -304,7 +305,7 @@ def run_adress_cpu(pos, vel, steps, warmup, budget_s, threads):
             O.multires_map_into_domain(sd, m, a)
             st["corr"] = O.multires_create_ghosts(m, a, sd)
             st["list"] = O.build_half_list(m.pos, m.numLocal + m.numGhost, 0, m.numLocal, rlist,
-                                           sd.minGhostCorner, sd.maxGhostCorner, 1.0, 64)
+                                           sd.minGhostCorner, sd.maxGhostCorner, 1.0, 96)
         else:
             O.update_ghosts(a, st["corr"], sd)
         O.update_molecules(m, a, slab)
@@ -383,13 +384,118 @@ def adress_main(args, rank, world, local_rank):
         "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}), flush=True)
 
 
+BATCH = dict(replicas=512, nmin=1000, nmax=50000, cross=20.0, rho=(0.4, 0.6), at=(10.0, 30.0), hy=8.0,
+             graph=50, seed=4)
+BATCH_WORKLOAD = ("512 independent AdResS replicas (LJ<->ideal gas, single-site), sizes log-uniform 1,000-50,000, "
+                  "cross-section 20x20, density U(0.4, 0.6), atomistic slab U(10, 30), hybrid 8, otherwise the "
+                  "34,560-molecule AdResS workload's physics; one launch per phase for all replicas, CUDA graphs "
+                  "of 50 steps")
+
+
+def batch_replicas(M, count=None):
+    """Seeded replica set: sizes, boxes, slabs and initial states."""
+    b = BATCH
+    rng = np.random.default_rng(b["seed"])
+    R = count or b["replicas"]
+    sizes = np.exp(rng.uniform(np.log(b["nmin"]), np.log(b["nmax"]), R)).astype(np.int64)
+    rhos = rng.uniform(*b["rho"], R)
+    ats = rng.uniform(*b["at"], R)
+    reps, P_, V_, geoms = [], [], [], []
+    for r in range(R):
+        lx = float(sizes[r] / (b["cross"] * b["cross"] * rhos[r]))
+        box = (lx, b["cross"], b["cross"])
+        center = (lx / 2, b["cross"] / 2, b["cross"] / 2)
+        reps.append(M.Replica(int(sizes[r]), [0, 0, 0], box, center, float(ats[r]), 10_000 + r))
+        P_.append(rng.uniform(0.0, 1.0, (int(sizes[r]), 3)) * np.asarray(box))
+        V_.append(rng.normal(0.0, 1.0, (int(sizes[r]), 3)))
+        geoms.append(dict(box=box, center=center, at=float(ats[r]), hy=b["hy"]))
+    return reps, np.concatenate(P_), np.concatenate(V_), geoms
+
+
+def batch_main(args, rank, world, local_rank):
+    """Config-4 batch of AdResS replicas, FP64 and mixed forms."""
+    import torch
+
+    import mrmd_gb300 as M
+
+    torch.cuda.set_device(local_rank)
+    ctx = M.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    c = ADRESS
+    reps, pos, vel, geoms = batch_replicas(M)
+    n = len(pos)
+    res = {}
+    forces = {}
+    for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        s = M.BatchSystem(reps, pos, vel, hybrid_diameter=BATCH["hy"], nu=c["nu"], rc=c["rc"], skin=c["skin"],
+                          capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
+                          temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
+                          tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
+                          tf_update_interval=c["U"], threads_per_row=1, block_size=128, rebuild_interval=c["K"],
+                          sort_every=5, graph_steps=BATCH["graph"], ctx=ctx)
+        s.run(1)
+        forces[form] = s.state()[2]
+        s.run(BATCH["graph"] - 1)
+        tuned, trials = (s.tuning, []) if args.no_autotune else s.autotune(trial_steps=BATCH["graph"])
+        s.run(args.warmup)
+        with ClockSampler(local_rank) as clk:
+            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream)
+        res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
+                         stats=s.stats(), tuning=tuned,
+                         trials=[dict(t, ms_per_step=m) for t, m in trials])
+        s.close()
+    ferr = None
+    if "fp64" in forces and "mixed" in forces:
+        fa, fb = forces["fp64"], forces["mixed"]
+        d = np.linalg.norm(fa - fb, axis=1)
+        mag = np.linalg.norm(fa, axis=1)
+        rms = float(np.sqrt((mag ** 2).mean()))
+        ferr = {"max_abs_over_rms": float(d.max() / rms),
+                "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
+    cpu = None
+    if not args.no_cpu:
+        ncores, model = cpu_info()
+        done_total, t_total, atoms_steps = 0, 0.0, 0.0
+        budget = args.cpu_budget
+        for r in range(3):  # the first replicas of the set, one after another
+            sl = slice(int(sum(x.num_molecules for x in reps[:r])), int(sum(x.num_molecules for x in reps[:r + 1])))
+            cv, done, ctime = run_adress_cpu(pos[sl], vel[sl], 10 ** 6, 1, budget / 3, ncores, geoms[r])
+            atoms_steps += cv * ctime
+            t_total += ctime
+            done_total += done
+        cpu = {"value": atoms_steps / t_total, "unit": METRIC, "cores": ncores, "kind": "port",
+               "sample": f"the first 3 replicas run one after another by the oracle loop, {done_total} steps in "
+                         f"{t_total:.1f} s, {ncores} OpenMP threads ({model})"}
+    head = "mixed" if "mixed" in res else next(iter(res))
+    r = res[head]
+    out = {
+        "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f64 state, f32 double-float pair arithmetic",
+        "data": "synthetic (seeded replica sizes, boxes and slabs; uniform positions, normal velocities)",
+        "config": {"workload": BATCH_WORKLOAD, "replicas": len(reps), "molecules": n, "form": head,
+                   "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
+                                 "kernel_launches": res[f]["launches"], "list_pairs": res[f]["stats"]["pairs"],
+                                 "ghost_molecules": res[f]["stats"]["ghost_molecules"],
+                                 "graph_launches": res[f]["stats"]["graph_launches"],
+                                 "tuning": res[f]["tuning"], "autotune_trials": res[f]["trials"]}
+                             for f in res}},
+        "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}
+    if "fp64" in res and "mixed" in res:
+        out["config"]["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+        out["config"]["force_error_mixed_vs_fp64"] = ferr
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["lj", "adress"], default="lj")
+    ap.add_argument("--workload", choices=["lj", "adress", "batch"], default="lj")
+    ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")
@@ -406,6 +512,9 @@ def main():
         return
     if args.workload == "adress":
         adress_main(args, rank, world, local_rank)
+        return
+    if args.workload == "batch":
+        batch_main(args, rank, world, local_rank)
         return
 
     import torch

@@ -457,6 +457,85 @@ int mrmd_adress_set_tf(mrmd_ctx* ctx, mrmd_adress* s, const double* force);
 /* [0] steps, [1] rebuilds, [2] molecule list pairs, [3] ghost molecules */
 int mrmd_adress_stats(const mrmd_adress* s, int64_t* out4);
 
+/* ------------------------------------------ batched AdResS replicas -- */
+/* Many independent single-site AdResS systems (the step of mrmd_adress:
+ * LJ_IdealGas::run, LJ_IdealGas.cpp:227-260; VelocityVerletLangevinThermostat,
+ * VelocityVerletLangevinThermostat.hpp:48-121; UpdateMolecules + Slab,
+ * UpdateMolecules.hpp:24-70; MultiResGhostLayer; ThermodynamicForce
+ * apply/sample/update, ThermodynamicForce.cpp:74-96) of different sizes and
+ * geometries, advanced together: one launch per phase for all replicas,
+ * whole rebuild cycles replayed as CUDA graphs.  Each replica's trajectory
+ * is bitwise the one it has when run alone with the same tuning (the force
+ * of every molecule is summed over a full list in a fixed order). */
+typedef struct mrmd_batch mrmd_batch;
+typedef struct {
+    int64_t numMolecules;
+    double boxMin[3];
+    double boxMax[3];
+    double slabCenter[3];
+    double atomisticDiameter;
+    uint64_t seed;            /* Langevin noise key of this replica */
+} mrmd_replica_desc;
+
+typedef struct {
+    int32_t threadsPerRow;    /* lanes sharing one molecule's neighbour row: 1, 2, 4 or 8 */
+    int32_t blockSize;        /* pair-kernel block: 64..1024, multiple of 32 */
+    int64_t rebuildInterval;  /* steps between list rebuilds */
+    int64_t sortEvery;        /* cell-sort the molecules at every k-th rebuild; 0 = never */
+    int64_t graphSteps;       /* steps per CUDA graph (0 = no graphs); a multiple of
+                                 rebuildInterval * max(sortEvery, 1) */
+} mrmd_batch_tuning;
+
+typedef struct {
+    double rc, skin, sigma, epsilon, cappingDistance;
+    int32_t shifted;
+    int32_t precision;        /* MRMD_PREC_FP64 or MRMD_PREC_MIXED */
+    double dt;
+    double hybridDiameter;
+    int64_t nu;
+    double gamma, temperature;
+    int32_t tfEnabled;
+    int32_t reserved0;
+    double tfBinWidth, tfTargetDensity, tfModulation, tfSmoothingSigma, tfSmoothingRange;
+    int64_t tfSampleInterval, tfUpdateInterval;
+    int64_t compSamplingInterval; /* LJ_IdealGas intervals; 0 = the reference's 200 */
+    int64_t compUpdateInterval;   /* 0 = the reference's 20000 */
+    int64_t initialMaxNeighbors;  /* 0 = measured at creation */
+    int64_t initialGhostCapacity; /* 0 = measured at creation */
+    mrmd_batch_tuning tuning;
+} mrmd_batch_config;
+
+/* pos3/vel3: [sum numMolecules][3], replica after replica. */
+int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* cfg, int64_t numReplicas,
+                      const mrmd_replica_desc* replicas, const double* pos3, const double* vel3);
+int mrmd_batch_destroy(mrmd_ctx* ctx, mrmd_batch* b);
+/* Advance nsteps; energies (may be NULL): [nsteps][numReplicas] LJ_IdealGas energies. */
+int mrmd_batch_run(mrmd_ctx* ctx, mrmd_batch* b, int64_t nsteps, double* energies);
+/* State in the input order ([sum n][3] each, NULL skips). */
+int mrmd_batch_get_state(mrmd_ctx* ctx, mrmd_batch* b, double* pos3, double* vel3, double* force3);
+/* Thermodynamic-force tables and density counts of all replicas, concatenated;
+ * binOffsets [numReplicas + 1]. */
+int mrmd_batch_get_tf(mrmd_ctx* ctx, mrmd_batch* b, double* force, double* density, int64_t* binOffsets);
+int mrmd_batch_set_tf(mrmd_ctx* ctx, mrmd_batch* b, const double* force);
+/* Mean drift-compensation energies [numReplicas][200]. */
+int mrmd_batch_get_compensation(mrmd_ctx* ctx, mrmd_batch* b, double* mean);
+int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t);
+int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning* t);
+/* Time each candidate tuning (lanes per row, block size, rebuild interval)
+ * on trialSteps steps from the current state (restored after every trial)
+ * and set the fastest.  A rebuild interval longer than the configured one is
+ * accepted only if no molecule moved skin/2 away from its position at the
+ * last rebuild during the trial.  msPerStep (may be NULL) receives
+ * [numCandidates] timings (negative = rejected), candidates (may be NULL) the
+ * tunings tried (at most 64). */
+int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_batch_tuning* best,
+                        double* msPerStep, mrmd_batch_tuning* candidates, int64_t* numCandidates);
+/* [0] steps, [1] rebuilds, [2] list pairs, [3] ghosts, [4] graph launches,
+ * [5] kernel launches, [6] overflow recoveries, [7] list capacity,
+ * [8] ghost capacity, [9] flags (1 ghost overflow, 2 list overflow,
+ * 4 a molecule moved skin/2 from its position at the last rebuild) */
+int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10);
+
 #ifdef __cplusplus
 }
 #endif

@@ -770,5 +770,169 @@ class AdResSSystem:
             pass
 
 
+class Replica:
+    """One replica of a batch: molecule count, box, slab centre and width, noise key."""
+
+    def __init__(self, num_molecules, box_min, box_max, slab_center, atomistic_diameter, seed):
+        self.num_molecules = int(num_molecules)
+        self.box_min = tuple(float(v) for v in box_min)
+        self.box_max = tuple(float(v) for v in box_max)
+        self.slab_center = tuple(float(v) for v in slab_center)
+        self.atomistic_diameter = float(atomistic_diameter)
+        self.seed = int(seed)
+
+    def _struct(self):
+        r = _abi.ReplicaS()
+        r.numMolecules = self.num_molecules
+        r.boxMin = (C.c_double * 3)(*self.box_min)
+        r.boxMax = (C.c_double * 3)(*self.box_max)
+        r.slabCenter = (C.c_double * 3)(*self.slab_center)
+        r.atomisticDiameter = self.atomistic_diameter
+        r.seed = self.seed
+        return r
+
+
+def _tuning_dict(t):
+    return dict(threads_per_row=int(t.threadsPerRow), block_size=int(t.blockSize),
+                rebuild_interval=int(t.rebuildInterval), sort_every=int(t.sortEvery),
+                graph_steps=int(t.graphSteps))
+
+
+def _tuning_struct(d):
+    t = _abi.BatchTuningS()
+    t.threadsPerRow = int(d["threads_per_row"])
+    t.blockSize = int(d["block_size"])
+    t.rebuildInterval = int(d["rebuild_interval"])
+    t.sortEvery = int(d["sort_every"])
+    t.graphSteps = int(d["graph_steps"])
+    return t
+
+
+class BatchSystem:
+    """Many independent single-site AdResS replicas advanced together (mrmd_batch_*).
+
+    `replicas` is a list of Replica; pos/vel are the replicas' molecules
+    concatenated in that order.  Physics parameters are shared, as in
+    AdResSSystem; the tuning (lanes per row, block size, rebuild interval,
+    sort interval, graph length) can be set or picked by autotune()."""
+
+    def __init__(self, replicas, pos, vel, hybrid_diameter, nu=1, rc=2.5, skin=0.3, sigma=1.0,
+                 epsilon=1.0, capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
+                 gamma=1.0, temperature=1.0, tf=True, tf_bin_width=1.2, tf_target_density=0.5,
+                 tf_modulation=1.0, tf_sigma=2.4, tf_range=3.0, tf_sample_interval=1,
+                 tf_update_interval=1000, comp_sampling_interval=0, comp_update_interval=0,
+                 threads_per_row=1, block_size=128, rebuild_interval=10, sort_every=5, graph_steps=50,
+                 initial_max_neighbors=0, initial_ghost_capacity=0, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        pos = _f64(pos)
+        vel = _f64(vel)
+        self.replicas = list(replicas)
+        self.sizes = np.array([r.num_molecules for r in self.replicas], dtype=np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+        self.n = int(self.offsets[-1])
+        if pos.shape != (self.n, 3) or vel.shape != (self.n, 3):
+            raise ValueError("pos/vel must be [sum of replica sizes][3]")
+        c = _abi.BatchConfigS()
+        c.rc, c.skin, c.sigma, c.epsilon = rc, skin, sigma, epsilon
+        c.cappingDistance = capping_distance
+        c.shifted = int(bool(shifted))
+        c.precision = int(precision)
+        c.dt = dt
+        c.hybridDiameter, c.nu = hybrid_diameter, int(nu)
+        c.gamma, c.temperature = gamma, temperature
+        c.tfEnabled = int(bool(tf))
+        c.tfBinWidth, c.tfTargetDensity, c.tfModulation = tf_bin_width, tf_target_density, tf_modulation
+        c.tfSmoothingSigma, c.tfSmoothingRange = tf_sigma, tf_range
+        c.tfSampleInterval, c.tfUpdateInterval = int(tf_sample_interval), int(tf_update_interval)
+        c.compSamplingInterval, c.compUpdateInterval = int(comp_sampling_interval), int(comp_update_interval)
+        c.initialMaxNeighbors, c.initialGhostCapacity = int(initial_max_neighbors), int(initial_ghost_capacity)
+        c.tuning = _tuning_struct(dict(threads_per_row=threads_per_row, block_size=block_size,
+                                       rebuild_interval=rebuild_interval, sort_every=sort_every,
+                                       graph_steps=graph_steps))
+        self.cfg = c
+        reps = (_abi.ReplicaS * len(self.replicas))(*[r._struct() for r in self.replicas])
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.mrmd_batch_create(self.ctx.h, C.byref(h), C.byref(c), len(self.replicas),
+                                                      reps, _dp(pos), _dp(vel)), "BatchSystem")
+        self.h = h
+
+    @property
+    def num_replicas(self):
+        return len(self.replicas)
+
+    def run(self, nsteps: int, energies: bool = True):
+        """Advance nsteps; returns the [nsteps][replicas] LJ_IdealGas energies."""
+        e = np.zeros((max(nsteps, 1), self.num_replicas)) if energies else None
+        self.ctx.check(self.ctx.lib.mrmd_batch_run(self.ctx.h, self.h, int(nsteps), _dp(e)), "run")
+        return e[:nsteps] if energies else None
+
+    def state(self):
+        p, v, f = (np.zeros((self.n, 3)) for _ in range(3))
+        self.ctx.check(self.ctx.lib.mrmd_batch_get_state(self.ctx.h, self.h, _dp(p), _dp(v), _dp(f)), "state")
+        return p, v, f
+
+    def replica_slice(self, r):
+        return slice(int(self.offsets[r]), int(self.offsets[r + 1]))
+
+    def thermodynamic_force(self):
+        """(tables, densities): lists with one array per replica."""
+        off = np.zeros(self.num_replicas + 1, dtype=np.int64)
+        self.ctx.check(self.ctx.lib.mrmd_batch_get_tf(self.ctx.h, self.h, None, None, _ip(off)), "tf")
+        f, d = np.zeros(max(int(off[-1]), 1)), np.zeros(max(int(off[-1]), 1))
+        self.ctx.check(self.ctx.lib.mrmd_batch_get_tf(self.ctx.h, self.h, _dp(f), _dp(d), None), "tf")
+        return ([f[off[r]:off[r + 1]] for r in range(self.num_replicas)],
+                [d[off[r]:off[r + 1]] for r in range(self.num_replicas)])
+
+    def set_thermodynamic_force(self, tables):
+        self.ctx.check(self.ctx.lib.mrmd_batch_set_tf(self.ctx.h, self.h, _dp(_f64(np.concatenate(tables)))),
+                       "set tf")
+
+    def compensation(self):
+        m = np.zeros((self.num_replicas, 200))
+        self.ctx.check(self.ctx.lib.mrmd_batch_get_compensation(self.ctx.h, self.h, _dp(m)), "compensation")
+        return m
+
+    @property
+    def tuning(self):
+        t = _abi.BatchTuningS()
+        self.ctx.lib.mrmd_batch_get_tuning(self.h, C.byref(t))
+        return _tuning_dict(t)
+
+    @tuning.setter
+    def tuning(self, d):
+        t = _tuning_struct({**self.tuning, **d})
+        self.ctx.check(self.ctx.lib.mrmd_batch_set_tuning(self.ctx.h, self.h, C.byref(t)), "tuning")
+
+    def autotune(self, trial_steps=50):
+        """Time the candidate tunings from the current state and keep the fastest safe one.
+        Returns (best, [(candidate, ms_per_step or None if rejected), ...])."""
+        best = _abi.BatchTuningS()
+        ms = np.zeros(64)
+        cands = (_abi.BatchTuningS * 64)()
+        n = C.c_int64()
+        self.ctx.check(self.ctx.lib.mrmd_batch_autotune(self.ctx.h, self.h, int(trial_steps), C.byref(best),
+                                                        _dp(ms), cands, C.byref(n)), "autotune")
+        trials = [(_tuning_dict(cands[k]), float(ms[k]) if ms[k] >= 0 else None) for k in range(n.value)]
+        return _tuning_dict(best), trials
+
+    def stats(self):
+        out = np.zeros(10, dtype=np.int64)
+        self.ctx.check(self.ctx.lib.mrmd_batch_stats(self.ctx.h, self.h, _ip(out)), "stats")
+        keys = ["steps", "rebuilds", "pairs", "ghost_molecules", "graph_launches", "kernel_launches",
+                "recoveries", "list_capacity", "ghost_capacity", "flags"]
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.mrmd_batch_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def version() -> str:
     return _abi.lib().mrmd_version().decode()

@@ -103,6 +103,29 @@ class AdResSConfigS(C.Structure):
                 ("maxNeighbors", C.c_int64)]
 
 
+class ReplicaS(C.Structure):
+    _fields_ = [("numMolecules", C.c_int64), ("boxMin", C.c_double * 3), ("boxMax", C.c_double * 3),
+                ("slabCenter", C.c_double * 3), ("atomisticDiameter", C.c_double), ("seed", C.c_uint64)]
+
+
+class BatchTuningS(C.Structure):
+    _fields_ = [("threadsPerRow", C.c_int32), ("blockSize", C.c_int32), ("rebuildInterval", C.c_int64),
+                ("sortEvery", C.c_int64), ("graphSteps", C.c_int64)]
+
+
+class BatchConfigS(C.Structure):
+    _fields_ = [("rc", C.c_double), ("skin", C.c_double), ("sigma", C.c_double), ("epsilon", C.c_double),
+                ("cappingDistance", C.c_double), ("shifted", C.c_int32), ("precision", C.c_int32),
+                ("dt", C.c_double), ("hybridDiameter", C.c_double), ("nu", C.c_int64),
+                ("gamma", C.c_double), ("temperature", C.c_double), ("tfEnabled", C.c_int32),
+                ("reserved0", C.c_int32), ("tfBinWidth", C.c_double), ("tfTargetDensity", C.c_double),
+                ("tfModulation", C.c_double), ("tfSmoothingSigma", C.c_double),
+                ("tfSmoothingRange", C.c_double), ("tfSampleInterval", C.c_int64),
+                ("tfUpdateInterval", C.c_int64), ("compSamplingInterval", C.c_int64),
+                ("compUpdateInterval", C.c_int64), ("initialMaxNeighbors", C.c_int64),
+                ("initialGhostCapacity", C.c_int64), ("tuning", BatchTuningS)]
+
+
 P = C.POINTER
 _v = C.c_void_p
 _i = C.c_int
@@ -197,6 +220,17 @@ SIGNATURES = {
     "mrmd_adress_get_tf": (_i, [_v, _v, c_double_p, c_double_p, c_int64_p]),
     "mrmd_adress_set_tf": (_i, [_v, _v, c_double_p]),
     "mrmd_adress_stats": (_i, [_v, c_int64_p]),
+    "mrmd_batch_create": (_i, [_v, P(_v), P(BatchConfigS), _i64, P(ReplicaS), c_double_p, c_double_p]),
+    "mrmd_batch_destroy": (_i, [_v, _v]),
+    "mrmd_batch_run": (_i, [_v, _v, _i64, c_double_p]),
+    "mrmd_batch_get_state": (_i, [_v, _v, c_double_p, c_double_p, c_double_p]),
+    "mrmd_batch_get_tf": (_i, [_v, _v, c_double_p, c_double_p, c_int64_p]),
+    "mrmd_batch_set_tf": (_i, [_v, _v, c_double_p]),
+    "mrmd_batch_get_compensation": (_i, [_v, _v, c_double_p]),
+    "mrmd_batch_get_tuning": (_i, [_v, P(BatchTuningS)]),
+    "mrmd_batch_set_tuning": (_i, [_v, _v, P(BatchTuningS)]),
+    "mrmd_batch_autotune": (_i, [_v, _v, _i64, P(BatchTuningS), c_double_p, P(BatchTuningS), c_int64_p]),
+    "mrmd_batch_stats": (_i, [_v, _v, c_int64_p]),
     "mrmd_md_atoms": (P(AtomsS), [_v]),
     "mrmd_md_nlist": (P(NListS), [_v]),
 }

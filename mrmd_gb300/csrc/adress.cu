@@ -8,70 +8,13 @@
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
 #include "nlist_impl.cuh"
+#include "adress_impl.cuh"
 
 using namespace mrmd_impl;
 
 namespace
 {
 constexpr int TB = 256;
-constexpr int COMP_BINS = 200;  // LJ_IdealGas.hpp:54
-
-struct SlabDev
-{
-    double cx;
-    double atHalf;  // atomisticRegionHalfDiameter
-    double hy;      // hybridRegionDiameter
-    int64_t exponent;
-    int32_t abrupt;
-};
-
-__device__ __forceinline__ double pow_int(double x, int64_t n)
-{
-    // util/math.hpp:31-46
-    double ww = x, yy = 1.0;
-    for (int64_t nn = (n > 0) ? n : -n; nn != 0; nn >>= 1)
-    {
-        if ((nn & 1) == 1) yy *= ww;
-        ww *= ww;
-    }
-    return (n > 0) ? yy : 1.0 / yy;
-}
-
-__device__ __forceinline__ void slab_eval(const SlabDev& s, double x, double& lambda, double& modLambda,
-                                          double& gx)
-{
-    // weighting_function/Slab.hpp:161-187 (+ setSmoothWeightInHY :96-120)
-    const double pi = 3.141592653589793238462643383279502884;
-    const double dx = x - s.cx;
-    const double absDx = fabs(dx);
-    gx = 0.0;
-    if (absDx < s.atHalf)
-    {
-        lambda = 1.0;
-        modLambda = 1.0;
-    }
-    else if (absDx > s.atHalf + s.hy)
-    {
-        lambda = 0.0;
-        modLambda = 0.0;
-    }
-    else if (s.abrupt)
-    {
-        lambda = 1.0;
-        modLambda = 1.0;
-    }
-    else
-    {
-        const double arg = pi / (2.0 * s.hy) * (absDx - s.atHalf);
-        const double base = cos(arg);
-        lambda = base * base;
-        modLambda = pow_int(base, s.exponent);
-        const double factor =
-            -pi / (2.0 * s.hy) * (double)s.exponent * sin(arg) * pow_int(base, s.exponent - 1) / absDx;
-        gx = factor * dx;
-    }
-}
-
 __global__ void k_update_molecules(mrmd_molecules m, const double4* __restrict__ apos,
                                    const double* __restrict__ relMass, int64_t n, SlabDev s)
 {
@@ -117,20 +60,6 @@ __global__ void k_contribute(mrmd_molecules m, double4* __restrict__ aforce, con
             aforce[a] = f;
         }
     }
-}
-
-// CheckRegion.hpp:25-38 with REGION_CHECK_EPSILON = 0
-__device__ __forceinline__ bool is_at(double l) { return l >= 1.0; }
-__device__ __forceinline__ bool is_cg(double l) { return l <= 0.0; }
-__device__ __forceinline__ bool is_hy(double l) { return !is_at(l) && !is_cg(l); }
-
-__device__ __forceinline__ int comp_bin(double lambda)
-{
-    // MultiHistogram(0, 1, 200).getBin (data/MultiHistogram.hpp:60-66)
-    const double inv = 1.0 / ((1.0 - 0.0) / (double)COMP_BINS);
-    int64_t b = (int64_t)floor((lambda - 0.0) * inv);
-    if (b < 0 || b >= COMP_BINS) return -1;
-    return (int)b;
 }
 
 struct LJIGArgs
@@ -281,17 +210,6 @@ __global__ void k_update_mean_comp(double* __restrict__ energy, double* __restri
     }
 }
 
-SlabDev to_slab(const mrmd_slab* s)
-{
-    // Slab constructor, weighting_function/Slab.hpp:189-200
-    SlabDev d{};
-    d.cx = s->center[0];
-    d.atHalf = 0.5 * s->atomisticRegionDiameter;
-    d.hy = s->hybridRegionDiameter;
-    d.exponent = 2 * s->nu;
-    d.abrupt = s->interfaceType == 1;
-    return d;
-}
 }  // namespace
 
 struct mrmd_ljig
@@ -349,11 +267,10 @@ int mrmd_ljig_create(mrmd_ctx* ctx, mrmd_ljig** out, int64_t numTypes, const dou
     for (int64_t t = 0; t < n2; ++t) dev[(size_t)t] = to_dev(s->table[(size_t)t]);
     int rc2 = dmalloc(ctx, reinterpret_cast<void**>(&s->dTable), sizeof(LJDev) * (size_t)n2);
     if (rc2 == MRMD_OK)
-        rc2 = check_cuda(ctx, cudaMemcpy(s->dTable, dev.data(), sizeof(LJDev) * (size_t)n2, cudaMemcpyHostToDevice),
-                         "ljig table");
+        rc2 = h2d(ctx, s->dTable, dev.data(), sizeof(LJDev) * (size_t)n2);
     const size_t compBytes = sizeof(double) * 3 * COMP_BINS * (size_t)numTypes;
     if (rc2 == MRMD_OK) rc2 = dmalloc(ctx, reinterpret_cast<void**>(&s->comp), compBytes);
-    if (rc2 == MRMD_OK) rc2 = check_cuda(ctx, cudaMemset(s->comp, 0, compBytes), "ljig comp");
+    if (rc2 == MRMD_OK) rc2 = dzero(ctx, s->comp, compBytes);
     if (rc2 != MRMD_OK)
     {
         dfree(s->dTable);
@@ -475,9 +392,9 @@ int mrmd_ljig_get_compensation(mrmd_ctx* ctx, const mrmd_ljig* s, double* mean, 
 {
     if (!ctx || !s) return MRMD_ERR_ARG;
     const size_t nb = COMP_BINS * (size_t)s->numTypes;
-    if (energy) MRMD_CUDA(ctx, cudaMemcpy(energy, s->comp, sizeof(double) * nb, cudaMemcpyDeviceToHost));
-    if (counter) MRMD_CUDA(ctx, cudaMemcpy(counter, s->comp + nb, sizeof(double) * nb, cudaMemcpyDeviceToHost));
-    if (mean) MRMD_CUDA(ctx, cudaMemcpy(mean, s->comp + 2 * nb, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+    if (energy) MRMD_TRY(d2h(ctx, energy, s->comp, sizeof(double) * nb));
+    if (counter) MRMD_TRY(d2h(ctx, counter, s->comp + nb, sizeof(double) * nb));
+    if (mean) MRMD_TRY(d2h(ctx, mean, s->comp + 2 * nb, sizeof(double) * nb));
     if (runCounter) *runCounter = s->runCounter;
     return MRMD_OK;
 }
@@ -486,7 +403,7 @@ int mrmd_ljig_set_compensation(mrmd_ctx* ctx, mrmd_ljig* s, const double* mean)
 {
     if (!ctx || !s || !mean) return MRMD_ERR_ARG;
     const size_t nb = COMP_BINS * (size_t)s->numTypes;
-    MRMD_CUDA(ctx, cudaMemcpy(s->comp + 2 * nb, mean, sizeof(double) * nb, cudaMemcpyHostToDevice));
+    MRMD_TRY(h2d(ctx, s->comp + 2 * nb, mean, sizeof(double) * nb));
     return MRMD_OK;
 }
 

@@ -1,0 +1,1821 @@
+// Batched AdResS replicas: many independent single-site LJ <-> ideal-gas
+// systems of different sizes and geometries advanced together, one kernel
+// launch per phase for all replicas, replayed as CUDA graphs.
+//
+// Each replica follows the step of the fused single-system stepper
+// (VelocityVerletLangevinThermostat pre, MultiResGhostLayer, UpdateMolecules
+// with a Slab, LJ_IdealGas::run, ContributeMoleculeForceToAtoms,
+// ThermodynamicForce apply/sample/update, VelocityVerlet post).  The layout
+// and the kernels are designed for one GPU holding all replicas at once:
+//
+//  * one flat slot space: the local molecules of all replicas, replica after
+//    replica, then all ghosts; every slot knows its replica, every replica
+//    its box, slab, cell grid, noise key and thermodynamic-force table;
+//  * rebuild decisions, ghost counts and list overflow live on the device,
+//    so a whole graph of steps (rebuilds included) runs without the host;
+//    overflow is detected after the graph, the state restored from a
+//    snapshot taken before it and the graph re-run with larger buffers;
+//  * the pair force walks a FULL molecule list and writes each local force
+//    once: no atomics, no ghost forces, no fold-back, and the result is
+//    bitwise independent of the other replicas.  For a pair with a ghost the
+//    kernel uses the weights of the pair instance that Cabana's half list
+//    (lexicographic order) keeps in the reference, so that boxes whose slab
+//    reaches into the ghost layer see the reference's weights exactly;
+//  * TF application, the velocity-Verlet post kick, density sampling and
+//    the drift-compensation sampling are fused into the pair kernel's
+//    epilogue; the per-replica table updates run in one tail kernel with one
+//    block per replica.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "adress_impl.cuh"
+#include "common.cuh"
+#include "integrate_impl.cuh"
+#include "lj_impl.cuh"
+#include "lj_mixed.cuh"
+#include "nlist_impl.cuh"
+#include "thermo_impl.cuh"
+
+using namespace mrmd_impl;
+
+namespace
+{
+constexpr int TB = 256;
+constexpr double COMP_SCALE = 4294967296.0;  // 2^32: fixed point of the compensation histogram
+
+// list entries with this bit refer to a ghost whose pair instance in the
+// reference's half list is (ghost's source, image of the row molecule)
+constexpr int32_t REVERSED = (int32_t)0x80000000u;
+
+enum : uint32_t
+{
+    FLAG_GHOST_OVERFLOW = 1u,
+    FLAG_LIST_OVERFLOW = 2u,
+    FLAG_UNSAFE_INTERVAL = 4u,
+};
+
+// Per-replica constants.
+struct RepDev
+{
+    double lo[3], mx[3], L[3], minIn[3], maxIn[3];  // box corners, lengths, inner corners
+    double gmn[3], grdx[3];  // ghost-inclusive cell grid
+    int32_t gn[3];
+    int32_t cellBase;
+    double splitScale, splitInv;  // mixed form: coordinates split relative to gmn
+    SlabDev slab;
+    int32_t consistent;  // slab weights of every image equal those of its real molecule
+    int32_t lbase, n;
+    int32_t tfBase, tfBins;
+    double tfMin, tfBinSize, tfInvBin, tfBinVolume;
+    uint64_t seed;
+};
+
+// Device scalars (one struct, snapshotted with the state).
+struct Scalars
+{
+    unsigned long long step;    // global step number of the next step
+    unsigned long long tfSamples;
+    unsigned long long run;     // LJ_IdealGas run counter
+    double maxDisp;             // largest displacement of any molecule since the last rebuild
+    double dispStep;            // max |x - x_rebuild|^2 of the current step
+    int32_t numGhost;           // total ghosts written at the last rebuild (true count on overflow)
+    int32_t maxCount;           // largest list row seen (true count on overflow)
+    uint32_t overflow;          // ghost / list overflow of the rebuilds since the host cleared it
+    uint32_t flags;             // sticky: a molecule moved skin/2 between rebuilds
+    uint32_t done;              // tail-kernel block ticket
+};
+
+// Everything the kernels read: pointers and run constants.
+struct BDev
+{
+    const RepDev* reps;
+    int32_t R, N, gCap;
+    int32_t listCap;
+    int64_t totalCells;
+    double4* pos;  // [N + gCap]
+    double4* vel;  // [N]
+    double4* force;
+    double* mass;
+    int32_t* orig;
+    int32_t* slotRep;  // [N + gCap]
+    int32_t* gSrc;     // [gCap]
+    uint8_t* gShift;   // [gCap] 2 bits per axis: 1 = +L, 2 = -L
+    uint8_t* imgFlags; // [N] bit 2d: has a +L image on axis d, bit 2d+1: has a -L image
+    float4* ref;       // [N] position at the last rebuild, relative to the replica's grid origin
+    int32_t* gCount;   // [N + 1] images per local, then exclusive offsets
+    double4* lam;      // [N + gCap] (lambda, modulated lambda, grad lambda x, 0)
+    double* lamt;      // [N + gCap] modulated lambda
+    float2* lamtf;     // [N + gCap] modulated lambda as a double-float
+    float4* hi;        // mixed split coordinates [N + gCap]
+    float4* lo;
+    // cells
+    int32_t* cellOf;
+    int32_t* cellStart;  // [totalCells + 1]
+    int32_t* cursor;
+    int32_t* unordered;
+    int32_t* sorted;
+    float4* spos;
+    // list (32-row tiles)
+    int32_t* counts;
+    int32_t* nbrs;
+    // shadow for the cell sort of locals
+    double4* sPos;
+    double4* sVel;
+    double* sMass;
+    int32_t* sOrig;
+    // thermodynamic force and compensation energy
+    double* tfForce;                   // [sum bins]
+    unsigned long long* tfDensity;     // [sum bins] counts
+    double* tfWork;                    // [3 * sum bins]: density, smoothed, gradient
+    const double* tfFF;                // modulation / target density
+    int64_t totalBins;
+    long long* compEnergy;             // [R][200] fixed point
+    unsigned long long* compCounter;   // [R][200]
+    double* compMean;                  // [R][200]
+    double* energyRing;                // [ring][R]
+    int32_t ring;
+    Scalars* sc;
+    // physics
+    LJDev lj;
+    double rcSqr;
+    RcSq rc2;
+    double dt, zeta, temperature;
+    double rlist, halfSkin;
+    int64_t K, tfSampleInterval, tfUpdateInterval, compSampling, compUpdate;
+    int32_t tfEnabled;
+    double tfSigma, tfRange;
+    double listRsq;
+    float listRsqLo, listRsqHi;
+};
+
+__device__ __forceinline__ double coord(const double4& p, int d) { return d == 0 ? p.x : (d == 1 ? p.y : p.z); }
+
+__device__ __forceinline__ void set_coord(double4& p, int d, double v)
+{
+    if (d == 0)
+        p.x = v;
+    else if (d == 1)
+        p.y = v;
+    else
+        p.z = v;
+}
+
+// lambda, modulated lambda and grad lambda (x) of one slot, plus the mixed
+// form's split coordinates (UpdateMolecules.hpp:39-69 for a single site).
+template <bool MIXED>
+__device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int64_t s, const double4& x)
+{
+    double l, m, g;
+    slab_eval(R.slab, x.x, l, m, g);
+    B.lam[s] = make_double4(l, m, g, 0.0);
+    B.lamt[s] = m;
+    if (MIXED)
+    {
+        const float h = (float)m;
+        B.lamtf[s] = make_float2(h, (float)(m - (double)h));
+        SplitParams sp;
+        sp.scale = R.splitScale;
+        sp.invScale = R.splitInv;
+        float4 hv, lv;
+        split_one(x.x - R.gmn[0], sp, hv.x, lv.x);
+        split_one(x.y - R.gmn[1], sp, hv.y, lv.y);
+        split_one(x.z - R.gmn[2], sp, hv.z, lv.z);
+        hv.w = 0.0f;
+        lv.w = 0.0f;
+        B.hi[s] = hv;
+        B.lo[s] = lv;
+    }
+}
+
+// ------------------------------------------------------------------ pre --
+// B(dt/2) A(dt/2) O(dt) A(dt/2) (VelocityVerletLangevinThermostat.hpp:64-113)
+// with noise keyed by (replica seed, step, index inside the replica); on a
+// rebuild step the molecule is then wrapped into its box by the
+// MultiResRealAtomsExchange rule (MultiResRealAtomsExchange.cpp:23-73).
+template <bool MIXED>
+__global__ void k_b_pre(BDev B, int rebuild)
+{
+    const unsigned long long st = B.sc->step;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (tid < B.R) B.energyRing[(int64_t)(st % (unsigned long long)B.ring) * B.R + tid] = 0.0;
+    double m2 = 0.0;
+    const double dtHalf = 0.5 * B.dt;
+    for (int64_t i = tid; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const RepDev& R = B.reps[B.slotRep[i]];
+        double4 x = B.pos[i], v = B.vel[i];
+        const double4 f = B.force[i];
+        const double m = B.mass[i];
+        kick(v, f, __ddiv_rn(dtHalf, m));
+        drift(x, v, dtHalf);
+        double g[3];
+        normal3(R.seed, st, (uint64_t)(i - R.lbase), g);
+        ornstein_uhlenbeck(v, B.dt, m, B.zeta, B.temperature, g);
+        drift(x, v, dtHalf);
+        {
+            // Verlet criterion: displacement since the list was built
+            const float4 r0 = B.ref[i];
+            const float dx = (float)(x.x - R.gmn[0]) - r0.x, dy = (float)(x.y - R.gmn[1]) - r0.y,
+                        dz = (float)(x.z - R.gmn[2]) - r0.z;
+            m2 = fmax(m2, (double)(dx * dx + dy * dy + dz * dz));
+        }
+        if (rebuild)
+        {
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+            {
+                double c = coord(x, d);
+                if (R.mx[d] <= c) c = __dsub_rn(c, R.L[d]);
+                if (c < R.lo[d]) c = __dadd_rn(c, R.L[d]);
+                set_coord(x, d, c);
+            }
+        }
+        B.pos[i] = x;
+        B.vel[i] = v;
+        slot_derived<MIXED>(B, R, i, x);
+    }
+    m2 = mrmd_dev::warp_max(m2);
+    if ((threadIdx.x & 31) == 0) mrmd_dev::atomic_max_nonneg(&B.sc->dispStep, m2);
+}
+
+// ----------------------------------------------------------------- cells --
+__device__ __forceinline__ int32_t rep_cell(const RepDev& R, const double4& p)
+{
+    int32_t c[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        const double t = floor(__dmul_rn(__dsub_rn(coord(p, d), R.gmn[d]), R.grdx[d]));
+        c[d] = t < 0.0 ? 0 : (t > (double)(R.gn[d] - 1) ? R.gn[d] - 1 : (int)t);
+    }
+    return R.cellBase + (c[0] * R.gn[1] + c[1]) * R.gn[2] + c[2];
+}
+
+__device__ __forceinline__ int32_t num_slots(const BDev& B, int withGhosts)
+{
+    if (!withGhosts) return B.N;
+    const int32_t g = B.sc->numGhost;
+    return B.N + (g < B.gCap ? g : B.gCap);
+}
+
+__global__ void k_b_cell_count(BDev B, int withGhosts)
+{
+    const int32_t n = num_slots(B, withGhosts);
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const int32_t c = rep_cell(B.reps[B.slotRep[s]], B.pos[s]);
+        B.cellOf[s] = c;
+        atomicAdd(&B.cellStart[c], 1);
+    }
+}
+
+__global__ void k_b_cell_scatter(BDev B, int withGhosts)
+{
+    const int32_t n = num_slots(B, withGhosts);
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const int32_t c = B.cellOf[s];
+        B.unordered[B.cellStart[c] + atomicAdd(&B.cursor[c], 1)] = s;
+    }
+}
+
+// stable order inside each cell (ascending slot), then FP32 coordinates
+// relative to the replica's grid origin with the slot in w
+__global__ void k_b_cell_rank(BDev B, int withGhosts)
+{
+    const int32_t n = num_slots(B, withGhosts);
+    for (int32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    {
+        const int32_t v = B.unordered[t];
+        const int32_t c = B.cellOf[v];
+        const int32_t b = B.cellStart[c], e = B.cellStart[c + 1];
+        int32_t rank = 0;
+        for (int32_t u = b; u < e; ++u) rank += B.unordered[u] < v;
+        B.sorted[b + rank] = v;
+        if (withGhosts)
+        {
+            const RepDev& R = B.reps[B.slotRep[v]];
+            const double4 p = B.pos[v];
+            B.spos[b + rank] = make_float4((float)(p.x - R.gmn[0]), (float)(p.y - R.gmn[1]),
+                                           (float)(p.z - R.gmn[2]), __int_as_float(v));
+        }
+    }
+}
+
+// ----------------------------------------------------------- local sort --
+__global__ void k_b_sort_gather(BDev B)
+{
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < B.N; s += gridDim.x * blockDim.x)
+    {
+        const int32_t src = B.sorted[s];
+        B.sPos[s] = B.pos[src];
+        B.sVel[s] = B.vel[src];
+        B.sMass[s] = B.mass[src];
+        B.sOrig[s] = B.orig[src];
+    }
+}
+
+template <bool MIXED>
+__global__ void k_b_sort_store(BDev B)
+{
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < B.N; s += gridDim.x * blockDim.x)
+    {
+        const double4 x = B.sPos[s];
+        B.pos[s] = x;
+        B.vel[s] = B.sVel[s];
+        B.mass[s] = B.sMass[s];
+        B.orig[s] = B.sOrig[s];
+        slot_derived<MIXED>(B, B.reps[B.slotRep[s]], s, x);
+    }
+}
+
+// --------------------------------------------------------------- ghosts --
+// Images of each local molecule: per axis x < minInner gives a +L image and
+// x >= maxInner a -L image (MultiResPeriodicGhostExchange.cpp:60-248, ghosts
+// of ghosts included), i.e. the product over the axes minus the molecule.
+__global__ void k_b_ghost_count(BDev B)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < B.N; i += gridDim.x * blockDim.x)
+    {
+        const RepDev& R = B.reps[B.slotRep[i]];
+        const double4 x = B.pos[i];
+        uint32_t flags = 0;
+        int32_t n = 1;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+            const double c = coord(x, d);
+            const bool plus = c < R.minIn[d], minus = c >= R.maxIn[d];
+            flags |= (plus ? 1u : 0u) << (2 * d);
+            flags |= (minus ? 1u : 0u) << (2 * d + 1);
+            n *= 1 + (int)plus + (int)minus;
+        }
+        B.imgFlags[i] = (uint8_t)flags;
+        B.gCount[i] = n - 1;
+        B.ref[i] = make_float4((float)(x.x - R.gmn[0]), (float)(x.y - R.gmn[1]), (float)(x.z - R.gmn[2]), 0.0f);
+    }
+}
+
+template <bool MIXED>
+__global__ void k_b_ghost_write(BDev B)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < B.N; i += gridDim.x * blockDim.x)
+    {
+        const int32_t r = B.slotRep[i];
+        const RepDev& R = B.reps[r];
+        const uint32_t flags = B.imgFlags[i];
+        const double4 x = B.pos[i];
+        int32_t k = B.gCount[i];  // exclusive offset
+        // options per axis: 0 (no shift), 2 (-L) if x >= maxInner, 1 (+L) if x < minInner
+        for (int ox = 0; ox < 3; ++ox)
+        {
+            const int cx = ox == 0 ? 0 : (ox == 1 ? 2 : 1);
+            if (cx && !(flags & (cx == 1 ? 1u : 2u))) continue;
+            for (int oy = 0; oy < 3; ++oy)
+            {
+                const int cy = oy == 0 ? 0 : (oy == 1 ? 2 : 1);
+                if (cy && !(flags & (cy == 1 ? 4u : 8u))) continue;
+                for (int oz = 0; oz < 3; ++oz)
+                {
+                    const int cz = oz == 0 ? 0 : (oz == 1 ? 2 : 1);
+                    if (cz && !(flags & (cz == 1 ? 16u : 32u))) continue;
+                    if (!cx && !cy && !cz) continue;
+                    const int32_t g = k++;
+                    if (g >= B.gCap)
+                    {
+                        atomicOr(&B.sc->overflow, FLAG_GHOST_OVERFLOW);
+                        continue;
+                    }
+                    double4 p = x;
+                    const int c3[3] = {cx, cy, cz};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                    {
+                        if (c3[d] == 1) set_coord(p, d, __dadd_rn(coord(p, d), R.L[d]));
+                        if (c3[d] == 2) set_coord(p, d, __dsub_rn(coord(p, d), R.L[d]));
+                    }
+                    p.w = 0.0;
+                    const int64_t s = (int64_t)B.N + g;
+                    B.pos[s] = p;
+                    B.slotRep[s] = r;
+                    B.gSrc[g] = i;
+                    B.gShift[g] = (uint8_t)(cx | (cy << 2) | (cz << 4));
+                    slot_derived<MIXED>(B, R, s, p);
+                }
+            }
+        }
+    }
+}
+
+// ghost position = real position +- L (UpdateGhostAtoms.cpp:31-68)
+template <bool MIXED>
+__global__ void k_b_ghost_update(BDev B)
+{
+    const int32_t n = num_slots(B, 1) - B.N;
+    for (int32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x)
+    {
+        const int32_t i = B.gSrc[g];
+        const uint32_t code = B.gShift[g];
+        const RepDev& R = B.reps[B.slotRep[i]];
+        double4 p = B.pos[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+            const uint32_t c = (code >> (2 * d)) & 3u;
+            if (c == 1) set_coord(p, d, __dadd_rn(coord(p, d), R.L[d]));
+            if (c == 2) set_coord(p, d, __dsub_rn(coord(p, d), R.L[d]));
+        }
+        p.w = 0.0;
+        const int64_t s = (int64_t)B.N + g;
+        B.pos[s] = p;
+        slot_derived<MIXED>(B, R, s, p);
+    }
+}
+
+// ------------------------------------------------------------ list build --
+// Cabana's half-list discriminator (lexicographic x, y, z): b above a
+__device__ __forceinline__ bool lex_above(const double4& a, const double4& b)
+{
+    return (b.x > a.x) || ((b.x == a.x) && ((b.y > a.y) || ((b.y == a.y) && (b.z > a.z))));
+}
+
+// Full list (every slot j != i of the same replica within r_list) of each
+// local molecule, 27-cell stencil walked as contiguous z-column spans of the
+// replica's cell-sorted FP32 coordinates; an FP32 prefilter settles the
+// clear cases and FP64 positions decide inside its error band.
+__global__ void __launch_bounds__(128) k_b_build_list(BDev B)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < B.N; i += gridDim.x * blockDim.x)
+    {
+        const RepDev& R = B.reps[B.slotRep[i]];
+        const double4 pi = B.pos[i];
+        const float xi = (float)(pi.x - R.gmn[0]), yi = (float)(pi.y - R.gmn[1]), zi = (float)(pi.z - R.gmn[2]);
+        const uint32_t myImg = B.imgFlags[i];
+        const int32_t ci = B.cellOf[i] - R.cellBase;
+        const int cz = ci % R.gn[2];
+        const int cy = (ci / R.gn[2]) % R.gn[1];
+        const int cx = ci / (R.gn[2] * R.gn[1]);
+        int32_t cnt = 0;
+        const int az0 = max(cz - 1, 0), az1 = min(cz + 1, R.gn[2] - 1);
+        for (int ax = max(cx - 1, 0); ax <= min(cx + 1, R.gn[0] - 1); ++ax)
+        {
+            for (int ay = max(cy - 1, 0); ay <= min(cy + 1, R.gn[1] - 1); ++ay)
+            {
+                const int32_t c0 = R.cellBase + (ax * R.gn[1] + ay) * R.gn[2];
+                const int32_t s0 = B.cellStart[c0 + az0], s1 = B.cellStart[c0 + az1 + 1];
+                for (int32_t s = s0; s < s1; ++s)
+                {
+                    const float4 q = B.spos[s];
+                    const int32_t j = __float_as_int(q.w);
+                    if (j == i) continue;
+                    const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                    const float d2f = dx * dx + dy * dy + dz * dz;
+                    if (d2f > B.listRsqHi) continue;
+                    bool keep = d2f < B.listRsqLo;
+                    if (!keep)
+                    {
+                        const double4 pj = B.pos[j];
+                        const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+                        const double d2 =
+                            __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+                        keep = d2 <= B.listRsq;
+                    }
+                    if (!keep) continue;
+                    int32_t entry = j;
+                    if (j >= B.N && !lex_above(pi, B.pos[j]))
+                    {
+                        // Cabana's half list keeps (source, image of i) instead of
+                        // (i, ghost): i must have that image, or the pair is absent
+                        const uint32_t code = B.gShift[j - B.N];
+                        bool has = true;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d)
+                        {
+                            const uint32_t c = (code >> (2 * d)) & 3u;
+                            if (c == 1) has = has && (myImg & (2u << (2 * d)));  // ghost +L: i needs a -L image
+                            if (c == 2) has = has && (myImg & (1u << (2 * d)));  // ghost -L: i needs a +L image
+                        }
+                        if (!has) continue;
+                        entry = j | REVERSED;
+                    }
+                    if (cnt < B.listCap) B.nbrs[mrmd_dev::nbr_row(i, B.listCap) + 32 * (int64_t)cnt] = entry;
+                    ++cnt;
+                }
+            }
+        }
+        B.counts[i] = cnt < B.listCap ? cnt : B.listCap;
+        if (cnt > B.listCap)
+        {
+            atomicMax(&B.sc->maxCount, cnt);
+            atomicOr(&B.sc->overflow, FLAG_LIST_OVERFLOW);
+        }
+    }
+}
+
+// ------------------------------------------------------------ pair force --
+__device__ __forceinline__ df df_shfl_xor(df v, int o)
+{
+    return {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+
+__device__ __forceinline__ double to_d(df v) { return (double)v.h + (double)v.l; }
+
+// CheckRegion's hybrid test on a double-float weight in [0, 1]
+__device__ __forceinline__ bool is_hy_df(float2 v)
+{
+    const bool at = v.x > 1.0f || (v.x == 1.0f && v.y >= 0.0f);
+    return !at && !(v.x <= 0.0f);
+}
+
+// double-float energy of a non-capped pair: u3 (r^-6) * (ef1 u3 - ef2) - shift
+__device__ __forceinline__ df energy_df(const df& r2, const LJDev& p)
+{
+    if (r2.h >= p.capSqrf)
+    {
+        const df u = df_rcp(r2);
+        const df u3 = df_mul(df_sqr(u), u);
+        const float ef1h = (float)p.ef1, ef2h = (float)p.ef2, sh = (float)p.shift;
+        const df ef1 = {ef1h, (float)(p.ef1 - (double)ef1h)};
+        const df ef2 = {ef2h, (float)(p.ef2 - (double)ef2h)};
+        const df t = df_add(df_mul(ef1, u3), df{-ef2.h, -ef2.l});
+        return df_add(df_mul(u3, t), df{-sh, -(float)(p.shift - (double)sh)});
+    }
+    // capped: E(r_cap) - (r - r_cap) capCoeff - shift, r = sqrt(r2) to double-float
+    float s = sqrtf(r2.h);
+    const float res = __fmaf_rn(-s, s, r2.h) + r2.l;
+    const df dist = fast_two_sum(s, res / (2.0f * s));
+    const df t = df_add(dist, df{-(float)p.capDist, -(float)(p.capDist - (double)(float)p.capDist)});
+    const float cch = (float)p.capCoeff;
+    const df lin = df_mul(t, df{cch, (float)(p.capCoeff - (double)cch)});
+    const float eh = (float)(p.eCap - p.shift);
+    return df_add(df{eh, (float)((p.eCap - p.shift) - (double)eh)}, df{-lin.h, -lin.l});
+}
+
+struct RowOut
+{
+    double fx, fy, fz;  // pair force on the molecule
+    double vsum;        // sum of V_ij of pairs with a hybrid member, own slot = the molecule itself
+    double comp;        // the same, only pairs whose own slot is hybrid with a valid bin
+    double imgFx;       // drift force from pairs whose own slot is an image of the molecule
+    double energy;      // sum of e w over the row (each pair is seen from both sides)
+};
+
+// One row (local molecule i), lanes `sub` of TPR.  Returns this lane's
+// partial sums.
+template <bool MIXED, int TPR>
+__device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, bool sampling)
+{
+    const RepDev& R = B.reps[B.slotRep[i]];
+    const double4 la = B.lam[i];  // lambda, modulated, grad x
+    const double4 pi = B.pos[i];
+    float4 hi_i, lo_i;
+    if (MIXED)
+    {
+        hi_i = B.hi[i];
+        lo_i = B.lo[i];
+    }
+    const float2 ltA = MIXED ? B.lamtf[i] : make_float2(0.f, 0.f);
+    df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, vs{0.f, 0.f}, cs{0.f, 0.f};
+    double dfx = 0.0, dfy = 0.0, dfz = 0.0, dvs = 0.0, dcs = 0.0;
+    double imgFx = 0.0, energy = 0.0;
+    float fenergy = 0.0f;
+    const int cnt = B.counts[i];
+    const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
+    const int binAlpha = is_hy(la.y) ? comp_bin(la.x) : -1;
+    for (int k = sub; k < cnt; k += TPR)
+    {
+        const int32_t entry = B.nbrs[rowBase + 32 * (int64_t)k];
+        const bool rev = entry < 0;
+        const int32_t j = entry & 0x7fffffff;
+        // own slot (the molecule or one of its images) and partner slot weights
+        bool ownIsSelf = true;
+        double ownLam = la.x, ownMod = la.y, ownGx = la.z;
+        double partMod = 0.0;
+        float2 partModF = make_float2(0.f, 0.f);
+        if (MIXED)
+            partModF = B.lamtf[j];
+        else
+            partMod = B.lamt[j];
+        double4 pj = make_double4(0.0, 0.0, 0.0, 0.0);
+        float4 hj, lj;
+        if (MIXED)
+        {
+            hj = B.hi[j];
+            lj = B.lo[j];
+        }
+        else
+        {
+            pj = B.pos[j];
+        }
+        if (rev && !R.consistent)
+        {
+            // the pair acts with the weights of (source, image of i)
+            const int32_t g = j - B.N;
+            const int32_t src = B.gSrc[g];
+            if (MIXED)
+                partModF = B.lamtf[src];
+            else
+                partMod = B.lamt[src];
+            const uint32_t cx = B.gShift[g] & 3u;
+            if (cx != 0)
+            {
+                const double xi = cx == 1 ? __dsub_rn(pi.x, R.L[0]) : __dadd_rn(pi.x, R.L[0]);
+                slab_eval(R.slab, xi, ownLam, ownMod, ownGx);
+                ownIsSelf = false;
+            }
+        }
+        if (MIXED)
+        {
+            const float2 ownF =
+                ownIsSelf ? ltA : make_float2((float)ownMod, (float)(ownMod - (double)(float)ownMod));
+            if (ownF.x <= 0.0f && partModF.x <= 0.0f) continue;  // both coarse grained: ideal gas
+            PairMixed q;
+            if (!pair_mixed(hi_i, lo_i, hj, lj, B.lj, B.rc2, q)) continue;
+            const bool hyPair = is_hy_df(ownF) || is_hy_df(partModF);
+            // weighting = (lambda~_own + lambda~_partner) / 2 as a double-float
+            const bool bothAT = ownF.x == 1.0f && ownF.y == 0.0f && partModF.x == 1.0f && partModF.y == 0.0f;
+            df ffw = q.ff;
+            if (!bothAT)
+            {
+                df w = df_add(df{ownF.x, ownF.y}, df{partModF.x, partModF.y});
+                w.h *= 0.5f;
+                w.l *= 0.5f;
+                ffw = df_mul(q.ff, w);
+            }
+            df_acc_prod(fx, q.dh.x, q.dl.x, ffw);
+            df_acc_prod(fy, q.dh.y, q.dl.y, ffw);
+            df_acc_prod(fz, q.dh.z, q.dl.z, ffw);
+            if (hyPair)
+            {
+                // V_ij = e/2 in double-float (it drives the drift force)
+                const df ed = energy_df(df{q.r2h, q.r2l}, B.lj);
+                const df V = {0.5f * ed.h, 0.5f * ed.l};
+                if (ownIsSelf)
+                {
+                    vs = df_add(vs, V);
+                    if (sampling && binAlpha != -1) cs = df_add(cs, V);
+                }
+                else
+                {
+                    const double Vd = to_d(V);
+                    imgFx += -Vd * ownGx;
+                    if (sampling && is_hy(ownMod))
+                    {
+                        const int b = comp_bin(ownLam);
+                        if (b != -1)
+                            atomicAdd(reinterpret_cast<unsigned long long*>(B.compEnergy + B.slotRep[i] * COMP_BINS + b),
+                                      (unsigned long long)llrint(Vd * COMP_SCALE));
+                    }
+                }
+            }
+            fenergy = __fmaf_rn(q.e, bothAT ? 1.0f : 0.5f * (ownF.x + partModF.x), fenergy);
+        }
+        else
+        {
+            if (ownMod <= 0.0 && partMod <= 0.0) continue;  // both coarse grained: ideal gas
+            const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const double distSqr = dx * dx + dy * dy + dz * dz;
+            if (distSqr > B.rcSqr) continue;
+            const bool hyPair = is_hy(ownMod) || is_hy(partMod);
+            double ff, e;
+            lj_eval_fp64(B.lj, distSqr, ff, e);
+            const double weighting = 0.5 * (ownMod + partMod);
+            const double ffactor = ff * weighting;
+            dfx += dx * ffactor;
+            dfy += dy * ffactor;
+            dfz += dz * ffactor;
+            energy += e * weighting;
+            if (hyPair)
+            {
+                const double Vij = 0.5 * e;
+                if (ownIsSelf)
+                {
+                    dvs += Vij;
+                    if (sampling && binAlpha != -1) dcs += Vij;
+                }
+                else
+                {
+                    imgFx += -Vij * ownGx;
+                    if (sampling && is_hy(ownMod))
+                    {
+                        const int b = comp_bin(ownLam);
+                        if (b != -1)
+                            atomicAdd(reinterpret_cast<unsigned long long*>(B.compEnergy + B.slotRep[i] * COMP_BINS + b),
+                                      (unsigned long long)llrint(Vij * COMP_SCALE));
+                    }
+                }
+            }
+        }
+    }
+    // reduce the TPR lanes of the row (fixed butterfly: identical sums on every lane)
+    RowOut o;
+    if (MIXED)
+    {
+#pragma unroll
+        for (int off = 1; off < TPR; off <<= 1)
+        {
+            fx = df_add(fx, df_shfl_xor(fx, off));
+            fy = df_add(fy, df_shfl_xor(fy, off));
+            fz = df_add(fz, df_shfl_xor(fz, off));
+            vs = df_add(vs, df_shfl_xor(vs, off));
+            cs = df_add(cs, df_shfl_xor(cs, off));
+        }
+        o.fx = to_d(fx);
+        o.fy = to_d(fy);
+        o.fz = to_d(fz);
+        o.vsum = to_d(vs);
+        o.comp = to_d(cs);
+        energy = (double)fenergy;
+    }
+    else
+    {
+#pragma unroll
+        for (int off = 1; off < TPR; off <<= 1)
+        {
+            dfx += __shfl_xor_sync(0xffffffffu, dfx, off);
+            dfy += __shfl_xor_sync(0xffffffffu, dfy, off);
+            dfz += __shfl_xor_sync(0xffffffffu, dfz, off);
+            dvs += __shfl_xor_sync(0xffffffffu, dvs, off);
+            dcs += __shfl_xor_sync(0xffffffffu, dcs, off);
+        }
+        o.fx = dfx;
+        o.fy = dfy;
+        o.fz = dfz;
+        o.vsum = dvs;
+        o.comp = dcs;
+    }
+#pragma unroll
+    for (int off = 1; off < TPR; off <<= 1)
+    {
+        imgFx += __shfl_xor_sync(0xffffffffu, imgFx, off);
+        energy += __shfl_xor_sync(0xffffffffu, energy, off);
+    }
+    o.imgFx = imgFx;
+    o.energy = energy;
+    return o;
+}
+
+// Pair force of every local molecule (LJ_IdealGas.cpp:52-225 on a full
+// list), then per molecule: drift-compensation force and sampling, TF apply
+// (ThermodynamicForce.hpp:98-122), density sample (AxialDensityProfile.cpp:
+// 36-47) and the velocity-Verlet post kick (VelocityVerlet.cpp:69-90).
+template <bool MIXED, int TPR>
+__global__ void k_b_force(BDev B)
+{
+    const unsigned long long st = B.sc->step;
+    const unsigned long long run = B.sc->run;
+    const bool sampling = (run % (unsigned long long)B.compSampling) == 0;
+    const bool tfSample = B.tfEnabled && (st % (unsigned long long)B.tfSampleInterval) == 0;
+    const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int32_t i = (int32_t)(gtid / TPR);
+    const int sub = (int)(gtid % TPR);
+    const bool valid = i < B.N;
+    RowOut o = row_force<MIXED, TPR>(B, valid ? i : 0, sub, sampling && valid);
+    if (!valid) o.energy = 0.0;
+    int32_t r = valid ? B.slotRep[i] : -1;
+    if (valid && sub == 0)
+    {
+        const RepDev& R = B.reps[r];
+        const double4 la = B.lam[i];
+        // molecule force: drift (-V_ij grad lambda) and compensation
+        double fmx = -o.vsum * la.z + o.imgFx;
+        if (is_hy(la.y))
+        {
+            const int b = comp_bin(la.x);
+            if (b != -1)
+            {
+                fmx += B.compMean[r * COMP_BINS + b] * la.z;
+                if (sampling)
+                {
+                    atomicAdd(B.compCounter + r * COMP_BINS + b, 1ull);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(B.compEnergy + r * COMP_BINS + b),
+                              (unsigned long long)llrint(o.comp * COMP_SCALE));
+                }
+            }
+        }
+        double4 f = make_double4(o.fx, o.fy, o.fz, 0.0);
+        f.x = __dadd_rn(f.x, fmx);
+        const double4 x = B.pos[i];
+        if (B.tfEnabled)
+        {
+            const int64_t b = (int64_t)floor((x.x - R.tfMin) * R.tfInvBin);
+            if (b >= 0 && b < R.tfBins)
+            {
+                f.x = __dadd_rn(f.x, B.tfForce[R.tfBase + b]);
+                if (tfSample) atomicAdd(B.tfDensity + R.tfBase + b, 1ull);
+            }
+        }
+        double4 v = B.vel[i];
+        kick(v, f, __ddiv_rn(0.5 * B.dt, B.mass[i]));
+        B.vel[i] = v;
+        B.force[i] = f;
+    }
+    // energy per replica: one atomic per warp when the warp's rows share a replica
+    double e = (sub == 0) ? 0.5 * o.energy : 0.0;
+    const int lane = threadIdx.x & 31;
+    const int32_t r0 = __shfl_sync(0xffffffffu, r, 0);
+    double* ring = B.energyRing + (int64_t)(st % (unsigned long long)B.ring) * B.R;
+    if (__all_sync(0xffffffffu, r == r0 || r == -1))
+    {
+        e = mrmd_dev::warp_sum(e);
+        if (lane == 0 && r0 >= 0) atomicAdd(ring + r0, e);
+    }
+    else if (r >= 0 && e != 0.0)
+    {
+        atomicAdd(ring + r, e);
+    }
+}
+
+// ------------------------------------------------------------------ tail --
+// One block per replica: the drift-compensation mean update
+// (LJ_IdealGas.cpp:21-50, 253-255) and the ThermodynamicForce update; the
+// last block advances the step counters and the displacement bookkeeping.
+__global__ void k_b_tail(BDev B, int rebuild)
+{
+    __shared__ unsigned long long sStep, sRun, sSamples;
+    if (threadIdx.x == 0)
+    {
+        sStep = B.sc->step;
+        sRun = B.sc->run;
+        sSamples = B.sc->tfSamples;
+    }
+    __syncthreads();
+    const unsigned long long st = sStep, run = sRun;
+    const int r = blockIdx.x;
+    const RepDev& R = B.reps[r];
+    if ((run % (unsigned long long)B.compUpdate) == 0)
+    {
+        for (int k = threadIdx.x; k < COMP_BINS; k += blockDim.x)
+        {
+            const int64_t q = (int64_t)r * COMP_BINS + k;
+            const double cnt = (double)B.compCounter[q];
+            if (cnt < 0.5) continue;
+            const double e = ((double)B.compEnergy[q] / COMP_SCALE) / cnt;
+            B.compMean[q] = (10.0 * B.compMean[q] + e) / (10.0 + 1.0);
+            B.compEnergy[q] = 0;
+            B.compCounter[q] = 0;
+        }
+    }
+    if (B.tfEnabled)
+    {
+        const unsigned long long samples = sSamples + ((st % (unsigned long long)B.tfSampleInterval) == 0 ? 1 : 0);
+        if (((st + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && samples > 0)
+        {
+            double* d = B.tfWork + R.tfBase;
+            for (int k = threadIdx.x; k < R.tfBins; k += blockDim.x)
+            {
+                d[k] = (double)B.tfDensity[R.tfBase + k];
+                B.tfDensity[R.tfBase + k] = 0ull;
+            }
+            __syncthreads();
+            UpdateArgs A{};
+            A.density = d;
+            A.force = B.tfForce + R.tfBase;
+            A.smooth = B.tfWork + B.totalBins + R.tfBase;
+            A.grad = B.tfWork + 2 * (int64_t)B.totalBins + R.tfBase;
+            A.forceFactor = B.tfFF;
+            A.numBins = R.tfBins;
+            A.numTypes = 1;
+            A.binSize = R.tfBinSize;
+            A.inverseBinSize = R.tfInvBin;
+            A.min = R.tfMin;
+            A.normalization = 1.0 / (R.tfBinVolume * (double)samples);
+            A.sigma = B.tfSigma;
+            A.range = B.tfRange;
+            A.enforceSymmetry = 0;
+            A.periodic = 1;
+            A.usePred = 0;
+            tf_update_block(A);
+        }
+    }
+    // last block: counters
+    __syncthreads();
+    __threadfence();
+    if (threadIdx.x == 0)
+    {
+        const unsigned int ticket = atomicAdd(&B.sc->done, 1u);
+        if (ticket == gridDim.x - 1)
+        {
+            __threadfence();
+            Scalars* s = B.sc;
+            unsigned long long samples = sSamples;
+            if (B.tfEnabled && (st % (unsigned long long)B.tfSampleInterval) == 0) ++samples;
+            if (B.tfEnabled && ((st + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && samples > 0) samples = 0;
+            s->tfSamples = samples;
+            // on a rebuild step the pre-force displacement is measured against
+            // the previous list, which this step no longer uses
+            if (rebuild)
+            {
+                s->maxDisp = 0.0;
+            }
+            else
+            {
+                const double d = sqrt(s->dispStep);
+                s->maxDisp = fmax(s->maxDisp, d);
+                if (d >= B.halfSkin) s->flags |= FLAG_UNSAFE_INTERVAL;
+            }
+            s->dispStep = 0.0;
+            s->run = run + 1;
+            s->step = st + 1;
+            s->done = 0u;
+        }
+    }
+}
+}  // namespace
+
+// ================================================================== host ==
+
+// Everything a step changes (positions, velocities, forces, the order of
+// the locals, the TF and compensation tables, the device scalars).
+struct Snap
+{
+    double4 *pos = nullptr, *vel = nullptr, *force = nullptr;
+    double* mass = nullptr;
+    int32_t* orig = nullptr;
+    double* tfForce = nullptr;
+    unsigned long long* tfDensity = nullptr;
+    long long* compE = nullptr;
+    unsigned long long* compC = nullptr;
+    double* compM = nullptr;
+    Scalars* sc = nullptr;
+};
+
+struct mrmd_batch
+{
+    mrmd_batch_config cfg{};
+    int32_t R = 0, N = 0;
+    std::vector<RepDev> reps;
+    std::vector<int64_t> offsets;  // [R + 1] molecule offsets
+    int64_t totalCells = 0, totalBins = 0;
+    double listExtent = 0.0;
+    BDev B{};
+    RepDev* dReps = nullptr;
+    double* dTfFF = nullptr;
+    Snap sn;  // state before the running graph (overflow roll-back)
+    Scalars* hSc = nullptr;    // pinned
+    double* hRing = nullptr;   // pinned [ring][R]
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t graphKernels = 0;
+    int64_t steps = 0, rebuilds = 0, graphLaunches = 0, recoveries = 0;
+    bool needRebuild = true;  // ghosts and list do not match the locals (new tuning, restored state)
+};
+
+namespace
+{
+template <typename T>
+int grow(mrmd_ctx* ctx, T*& p, int64_t oldCount, int64_t newCount)
+{
+    T* q = nullptr;
+    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&q), sizeof(T) * (size_t)(newCount > 0 ? newCount : 1)));
+    if (p && oldCount > 0)
+    {
+        const int64_t c = oldCount < newCount ? oldCount : newCount;
+        MRMD_CUDA(ctx, cudaMemcpyAsync(q, p, sizeof(T) * (size_t)c, cudaMemcpyDeviceToDevice, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    dfree(p);
+    p = q;
+    return MRMD_OK;
+}
+
+void drop_graph(mrmd_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// (Re)size the ghost-dependent and list buffers.
+int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap)
+{
+    BDev& B = b->B;
+    const int64_t N = b->N;
+    if (gCap != B.gCap)
+    {
+        const int64_t o = N + B.gCap, n = N + gCap;
+        MRMD_TRY(grow(ctx, B.pos, o, n));
+        MRMD_TRY(grow(ctx, B.slotRep, o, n));
+        MRMD_TRY(grow(ctx, B.lam, o, n));
+        MRMD_TRY(grow(ctx, B.lamt, o, n));
+        MRMD_TRY(grow(ctx, B.lamtf, o, n));
+        MRMD_TRY(grow(ctx, B.hi, o, n));
+        MRMD_TRY(grow(ctx, B.lo, o, n));
+        MRMD_TRY(grow(ctx, B.cellOf, 0, n));
+        MRMD_TRY(grow(ctx, B.unordered, 0, n));
+        MRMD_TRY(grow(ctx, B.sorted, 0, n));
+        MRMD_TRY(grow(ctx, B.spos, 0, n));
+        MRMD_TRY(grow(ctx, B.gSrc, 0, (int64_t)gCap));
+        MRMD_TRY(grow(ctx, B.gShift, 0, (int64_t)gCap));
+        B.gCap = gCap;
+        drop_graph(b);
+    }
+    if (listCap != B.listCap)
+    {
+        const int64_t tiles = div_up(N, 32);
+        MRMD_TRY(grow(ctx, B.nbrs, 0, tiles * 32 * (int64_t)listCap));
+        B.listCap = listCap;
+        drop_graph(b);
+    }
+    return MRMD_OK;
+}
+
+// Cell binning of the locals (withGhosts = 0) or of every slot.
+int cell_pass(mrmd_ctx* ctx, mrmd_batch* b, int withGhosts)
+{
+    BDev& B = b->B;
+    const int64_t n = withGhosts ? (int64_t)b->N + B.gCap : b->N;
+    MRMD_CUDA(ctx, cudaMemsetAsync(B.cellStart, 0, sizeof(int32_t) * (size_t)(b->totalCells + 1), ctx->stream));
+    MRMD_CUDA(ctx, cudaMemsetAsync(B.cursor, 0, sizeof(int32_t) * (size_t)(b->totalCells + 1), ctx->stream));
+    const unsigned g = grid_for(ctx, n, TB);
+    k_b_cell_count<<<g, TB, 0, ctx->stream>>>(B, withGhosts);
+    MRMD_TRY(after_launch(ctx, "batch cell_count"));
+    MRMD_TRY(scan_exclusive_i32(ctx, B.cellStart, B.cellStart, b->totalCells + 1, nullptr));
+    k_b_cell_scatter<<<g, TB, 0, ctx->stream>>>(B, withGhosts);
+    MRMD_TRY(after_launch(ctx, "batch cell_scatter"));
+    k_b_cell_rank<<<g, TB, 0, ctx->stream>>>(B, withGhosts);
+    return after_launch(ctx, "batch cell_rank");
+}
+
+template <bool M>
+int rebuild_t(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
+{
+    BDev& B = b->B;
+    const unsigned gN = grid_for(ctx, b->N, TB);
+    if (sort)
+    {
+        MRMD_TRY(cell_pass(ctx, b, 0));
+        k_b_sort_gather<<<gN, TB, 0, ctx->stream>>>(B);
+        MRMD_TRY(after_launch(ctx, "batch sort_gather"));
+        k_b_sort_store<M><<<gN, TB, 0, ctx->stream>>>(B);
+        MRMD_TRY(after_launch(ctx, "batch sort_store"));
+    }
+    k_b_ghost_count<<<gN, TB, 0, ctx->stream>>>(B);
+    MRMD_TRY(after_launch(ctx, "batch ghost_count"));
+    MRMD_TRY(scan_exclusive_i32(ctx, B.gCount, B.gCount, b->N, &B.sc->numGhost));
+    k_b_ghost_write<M><<<gN, TB, 0, ctx->stream>>>(B);
+    MRMD_TRY(after_launch(ctx, "batch ghost_write"));
+    MRMD_TRY(cell_pass(ctx, b, 1));
+    k_b_build_list<<<grid_for(ctx, b->N, 128, 16), 128, 0, ctx->stream>>>(B);
+    return after_launch(ctx, "batch build_list");
+}
+
+int rebuild(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
+{
+    return b->cfg.precision == MRMD_PREC_MIXED ? rebuild_t<true>(ctx, b, sort) : rebuild_t<false>(ctx, b, sort);
+}
+
+template <bool M, int TPR>
+int force_t(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    const int bs = b->cfg.tuning.blockSize;
+    const int64_t threads = (int64_t)b->N * TPR;
+    k_b_force<M, TPR><<<(unsigned)div_up(threads, bs), bs, 0, ctx->stream>>>(b->B);
+    return after_launch(ctx, "batch force");
+}
+
+template <bool M>
+int force_m(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    switch (b->cfg.tuning.threadsPerRow)
+    {
+        case 1: return force_t<M, 1>(ctx, b);
+        case 2: return force_t<M, 2>(ctx, b);
+        case 4: return force_t<M, 4>(ctx, b);
+        case 8: return force_t<M, 8>(ctx, b);
+        default: return set_error(ctx, MRMD_ERR_ARG, "threadsPerRow must be 1, 2, 4 or 8");
+    }
+}
+
+bool is_rebuild(const mrmd_batch* b, int64_t st) { return st % b->cfg.tuning.rebuildInterval == 0; }
+
+bool is_sort(const mrmd_batch* b, int64_t st)
+{
+    const int64_t se = b->cfg.tuning.sortEvery;
+    return se > 0 && is_rebuild(b, st) && (st / b->cfg.tuning.rebuildInterval) % se == 0;
+}
+
+// One step, asynchronously.  With checkRebuild the rebuild is verified on the
+// host (one synchronisation) and repeated with larger buffers on overflow.
+int step(mrmd_ctx* ctx, mrmd_batch* b, int64_t st, bool checkRebuild)
+{
+    BDev& B = b->B;
+    const bool M = b->cfg.precision == MRMD_PREC_MIXED;
+    const bool reb = is_rebuild(b, st) || b->needRebuild;
+    b->needRebuild = false;
+    const unsigned gN = grid_for(ctx, b->N, TB);
+    if (M)
+        k_b_pre<true><<<gN, TB, 0, ctx->stream>>>(B, reb ? 1 : 0);
+    else
+        k_b_pre<false><<<gN, TB, 0, ctx->stream>>>(B, reb ? 1 : 0);
+    MRMD_TRY(after_launch(ctx, "batch pre"));
+    if (reb)
+    {
+        bool sort = is_sort(b, st);
+        for (int attempt = 0;; ++attempt)
+        {
+            if (checkRebuild)
+                MRMD_CUDA(ctx, cudaMemsetAsync(&B.sc->overflow, 0, sizeof(uint32_t), ctx->stream));
+            MRMD_TRY(rebuild(ctx, b, sort));
+            if (!checkRebuild) break;
+            MRMD_CUDA(ctx, cudaMemcpyAsync(b->hSc, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+            MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            const uint32_t f = b->hSc->overflow;
+            if (!f) break;
+            if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
+            int32_t gCap = B.gCap, lCap = B.listCap;
+            if (f & FLAG_GHOST_OVERFLOW) gCap = b->hSc->numGhost + b->hSc->numGhost / 4 + 1024;
+            if (f & FLAG_LIST_OVERFLOW) lCap = b->hSc->maxCount + b->hSc->maxCount / 5 + 8;
+            MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
+            b->recoveries++;
+            sort = false;  // the locals are already in cell order
+        }
+        b->rebuilds++;
+    }
+    else
+    {
+        if (M)
+            k_b_ghost_update<true><<<grid_for(ctx, B.gCap, TB), TB, 0, ctx->stream>>>(B);
+        else
+            k_b_ghost_update<false><<<grid_for(ctx, B.gCap, TB), TB, 0, ctx->stream>>>(B);
+        MRMD_TRY(after_launch(ctx, "batch ghost_update"));
+    }
+    MRMD_TRY(M ? force_m<true>(ctx, b) : force_m<false>(ctx, b));
+    k_b_tail<<<(unsigned)b->R, TB, 0, ctx->stream>>>(B, reb ? 1 : 0);
+    return after_launch(ctx, "batch tail");
+}
+
+int snap_alloc(mrmd_ctx* ctx, const mrmd_batch* b, Snap& s)
+{
+    const int64_t N = b->N, nb = std::max<int64_t>(b->totalBins, 1), nc = (int64_t)b->R * COMP_BINS;
+    MRMD_TRY(grow(ctx, s.pos, 0, N));
+    MRMD_TRY(grow(ctx, s.vel, 0, N));
+    MRMD_TRY(grow(ctx, s.force, 0, N));
+    MRMD_TRY(grow(ctx, s.mass, 0, N));
+    MRMD_TRY(grow(ctx, s.orig, 0, N));
+    MRMD_TRY(grow(ctx, s.tfForce, 0, nb));
+    MRMD_TRY(grow(ctx, s.tfDensity, 0, nb));
+    MRMD_TRY(grow(ctx, s.compE, 0, nc));
+    MRMD_TRY(grow(ctx, s.compC, 0, nc));
+    MRMD_TRY(grow(ctx, s.compM, 0, nc));
+    return grow(ctx, s.sc, 0, (int64_t)1);
+}
+
+void snap_free(Snap& s)
+{
+    void* ptrs[] = {s.pos, s.vel, s.force, s.mass, s.orig, s.tfForce, s.tfDensity, s.compE, s.compC, s.compM, s.sc};
+    for (void* p : ptrs) dfree(p);
+    s = Snap{};
+}
+
+// save (live -> s) or restore (s -> live)
+int snapshot(mrmd_ctx* ctx, mrmd_batch* b, Snap& sn, bool save)
+{
+    BDev& B = b->B;
+    const size_t N = (size_t)b->N, nb = (size_t)b->totalBins, nc = (size_t)b->R * COMP_BINS;
+    auto cp = [&](void* snap, void* live, size_t bytes) {
+        if (bytes == 0) return (int)MRMD_OK;
+        return check_cuda(ctx,
+                          cudaMemcpyAsync(save ? snap : live, save ? live : snap, bytes, cudaMemcpyDeviceToDevice,
+                                          ctx->stream),
+                          "batch snapshot");
+    };
+    MRMD_TRY(cp(sn.pos, B.pos, sizeof(double4) * N));
+    MRMD_TRY(cp(sn.vel, B.vel, sizeof(double4) * N));
+    MRMD_TRY(cp(sn.force, B.force, sizeof(double4) * N));
+    MRMD_TRY(cp(sn.mass, B.mass, sizeof(double) * N));
+    MRMD_TRY(cp(sn.orig, B.orig, sizeof(int32_t) * N));
+    MRMD_TRY(cp(sn.tfForce, B.tfForce, sizeof(double) * nb));
+    MRMD_TRY(cp(sn.tfDensity, B.tfDensity, sizeof(unsigned long long) * nb));
+    MRMD_TRY(cp(sn.compE, B.compEnergy, sizeof(long long) * nc));
+    MRMD_TRY(cp(sn.compC, B.compCounter, sizeof(unsigned long long) * nc));
+    MRMD_TRY(cp(sn.compM, B.compMean, sizeof(double) * nc));
+    MRMD_TRY(cp(sn.sc, B.sc, sizeof(Scalars)));
+    return MRMD_OK;
+}
+
+int capture(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
+{
+    drop_graph(b);
+    const int64_t P = b->cfg.tuning.graphSteps;
+    MRMD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = ctx->launches, r0 = b->rebuilds;
+    int rc = MRMD_OK;
+    for (int64_t k = 0; k < P && rc == MRMD_OK; ++k) rc = step(ctx, b, st0 + k, false);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    b->graphKernels = ctx->launches - l0;
+    ctx->launches = l0;
+    b->rebuilds = r0;  // counted when the graph runs
+    if (rc != MRMD_OK)
+    {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    MRMD_TRY(check_cuda(ctx, e, "batch end capture"));
+    b->graph = g;
+    MRMD_CUDA(ctx, cudaGraphInstantiate(&b->exec, g, 0));
+    return MRMD_OK;
+}
+
+// energies of steps [st0, st0 + count) from the ring into out[k][R]
+int read_ring(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0, int64_t count, double* out)
+{
+    if (!out || count <= 0) return MRMD_OK;
+    const int64_t R = b->R, ring = b->B.ring;
+    MRMD_CUDA(ctx, cudaMemcpyAsync(b->hRing, b->B.energyRing, sizeof(double) * (size_t)(ring * R),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t k = 0; k < count; ++k)
+        std::memcpy(out + k * R, b->hRing + ((st0 + k) % ring) * R, sizeof(double) * (size_t)R);
+    return MRMD_OK;
+}
+
+int run_graph(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
+{
+    BDev& B = b->B;
+    for (int attempt = 0;; ++attempt)
+    {
+        if (!b->exec) MRMD_TRY(capture(ctx, b, st0));
+        MRMD_CUDA(ctx, cudaMemsetAsync(&B.sc->overflow, 0, sizeof(uint32_t), ctx->stream));
+        MRMD_TRY(snapshot(ctx, b, b->sn, true));
+        MRMD_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+        ctx->launches += b->graphKernels;
+        b->graphLaunches++;
+        MRMD_CUDA(ctx, cudaMemcpyAsync(b->hSc, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const uint32_t f = b->hSc->overflow;
+        const int64_t P = b->cfg.tuning.graphSteps;
+        if (!f)
+        {
+            b->rebuilds += P / b->cfg.tuning.rebuildInterval;
+            return MRMD_OK;
+        }
+        if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
+        // roll back, grow, re-capture
+        const int32_t needG = b->hSc->numGhost, needL = b->hSc->maxCount;
+        MRMD_TRY(snapshot(ctx, b, b->sn, false));
+        int32_t gCap = B.gCap, lCap = B.listCap;
+        if (f & FLAG_GHOST_OVERFLOW) gCap = needG + needG / 4 + 1024;
+        if (f & FLAG_LIST_OVERFLOW) lCap = needL + needL / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
+        drop_graph(b);
+        b->recoveries++;
+    }
+}
+
+int validate_tuning(mrmd_ctx* ctx, const mrmd_batch_tuning& t)
+{
+    MRMD_CHECK_ARG(t.threadsPerRow == 1 || t.threadsPerRow == 2 || t.threadsPerRow == 4 || t.threadsPerRow == 8, ctx,
+                   "threadsPerRow must be 1, 2, 4 or 8");
+    MRMD_CHECK_ARG(t.blockSize >= 64 && t.blockSize <= 1024 && t.blockSize % 32 == 0, ctx, "bad blockSize");
+    MRMD_CHECK_ARG(t.rebuildInterval >= 1 && t.sortEvery >= 0 && t.graphSteps >= 0, ctx, "bad tuning intervals");
+    const int64_t period = t.rebuildInterval * (t.sortEvery > 0 ? t.sortEvery : 1);
+    MRMD_CHECK_ARG(t.graphSteps == 0 || t.graphSteps % period == 0, ctx,
+                   "graphSteps must be a multiple of rebuildInterval * sortEvery");
+    return MRMD_OK;
+}
+
+// ring size and pinned host copy follow graphSteps
+int ensure_ring(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    const int32_t need = (int32_t)std::max<int64_t>(b->cfg.tuning.graphSteps, 64);
+    if (need <= b->B.ring) return MRMD_OK;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(b->B.energyRing);
+    b->B.energyRing = nullptr;
+    if (b->hRing) cudaFreeHost(b->hRing);
+    b->hRing = nullptr;
+    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&b->B.energyRing), sizeof(double) * (size_t)need * b->R));
+    MRMD_TRY(dzero(ctx, b->B.energyRing, sizeof(double) * (size_t)need * b->R));
+    MRMD_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&b->hRing), sizeof(double) * (size_t)need * b->R));
+    b->B.ring = need;
+    drop_graph(b);
+    return MRMD_OK;
+}
+
+void free_all(mrmd_batch* b)
+{
+    drop_graph(b);
+    BDev& B = b->B;
+    void* ptrs[] = {B.pos, B.vel, B.force, B.mass, B.orig, B.slotRep, B.gSrc, B.gShift, B.imgFlags, B.ref, B.gCount,
+                    B.lam, B.lamt, B.lamtf, B.hi, B.lo, B.cellOf, B.cellStart, B.cursor, B.unordered, B.sorted,
+                    B.spos, B.counts, B.nbrs, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce, B.tfDensity, B.tfWork,
+                    B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc, b->dReps, b->dTfFF};
+    for (void* p : ptrs) dfree(p);
+    snap_free(b->sn);
+    if (b->hSc) cudaFreeHost(b->hSc);
+    if (b->hRing) cudaFreeHost(b->hRing);
+}
+}  // namespace
+
+extern "C" {
+
+int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* cfg, int64_t numReplicas,
+                      const mrmd_replica_desc* replicas, const double* pos3, const double* vel3)
+{
+    if (!ctx || !out || !cfg || !replicas || !pos3 || !vel3 || numReplicas <= 0) return MRMD_ERR_ARG;
+    MRMD_CHECK_ARG(cfg->rc > 0 && cfg->skin >= 0 && cfg->dt > 0, ctx, "bad config");
+    MRMD_CHECK_ARG(cfg->precision == MRMD_PREC_FP64 || cfg->precision == MRMD_PREC_MIXED, ctx, "bad precision");
+    MRMD_CHECK_ARG(cfg->hybridDiameter > 0.0 && cfg->nu >= 1, ctx, "bad hybrid region");
+    MRMD_CHECK_ARG(!cfg->tfEnabled || (cfg->tfSampleInterval >= 1 && cfg->tfUpdateInterval >= 1 && cfg->tfBinWidth > 0),
+                   ctx, "bad thermodynamic-force settings");
+    MRMD_TRY(validate_tuning(ctx, cfg->tuning));
+    *out = nullptr;
+    mrmd_batch* b = new mrmd_batch();
+    b->cfg = *cfg;
+    if (b->cfg.compSamplingInterval <= 0) b->cfg.compSamplingInterval = 200;   // LJ_IdealGas.hpp:69
+    if (b->cfg.compUpdateInterval <= 0) b->cfg.compUpdateInterval = 20000;    // LJ_IdealGas.hpp:70
+    const double rlist = cfg->rc + cfg->skin;
+    const double ghost3[3] = {rlist, rlist, rlist};
+    b->R = (int32_t)numReplicas;
+    b->offsets.assign((size_t)numReplicas + 1, 0);
+    b->reps.resize((size_t)numReplicas);
+    int rc = MRMD_OK;
+    int64_t cellBase = 0, binBase = 0;
+    for (int64_t r = 0; r < numReplicas && rc == MRMD_OK; ++r)
+    {
+        const mrmd_replica_desc& d = replicas[r];
+        RepDev& R = b->reps[(size_t)r];
+        mrmd_subdomain sd{};
+        if (d.numMolecules < 1 || mrmd_subdomain_init(&sd, d.boxMin, d.boxMax, ghost3) != MRMD_OK)
+        {
+            rc = set_error(ctx, MRMD_ERR_ARG, "replica %lld: bad size or box", (long long)r);
+            break;
+        }
+        for (int a = 0; a < 3; ++a)
+            if (!(sd.diameter[a] > rlist)) rc = set_error(ctx, MRMD_ERR_ARG, "replica %lld: box must exceed the list radius", (long long)r);
+        const CellGrid g = make_grid(sd.minGhostCorner, sd.maxGhostCorner, rlist);
+        for (int a = 0; a < 3; ++a)
+        {
+            R.lo[a] = sd.minCorner[a];
+            R.mx[a] = sd.maxCorner[a];
+            R.L[a] = sd.diameter[a];
+            R.minIn[a] = sd.minInnerCorner[a];
+            R.maxIn[a] = sd.maxInnerCorner[a];
+        }
+        R.gmn[0] = g.mn.x;
+        R.gmn[1] = g.mn.y;
+        R.gmn[2] = g.mn.z;
+        R.grdx[0] = g.rdx.x;
+        R.grdx[1] = g.rdx.y;
+        R.grdx[2] = g.rdx.z;
+        R.gn[0] = g.n.x;
+        R.gn[1] = g.n.y;
+        R.gn[2] = g.n.z;
+        R.cellBase = (int32_t)cellBase;
+        cellBase += g.ncell;
+        b->listExtent = std::fmax(b->listExtent, g.extent);
+        double ext = 0.0;
+        for (int a = 0; a < 3; ++a) ext = std::fmax(ext, sd.diameterWithGhostLayer[a]);
+        const SplitParams sp = split_params(sd.minGhostCorner, ext * 1.25 + 8.0);
+        R.splitScale = sp.scale;
+        R.splitInv = sp.invScale;
+        mrmd_slab slab{};
+        slab.center[0] = d.slabCenter[0];
+        slab.center[1] = d.slabCenter[1];
+        slab.center[2] = d.slabCenter[2];
+        slab.atomisticRegionDiameter = d.atomisticDiameter;
+        slab.hybridRegionDiameter = cfg->hybridDiameter;
+        slab.nu = cfg->nu;
+        slab.interfaceType = 0;
+        R.slab = to_slab(&slab);
+        // every molecule within r_list (+ skin of drift) of an x face and every
+        // image lies outside the slab's outer edge on both sides
+        const double rOut = R.slab.atHalf + R.slab.hy, margin = rlist + cfg->skin + 1e-9 * (1.0 + sd.diameter[0]);
+        R.consistent = (R.slab.cx - rOut > sd.minCorner[0] + margin) && (R.slab.cx + rOut < sd.maxCorner[0] - margin);
+        R.lbase = (int32_t)b->offsets[(size_t)r];
+        R.n = (int32_t)d.numMolecules;
+        b->offsets[(size_t)r + 1] = b->offsets[(size_t)r] + d.numMolecules;
+        R.seed = d.seed;
+        // ThermodynamicForce on x bins (ThermodynamicForce.cpp:25-57, MultiHistogram.hpp:40-41)
+        R.tfBins = 0;
+        if (cfg->tfEnabled)
+        {
+            const int64_t nb = (int64_t)std::ceil(sd.diameter[0] / cfg->tfBinWidth);
+            R.tfBins = (int32_t)nb;
+            R.tfMin = sd.minCorner[0];
+            R.tfBinSize = (sd.maxCorner[0] - sd.minCorner[0]) / (double)nb;
+            R.tfInvBin = 1.0 / R.tfBinSize;
+            R.tfBinVolume = sd.diameter[1] * sd.diameter[2] * R.tfBinSize;
+            if (!(R.tfBinSize <= cfg->tfBinWidth)) rc = set_error(ctx, MRMD_ERR_ARG, "requested bin size is not achieved");
+        }
+        R.tfBase = (int32_t)binBase;
+        binBase += R.tfBins;
+    }
+    const int64_t N = b->offsets.back();
+    if (rc == MRMD_OK && (N > INT32_MAX / 4 || cellBase > INT32_MAX - 1))
+        rc = set_error(ctx, MRMD_ERR_CAPACITY, "too many molecules or cells");
+    if (rc != MRMD_OK)
+    {
+        delete b;
+        return rc;
+    }
+    b->N = (int32_t)N;
+    b->totalCells = cellBase;
+    b->totalBins = binBase;
+    BDev& B = b->B;
+    B.R = b->R;
+    B.N = b->N;
+    B.totalCells = cellBase;
+    B.totalBins = binBase;
+    // physics
+    {
+        mrmd_lj_params t{};
+        const double c = cfg->cappingDistance, r = cfg->rc, sg = cfg->sigma, e = cfg->epsilon;
+        lj_table_host(&t, 1, &c, &r, &sg, &e, cfg->shifted);
+        B.lj = to_dev(t);
+        B.rcSqr = cfg->rc * cfg->rc;  // LJ_IdealGas.cpp:290-291
+        B.rc2 = make_rcsq(B.rcSqr);
+    }
+    B.dt = cfg->dt;
+    B.zeta = cfg->gamma;
+    B.temperature = cfg->temperature;
+    B.rlist = rlist;
+    B.halfSkin = 0.5 * cfg->skin;
+    B.K = cfg->tuning.rebuildInterval;
+    B.tfEnabled = cfg->tfEnabled;
+    B.tfSampleInterval = cfg->tfEnabled ? cfg->tfSampleInterval : 1;
+    B.tfUpdateInterval = cfg->tfEnabled ? cfg->tfUpdateInterval : 1;
+    B.compSampling = b->cfg.compSamplingInterval;
+    B.compUpdate = b->cfg.compUpdateInterval;
+    B.tfSigma = cfg->tfSmoothingSigma;
+    B.tfRange = cfg->tfSmoothingRange;
+    {
+        // FP32 error band of the list build (as in build_half_list)
+        const double delta = std::ldexp(b->listExtent, -22);
+        const double band = 6.0 * rlist * delta + 3.0 * delta * delta + std::ldexp(rlist * rlist, -20);
+        B.listRsq = rlist * rlist;
+        B.listRsqLo = (float)std::fmax(0.0, (B.listRsq - 2.0 * band) * (1.0 - 1e-6));
+        B.listRsqHi = (float)((B.listRsq + 2.0 * band) * (1.0 + 1e-6));
+    }
+    // buffers
+    const int64_t nb = std::max<int64_t>(binBase, 1), nc = (int64_t)b->R * COMP_BINS;
+    auto alloc = [&](auto*& p, int64_t count) {
+        if (rc == MRMD_OK) rc = grow(ctx, p, 0, count);
+        if (rc == MRMD_OK) rc = dzero(ctx, p, sizeof(*p) * (size_t)std::max<int64_t>(count, 1));
+    };
+    alloc(B.vel, N);
+    alloc(B.force, N);
+    alloc(B.mass, N);
+    alloc(B.orig, N);
+    alloc(B.imgFlags, N);
+    alloc(B.ref, N);
+    alloc(B.gCount, N + 1);
+    alloc(B.counts, N);
+    alloc(B.sPos, N);
+    alloc(B.sVel, N);
+    alloc(B.sMass, N);
+    alloc(B.sOrig, N);
+    alloc(B.cellStart, cellBase + 1);
+    alloc(B.cursor, cellBase + 1);
+    alloc(B.tfForce, nb);
+    alloc(B.tfDensity, nb);
+    alloc(B.tfWork, 3 * nb);
+    alloc(B.compEnergy, nc);
+    alloc(B.compCounter, nc);
+    alloc(B.compMean, nc);
+    alloc(B.sc, 1);
+    alloc(b->dReps, b->R);
+    alloc(b->dTfFF, 1);
+    if (rc == MRMD_OK) rc = snap_alloc(ctx, b, b->sn);
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaMallocHost(reinterpret_cast<void**>(&b->hSc), sizeof(Scalars)), "batch pinned");
+    if (rc == MRMD_OK) rc = ensure_ring(ctx, b);
+    // initial guesses for the ghost and list capacity: measured below
+    const int32_t g0 = cfg->initialGhostCapacity > 0 ? (int32_t)cfg->initialGhostCapacity : (int32_t)std::min<int64_t>(2 * N + 1024, INT32_MAX / 2);
+    const int32_t l0 = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : 64;
+    if (rc == MRMD_OK) rc = set_capacity(ctx, b, g0, l0);
+    B.reps = b->dReps;
+    B.tfFF = b->dTfFF;
+    if (rc == MRMD_OK)
+        rc = h2d(ctx, b->dReps, b->reps.data(), sizeof(RepDev) * b->reps.size());
+    if (rc == MRMD_OK)
+    {
+        const double ff = cfg->tfTargetDensity != 0.0 ? cfg->tfModulation / cfg->tfTargetDensity : 0.0;
+        rc = h2d(ctx, b->dTfFF, &ff, sizeof(double));
+    }
+    if (rc == MRMD_OK)
+    {
+        // molecules, replica after replica (slot i = input index i)
+        std::vector<double4> p4((size_t)N), v4((size_t)N);
+        std::vector<int32_t> rep((size_t)N), orig((size_t)N);
+        std::vector<double> mass((size_t)N, 1.0);
+        for (int32_t r = 0; r < b->R; ++r)
+            for (int64_t i = b->offsets[(size_t)r]; i < b->offsets[(size_t)r + 1]; ++i) rep[(size_t)i] = r;
+        for (int64_t i = 0; i < N; ++i)
+        {
+            p4[(size_t)i] = make_double4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], 0.0);
+            v4[(size_t)i] = make_double4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0);
+            orig[(size_t)i] = (int32_t)i;
+        }
+        rc = h2d(ctx, B.pos, p4.data(), sizeof(double4) * (size_t)N);
+        if (rc == MRMD_OK) rc = h2d(ctx, B.vel, v4.data(), sizeof(double4) * (size_t)N);
+        if (rc == MRMD_OK) rc = h2d(ctx, B.mass, mass.data(), sizeof(double) * (size_t)N);
+        if (rc == MRMD_OK) rc = h2d(ctx, B.orig, orig.data(), sizeof(int32_t) * (size_t)N);
+        if (rc == MRMD_OK) rc = h2d(ctx, B.slotRep, rep.data(), sizeof(int32_t) * (size_t)N);
+    }
+    if (rc == MRMD_OK)
+    {
+        // size the buffers on the initial configuration: a rebuild that only
+        // writes ghosts, cells and lists (overwritten by the first step);
+        // it also sizes the scan scratch before any graph capture
+        const int oldSync = ctx->sync;
+        ctx->sync = 0;
+        rc = rebuild(ctx, b, false);
+        // the context stream does not synchronise with the legacy stream
+        if (rc == MRMD_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "probe");
+        if (rc == MRMD_OK) rc = d2h(ctx, b->hSc, B.sc, sizeof(Scalars));
+        ctx->sync = oldSync;
+        if (rc == MRMD_OK)
+        {
+            const int32_t ng = b->hSc->numGhost;
+            int32_t mc = b->hSc->maxCount;
+            if (!(b->hSc->overflow & FLAG_LIST_OVERFLOW))
+            {
+                // no overflow: the largest row is below the guess; measure it
+                std::vector<int32_t> counts((size_t)N);
+                rc = d2h(ctx, counts.data(), B.counts, sizeof(int32_t) * (size_t)N);
+                mc = 0;
+                for (int32_t c : counts) mc = std::max(mc, c);
+            }
+            const int32_t gCap = cfg->initialGhostCapacity > 0 ? (int32_t)cfg->initialGhostCapacity : ng + ng / 3 + 1024;
+            const int32_t lCap = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : mc + mc / 3 + 8;
+            Scalars z{};
+            if (rc == MRMD_OK) rc = h2d(ctx, B.sc, &z, sizeof(Scalars));
+            if (rc == MRMD_OK) rc = set_capacity(ctx, b, gCap, lCap);
+        }
+    }
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaDeviceSynchronize(), "batch create");
+    if (rc != MRMD_OK)
+    {
+        free_all(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return MRMD_OK;
+}
+
+int mrmd_batch_destroy(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    if (!b) return MRMD_OK;
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    free_all(b);
+    delete b;
+    return MRMD_OK;
+}
+
+int mrmd_batch_run(mrmd_ctx* ctx, mrmd_batch* b, int64_t nsteps, double* energies)
+{
+    if (!ctx || !b || nsteps < 0) return MRMD_ERR_ARG;
+    const int oldSync = ctx->sync;
+    ctx->sync = 0;
+    const int64_t P = b->cfg.tuning.graphSteps;
+    int rc = MRMD_OK;
+    int64_t k = 0;
+    while (rc == MRMD_OK && k < nsteps)
+    {
+        const int64_t st = b->steps + k;
+        if (P > 0 && st % P == 0 && nsteps - k >= P)
+        {
+            rc = run_graph(ctx, b, st);
+            if (rc == MRMD_OK) rc = read_ring(ctx, b, st, P, energies ? energies + k * b->R : nullptr);
+            k += P;
+        }
+        else
+        {
+            rc = step(ctx, b, st, true);
+            if (rc == MRMD_OK) rc = read_ring(ctx, b, st, 1, energies ? energies + k * b->R : nullptr);
+            ++k;
+        }
+    }
+    b->steps += k;
+    ctx->sync = oldSync;
+    MRMD_TRY(rc);
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "batch run");
+}
+
+int mrmd_batch_get_state(mrmd_ctx* ctx, mrmd_batch* b, double* pos3, double* vel3, double* force3)
+{
+    if (!ctx || !b) return MRMD_ERR_ARG;
+    const size_t N = (size_t)b->N;
+    std::vector<double4> h(N);
+    std::vector<int32_t> orig(N);
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MRMD_TRY(d2h(ctx, orig.data(), b->B.orig, sizeof(int32_t) * N));
+    double* outs[3] = {pos3, vel3, force3};
+    const double4* src[3] = {b->B.pos, b->B.vel, b->B.force};
+    for (int q = 0; q < 3; ++q)
+    {
+        if (!outs[q]) continue;
+        MRMD_TRY(d2h(ctx, h.data(), src[q], sizeof(double4) * N));
+        for (size_t i = 0; i < N; ++i)
+        {
+            const size_t o = (size_t)orig[i];
+            outs[q][3 * o] = h[i].x;
+            outs[q][3 * o + 1] = h[i].y;
+            outs[q][3 * o + 2] = h[i].z;
+        }
+    }
+    return MRMD_OK;
+}
+
+int mrmd_batch_get_tf(mrmd_ctx* ctx, mrmd_batch* b, double* force, double* density, int64_t* binOffsets)
+{
+    if (!ctx || !b) return MRMD_ERR_ARG;
+    const size_t nb = (size_t)b->totalBins;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (force && nb) MRMD_TRY(d2h(ctx, force, b->B.tfForce, sizeof(double) * nb));
+    if (density && nb)
+    {
+        std::vector<unsigned long long> c(nb);
+        MRMD_TRY(d2h(ctx, c.data(), b->B.tfDensity, sizeof(unsigned long long) * nb));
+        for (size_t k = 0; k < nb; ++k) density[k] = (double)c[k];
+    }
+    if (binOffsets)
+    {
+        for (int32_t r = 0; r < b->R; ++r) binOffsets[r] = b->reps[(size_t)r].tfBase;
+        binOffsets[b->R] = b->totalBins;
+    }
+    return MRMD_OK;
+}
+
+int mrmd_batch_set_tf(mrmd_ctx* ctx, mrmd_batch* b, const double* force)
+{
+    if (!ctx || !b || !force) return MRMD_ERR_ARG;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (b->totalBins)
+        MRMD_TRY(h2d(ctx, b->B.tfForce, force, sizeof(double) * (size_t)b->totalBins));
+    return MRMD_OK;
+}
+
+int mrmd_batch_get_compensation(mrmd_ctx* ctx, mrmd_batch* b, double* mean)
+{
+    if (!ctx || !b || !mean) return MRMD_ERR_ARG;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MRMD_TRY(d2h(ctx, mean, b->B.compMean, sizeof(double) * (size_t)b->R * COMP_BINS));
+    return MRMD_OK;
+}
+
+int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t)
+{
+    if (!b || !t) return MRMD_ERR_ARG;
+    *t = b->cfg.tuning;
+    return MRMD_OK;
+}
+
+int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning* t)
+{
+    if (!ctx || !b || !t) return MRMD_ERR_ARG;
+    MRMD_TRY(validate_tuning(ctx, *t));
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    b->cfg.tuning = *t;
+    b->B.K = t->rebuildInterval;
+    b->needRebuild = true;
+    drop_graph(b);
+    return ensure_ring(ctx, b);
+}
+
+int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
+{
+    if (!ctx || !b || !out10) return MRMD_ERR_ARG;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    MRMD_TRY(d2h(ctx, b->hSc, b->B.sc, sizeof(Scalars)));
+    std::vector<int32_t> counts((size_t)b->N);
+    MRMD_TRY(d2h(ctx, counts.data(), b->B.counts, sizeof(int32_t) * counts.size()));
+    int64_t pairs = 0;
+    for (int32_t c : counts) pairs += c;
+    out10[0] = b->steps;
+    out10[1] = b->rebuilds;
+    out10[2] = pairs;
+    out10[3] = b->hSc->numGhost;
+    out10[4] = b->graphLaunches;
+    out10[5] = ctx->launches;
+    out10[6] = b->recoveries;
+    out10[7] = b->B.listCap;
+    out10[8] = b->B.gCap;
+    out10[9] = b->hSc->flags | b->hSc->overflow;
+    return MRMD_OK;
+}
+
+}  // extern "C"
+
+namespace
+{
+// steps [b->steps, b->steps + n) through the same path as mrmd_batch_run,
+// without energies
+int advance(mrmd_ctx* ctx, mrmd_batch* b, int64_t n)
+{
+    const int64_t P = b->cfg.tuning.graphSteps;
+    int64_t k = 0;
+    while (k < n)
+    {
+        const int64_t st = b->steps + k;
+        if (P > 0 && st % P == 0 && n - k >= P)
+        {
+            MRMD_TRY(run_graph(ctx, b, st));
+            k += P;
+        }
+        else
+        {
+            MRMD_TRY(step(ctx, b, st, true));
+            ++k;
+        }
+    }
+    b->steps += k;
+    return MRMD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_batch_tuning* best,
+                        double* msPerStep, mrmd_batch_tuning* candidates, int64_t* numCandidates)
+{
+    if (!ctx || !b || trialSteps < 1) return MRMD_ERR_ARG;
+    const mrmd_batch_tuning t0 = b->cfg.tuning;
+    // candidates: lanes per row x block size x rebuild interval
+    std::vector<mrmd_batch_tuning> cand;
+    const int tprs[4] = {1, 2, 4, 8};
+    const int blocks[3] = {64, 128, 256};
+    const int64_t Ks[2] = {t0.rebuildInterval, 2 * t0.rebuildInterval};
+    for (int64_t K : Ks)
+        for (int tpr : tprs)
+            for (int bs : blocks)
+            {
+                mrmd_batch_tuning t = t0;
+                t.threadsPerRow = tpr;
+                t.blockSize = bs;
+                t.rebuildInterval = K;
+                const int64_t period = K * (t.sortEvery > 0 ? t.sortEvery : 1);
+                if (t.graphSteps > 0) t.graphSteps = ((t0.graphSteps + period - 1) / period) * period;
+                cand.push_back(t);
+            }
+    const int oldSync = ctx->sync;
+    ctx->sync = 0;
+    Snap keep;
+    int rc = snap_alloc(ctx, b, keep);
+    if (rc == MRMD_OK) rc = snapshot(ctx, b, keep, true);
+    const int64_t steps0 = b->steps, reb0 = b->rebuilds, gl0 = b->graphLaunches, rec0 = b->recoveries;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventCreate(&e0), "event");
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventCreate(&e1), "event");
+    std::vector<double> ms(cand.size(), -1.0);
+    int bestIdx = -1;
+    for (size_t c = 0; c < cand.size() && rc == MRMD_OK; ++c)
+    {
+        b->cfg.tuning = cand[c];
+        b->B.K = cand[c].rebuildInterval;
+        b->needRebuild = true;
+        drop_graph(b);
+        rc = ensure_ring(ctx, b);
+        // warm-up (captures the graph), then the timed trial from the same state
+        if (rc == MRMD_OK) rc = advance(ctx, b, std::max<int64_t>(cand[c].graphSteps, 1));
+        b->steps = steps0;
+        b->needRebuild = true;
+        if (rc == MRMD_OK) rc = snapshot(ctx, b, keep, false);
+        if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventRecord(e0, ctx->stream), "event");
+        if (rc == MRMD_OK) rc = advance(ctx, b, trialSteps);
+        if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventRecord(e1, ctx->stream), "event");
+        if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventSynchronize(e1), "event");
+        float t = 0.0f;
+        if (rc == MRMD_OK) rc = check_cuda(ctx, cudaEventElapsedTime(&t, e0, e1), "event");
+        if (rc == MRMD_OK) rc = d2h(ctx, b->hSc, b->B.sc, sizeof(Scalars));
+        if (rc == MRMD_OK)
+        {
+            // a longer rebuild interval than the configured one must keep every
+            // molecule within skin/2 of its position at the last rebuild
+            const bool safe = !(b->hSc->flags & FLAG_UNSAFE_INTERVAL) || cand[c].rebuildInterval <= t0.rebuildInterval;
+            ms[c] = safe ? (double)t / (double)trialSteps : -1.0;
+            if (safe && (bestIdx < 0 || ms[c] < ms[(size_t)bestIdx])) bestIdx = (int)c;
+        }
+        b->steps = steps0;
+        if (rc == MRMD_OK) rc = snapshot(ctx, b, keep, false);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    b->rebuilds = reb0;
+    b->graphLaunches = gl0;
+    b->recoveries = rec0;
+    b->cfg.tuning = bestIdx >= 0 ? cand[(size_t)bestIdx] : t0;
+    b->B.K = b->cfg.tuning.rebuildInterval;
+    b->needRebuild = true;
+    drop_graph(b);
+    if (rc == MRMD_OK) rc = ensure_ring(ctx, b);
+    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "autotune");
+    snap_free(keep);
+    ctx->sync = oldSync;
+    MRMD_TRY(rc);
+    if (best) *best = b->cfg.tuning;
+    if (numCandidates) *numCandidates = (int64_t)cand.size();
+    for (size_t c = 0; c < cand.size(); ++c)
+    {
+        if (msPerStep) msPerStep[c] = ms[c];
+        if (candidates) candidates[c] = cand[c];
+    }
+    return bestIdx >= 0 ? MRMD_OK : set_error(ctx, MRMD_ERR_STATE, "no candidate kept the displacement below skin/2");
+}
+
+}  // extern "C"

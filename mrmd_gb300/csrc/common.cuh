@@ -50,6 +50,13 @@ void* scratch(mrmd_ctx* ctx, size_t bytes);
 int dmalloc(mrmd_ctx* ctx, void** p, size_t bytes);
 void dfree(void* p);
 
+// Synchronous copies and fills ordered with the context stream (which is
+// non-blocking, so plain cudaMemcpy/cudaMemset on the legacy stream would
+// not be ordered with its kernels).
+int h2d(mrmd_ctx* ctx, void* dst, const void* src, size_t bytes);
+int d2h(mrmd_ctx* ctx, void* dst, const void* src, size_t bytes);
+int dzero(mrmd_ctx* ctx, void* p, size_t bytes);
+
 inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // Grid size for a grid-stride kernel over n items: a multiple of the SM

@@ -59,6 +59,27 @@ void dfree(void* p)
     if (p) cudaFree(p);
 }
 
+int h2d(mrmd_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+    if (bytes == 0) return MRMD_OK;
+    MRMD_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "h2d");
+}
+
+int d2h(mrmd_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+    if (bytes == 0) return MRMD_OK;
+    MRMD_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "d2h");
+}
+
+int dzero(mrmd_ctx* ctx, void* p, size_t bytes)
+{
+    if (bytes == 0) return MRMD_OK;
+    MRMD_CUDA(ctx, cudaMemsetAsync(p, 0, bytes, ctx->stream));
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "dzero");
+}
+
 static void* grow_buffer(mrmd_ctx* ctx, void*& buf, size_t& have, size_t bytes)
 {
     if (bytes <= have) return buf;

@@ -170,8 +170,7 @@ int mrmd_lj_create(mrmd_ctx* ctx, mrmd_lj** out, int64_t numTypes, int64_t numTy
     lj->p0 = dev[0];
     int rc2 = dmalloc(ctx, reinterpret_cast<void**>(&lj->dTable), sizeof(LJDev) * (size_t)n2);
     if (rc2 == MRMD_OK)
-        rc2 = check_cuda(ctx, cudaMemcpy(lj->dTable, dev.data(), sizeof(LJDev) * (size_t)n2, cudaMemcpyHostToDevice),
-                         "lj table");
+        rc2 = h2d(ctx, lj->dTable, dev.data(), sizeof(LJDev) * (size_t)n2);
     if (rc2 != MRMD_OK)
     {
         dfree(lj->dTable);

@@ -56,12 +56,12 @@ inline RcSq make_rcsq(double rcSqr)
 
 // Result of one pair in the mixed form.  dx = dh + dl exactly (the split
 // coordinates make hi_i - hi_j exact), ff is the double-float force factor
-// (F_i += dx * ff), e the FP32 pair energy, r2h the FP32 head of r^2.
+// (F_i += dx * ff), e the FP32 pair energy, (r2h, r2l) r^2 as a double-float.
 struct PairMixed
 {
     float3 dh, dl;
     df ff;
-    float e, r2h;
+    float e, r2h, r2l;
 };
 
 // One pair in the mixed form; false when outside the cutoff (distSqr > rcSqr).
@@ -88,6 +88,7 @@ __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_
     const df r2 = fast_two_sum(s2.h, s2.l + s1.l + lo);
     if (r2.h > rc2.h || (r2.h == rc2.h && r2.l > rc2.l)) return false;
     o.r2h = r2.h;
+    o.r2l = r2.l;
     if (r2.h >= p.capSqrf)
     {
         const df u = df_rcp(r2);

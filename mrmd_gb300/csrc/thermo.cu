@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "thermo_impl.cuh"
 
 using namespace mrmd_impl;
 
@@ -28,21 +29,6 @@ struct mrmd_tf
 namespace
 {
 constexpr int TB = 256;
-
-struct HistDev
-{
-    double min, binSize, inverseBinSize;
-    int64_t numBins, numTypes;
-};
-
-__device__ __forceinline__ int64_t get_bin(const HistDev& h, double v)
-{
-    // data/MultiHistogram.hpp:60-66
-    int64_t b = (int64_t)floor((v - h.min) * h.inverseBinSize);
-    if (b < 0) b = -1;
-    if (b >= h.numBins) b = -1;
-    return b;
-}
 
 __global__ void k_density(const double4* __restrict__ pos, const int32_t* __restrict__ type, int64_t n, HistDev h,
                           double* __restrict__ density, int useShared)
@@ -126,101 +112,7 @@ __global__ void k_tf_apply(double4* __restrict__ force, const double4* __restric
     }
 }
 
-struct UpdateArgs
-{
-    double* density;
-    double* force;
-    double* smooth;
-    double* grad;
-    const double* forceFactor;
-    int64_t numBins, numTypes;
-    double binSize, inverseBinSize, min;
-    double normalization;
-    double sigma, range;
-    int enforceSymmetry, periodic;
-    mrmd_dev::Pred pred;
-    int usePred;
-};
-
-__global__ void k_tf_update(UpdateArgs A)
-{
-    // ThermodynamicForce.hpp:124-152 as one block
-    const int64_t nb = A.numBins, nh = A.numTypes, nbh = nb * nh;
-    double* d = A.density;
-    if (A.enforceSymmetry)
-    {
-        // MultiHistogram.cpp:76-90
-        const int64_t maxIdx = nb - 1;
-        for (int64_t k = threadIdx.x; k < (nb / 2) * nh; k += blockDim.x)
-        {
-            const int64_t i = k / nh, j = k % nh;
-            const double val = 0.5 * (d[i * nh + j] + d[(maxIdx - i) * nh + j]);
-            d[i * nh + j] = val;
-            d[(maxIdx - i) * nh + j] = val;
-        }
-        __syncthreads();
-    }
-    for (int64_t k = threadIdx.x; k < nbh; k += blockDim.x) d[k] = __dmul_rn(d[k], A.normalization);
-    __syncthreads();
-    // smoothen, MultiHistogram.cpp:163-212
-    const double inverseSigma = 1.0 / A.sigma;
-    const int64_t delta = (int64_t)(int)(A.range * A.sigma * A.inverseBinSize);
-    for (int64_t k = threadIdx.x; k < nbh; k += blockDim.x)
-    {
-        const int64_t b = k / nh, h = k % nh;
-        double normalization = 0.0, acc = 0.0;
-        int64_t jMin = b - delta, jMax = b + delta;
-        if (!A.periodic)
-        {
-            jMin = jMin < 0 ? 0 : jMin;
-            jMax = jMax > nb - 1 ? nb - 1 : jMax;
-        }
-        for (int64_t j = jMin; j <= jMax; ++j)
-        {
-            int64_t m = j;
-            if (A.periodic)
-            {
-                if (m < 0) m += nb;
-                if (m >= nb) m -= nb;
-            }
-            const double t = __dmul_rn(__dmul_rn((double)(b - j), A.binSize), inverseSigma);
-            const double eFunc = exp(-__dmul_rn(t, t));
-            normalization = __dadd_rn(normalization, eFunc);
-            acc = __dadd_rn(acc, __dmul_rn(d[m * nh + h], eFunc));
-        }
-        A.smooth[k] = __ddiv_rn(acc, normalization);
-    }
-    __syncthreads();
-    // gradient, MultiHistogram.cpp:113-161; scale by forceFactor; replace_if; force -= grad
-    const double inv = A.inverseBinSize, inv2 = 0.5 * A.inverseBinSize;
-    const double* s = A.smooth;
-    for (int64_t k = threadIdx.x; k < nbh; k += blockDim.x)
-    {
-        const int64_t i = k / nh, j = k % nh;
-        double g;
-        if (i == 0)
-            g = A.periodic ? __dmul_rn(__dsub_rn(s[(i + 1) * nh + j], s[(nb - 1) * nh + j]), inv2)
-                           : __dmul_rn(__dsub_rn(s[(i + 1) * nh + j], s[i * nh + j]), inv);
-        else if (i == nb - 1)
-            g = A.periodic ? __dmul_rn(__dsub_rn(s[j], s[(i - 1) * nh + j]), inv2)
-                           : __dmul_rn(__dsub_rn(s[i * nh + j], s[(i - 1) * nh + j]), inv);
-        else
-            g = __dmul_rn(__dsub_rn(s[(i + 1) * nh + j], s[(i - 1) * nh + j]), inv2);
-        g = __dmul_rn(g, A.forceFactor[j]);
-        if (A.usePred)
-        {
-            const double x = A.min + ((double)i + 0.5) * A.binSize;  // getBinPosition
-            if (!mrmd_dev::pred_coord(A.pred, x)) g = 0.0;
-        }
-        A.grad[k] = g;
-    }
-    __syncthreads();
-    for (int64_t k = threadIdx.x; k < nbh; k += blockDim.x)
-    {
-        A.force[k] = __dsub_rn(A.force[k], A.grad[k]);
-        d[k] = 0.0;
-    }
-}
+__global__ void k_tf_update(UpdateArgs A) { tf_update_block(A); }
 
 HistDev hist_of(const mrmd_tf* tf)
 {
@@ -266,11 +158,10 @@ int mrmd_tf_create(mrmd_ctx* ctx, mrmd_tf** out, int64_t numTypes, const double*
     int rc = dmalloc(ctx, reinterpret_cast<void**>(&tf->dForce), sizeof(double) * nbh);
     if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&tf->dDensity), sizeof(double) * nbh);
     if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&tf->dWork), sizeof(double) * (2 * nbh + numTypes));
-    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaMemset(tf->dForce, 0, sizeof(double) * nbh), "tf");
-    if (rc == MRMD_OK) rc = check_cuda(ctx, cudaMemset(tf->dDensity, 0, sizeof(double) * nbh), "tf");
+    if (rc == MRMD_OK) rc = dzero(ctx, tf->dForce, sizeof(double) * nbh);
+    if (rc == MRMD_OK) rc = dzero(ctx, tf->dDensity, sizeof(double) * nbh);
     if (rc == MRMD_OK)
-        rc = check_cuda(ctx, cudaMemcpy(tf->dWork + 2 * nbh, tf->forceFactor.data(), sizeof(double) * numTypes,
-                                        cudaMemcpyHostToDevice), "tf");
+        rc = h2d(ctx, tf->dWork + 2 * nbh, tf->forceFactor.data(), sizeof(double) * numTypes);
     if (rc != MRMD_OK)
     {
         dfree(tf->dForce);
@@ -370,8 +261,7 @@ int mrmd_tf_get_force(mrmd_ctx* ctx, const mrmd_tf* tf, double* out)
 {
     if (!ctx || !tf || !out) return MRMD_ERR_ARG;
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    MRMD_CUDA(ctx, cudaMemcpy(out, tf->dForce, sizeof(double) * (size_t)(tf->numBins * tf->numTypes),
-                              cudaMemcpyDeviceToHost));
+    MRMD_TRY(d2h(ctx, out, tf->dForce, sizeof(double) * (size_t)(tf->numBins * tf->numTypes)));
     return MRMD_OK;
 }
 
@@ -379,8 +269,7 @@ int mrmd_tf_set_force(mrmd_ctx* ctx, mrmd_tf* tf, const double* in)
 {
     if (!ctx || !tf || !in) return MRMD_ERR_ARG;
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    MRMD_CUDA(ctx, cudaMemcpy(tf->dForce, in, sizeof(double) * (size_t)(tf->numBins * tf->numTypes),
-                              cudaMemcpyHostToDevice));
+    MRMD_TRY(h2d(ctx, tf->dForce, in, sizeof(double) * (size_t)(tf->numBins * tf->numTypes)));
     return MRMD_OK;
 }
 
@@ -389,8 +278,7 @@ int mrmd_tf_get_density(mrmd_ctx* ctx, const mrmd_tf* tf, double* out, int64_t* 
     if (!ctx || !tf) return MRMD_ERR_ARG;
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (out)
-        MRMD_CUDA(ctx, cudaMemcpy(out, tf->dDensity, sizeof(double) * (size_t)(tf->numBins * tf->numTypes),
-                                  cudaMemcpyDeviceToHost));
+        MRMD_TRY(d2h(ctx, out, tf->dDensity, sizeof(double) * (size_t)(tf->numBins * tf->numTypes)));
     if (samples) *samples = tf->samples;
     return MRMD_OK;
 }

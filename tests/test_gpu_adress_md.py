@@ -4,6 +4,8 @@ MultiResGhostLayer, ThermodynamicForce sample/apply/update)."""
 import numpy as np
 import pytest
 
+from tests.adress_loop import oracle_loop, random_system
+
 pytestmark = pytest.mark.gpu
 
 
@@ -20,52 +22,7 @@ P = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=5, ga
 
 
 def system(n, box, seed):
-    rng = np.random.default_rng(seed)
-    pos = rng.uniform(0, 1, (n, 3)) * np.asarray(box)
-    vel = rng.normal(0, 1, (n, 3))
-    return pos, vel
-
-
-def oracle_loop(orc, pos, vel, box, nsteps, p):
-    n = len(pos)
-    rlist = p["rc"] + p["skin"]
-    sd = orc.subdomain([0, 0, 0], box, rlist)
-    a = orc.Atoms.from_positions(pos, capacity=4 * n)
-    a.vel[:n] = vel
-    m = orc.Molecules(4 * n)
-    m.atomsOffset[:n] = np.arange(n)
-    m.numAtoms[:n] = 1
-    m.numLocal = n
-    slab = orc.slab([box[0] / 2, box[1] / 2, box[2] / 2], p["at"], p["hy"], p["nu"])
-    ljig = orc.LJIdealGas(p["cap"], p["rc"], p["sigma"], p["epsilon"], True)
-    tf = orc.ThermodynamicForce([p["rho"]], sd, p["binw"], [p["mod"]], False, True)
-    energies = []
-    corr = co = no = None
-    for st in range(nsteps):
-        orc.langevin_pre(a, p["dt"], p["gamma"], p["T"], p["seed"], st)
-        if st % p["K"] == 0:
-            a.numGhost = 0
-            m.numGhost = 0
-            orc.update_molecules(m, a, slab)
-            orc.multires_map_into_domain(sd, m, a)
-            corr = orc.multires_create_ghosts(m, a, sd)
-            co, no = orc.build_half_list(m.pos, m.numLocal + m.numGhost, 0, m.numLocal, rlist,
-                                         sd.minGhostCorner, sd.maxGhostCorner, 1.0, 96)
-        else:
-            orc.update_ghosts(a, corr, sd)
-        orc.update_molecules(m, a, slab)
-        a.force[:] = 0
-        m.force[:] = 0
-        energies.append(ljig.run(m, co, no, a))
-        orc.contribute_molecule_force(m, a)
-        tf.apply(a)
-        orc.ghost_to_real(a, corr)
-        orc.vv_post(a, p["dt"])
-        if st % p["S"] == 0:
-            tf.sample(a)
-        if (st + 1) % p["U"] == 0:
-            tf.update(p["tfs"], p["tfr"])
-    return a.pos[:n].copy(), a.vel[:n].copy(), np.array(energies), tf.force[:, 0].copy()
+    return random_system(n, box, seed)
 
 
 def gpu_system(M, pos, vel, box, p, precision, graph=True):
@@ -83,7 +40,7 @@ def test_adress_trajectory_matches_oracle(M, orc, graph):
     box = [36.0, 10.0, 10.0]
     pos, vel = system(1800, box, 5)
     steps = 13
-    po, vo, eo, fo = oracle_loop(orc, pos, vel, box, steps, P)
+    po, vo, eo, fo, _ = oracle_loop(orc, pos, vel, box, steps, P)
     s = gpu_system(M, pos, vel, box, P, M.PREC_FP64, graph)
     eg = s.run(steps)
     pg, vg, _ = s.state()

@@ -1,0 +1,166 @@
+"""Batched AdResS replicas (mrmd_batch_*): one replica against the
+oracle-driven AdResS loop, every replica of a batch bitwise against the same
+replica run alone, capacity overflow recovery, and the autotuner."""
+import numpy as np
+import pytest
+
+from tests.adress_loop import oracle_loop, random_system
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    import mrmd_gb300 as M
+
+    M.default_context()
+    return M
+
+
+P = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=5, gamma=1.0, T=1.0, seed=77,
+         at=10.0, hy=5.0, nu=1, binw=1.2, rho=0.5, mod=1.0, tfs=2.4, tfr=3.0, S=2, U=6)
+
+
+def batch(M, replicas, pos, vel, p=P, precision=None, **tuning):
+    kw = dict(threads_per_row=1, block_size=128, rebuild_interval=p["K"], sort_every=0, graph_steps=p["K"])
+    kw.update(tuning)
+    return M.BatchSystem(replicas, pos, vel, hybrid_diameter=p["hy"], nu=p["nu"], rc=p["rc"], skin=p["skin"],
+                         sigma=p["sigma"], epsilon=p["epsilon"], capping_distance=p["cap"],
+                         precision=M.PREC_FP64 if precision is None else precision, dt=p["dt"],
+                         gamma=p["gamma"], temperature=p["T"], tf=True, tf_bin_width=p["binw"],
+                         tf_target_density=p["rho"], tf_modulation=p["mod"], tf_sigma=p["tfs"], tf_range=p["tfr"],
+                         tf_sample_interval=p["S"], tf_update_interval=p["U"], **kw)
+
+
+def replica(M, n, box, at, seed, center=None):
+    c = center if center is not None else [box[0] / 2, box[1] / 2, box[2] / 2]
+    return M.Replica(n, [0, 0, 0], box, c, at, seed)
+
+
+@pytest.mark.parametrize("graph", [0, 5])
+def test_single_replica_matches_oracle(M, orc, graph):
+    box = [36.0, 10.0, 10.0]
+    pos, vel = random_system(1800, box, 5)
+    steps = 13
+    po, vo, eo, fo, mo = oracle_loop(orc, pos, vel, box, steps, P)
+    b = batch(M, [replica(M, 1800, box, P["at"], P["seed"])], pos, vel, graph_steps=graph)
+    eg = b.run(steps)[:, 0]
+    pg, vg, _ = b.state()
+    # the compensation histogram is accumulated in 2^-32 fixed point and the
+    # Langevin noise goes through exp/log/cos/sin (host vs device ulps)
+    np.testing.assert_allclose(pg, po, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(vg, vo, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(eg, eo, rtol=1e-9)
+    fg, _ = b.thermodynamic_force()
+    np.testing.assert_allclose(fg[0], fo, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(b.compensation()[0], mo, rtol=1e-8, atol=1e-8)
+    st = b.stats()
+    assert st["steps"] == steps and st["rebuilds"] == 3 and st["ghost_molecules"] > 0
+    assert st["flags"] & 3 == 0
+
+
+def test_slab_reaching_into_the_ghost_layer_matches_oracle(M, orc):
+    """A box whose slab extends past the ghost layer: the weights of a pair
+    with a ghost differ between its two periodic instances, and the batch
+    must use the instance Cabana's half list keeps."""
+    box = [12.0, 9.0, 9.0]
+    p = dict(P, at=4.0, hy=5.0)
+    n = int(0.5 * 12 * 9 * 9)
+    pos, vel = random_system(n, box, 9)
+    steps = 11
+    po, vo, eo, fo, mo = oracle_loop(orc, pos, vel, box, steps, p)
+    for prec, tol, etol in ((M.PREC_FP64, 1e-9, 1e-9), (M.PREC_MIXED, 1e-6, 1e-5)):
+        b = batch(M, [replica(M, n, box, p["at"], p["seed"])], pos, vel, p=p, precision=prec)
+        eg = b.run(steps)[:, 0]
+        pg, vg, _ = b.state()
+        np.testing.assert_allclose(pg, po, rtol=0, atol=tol)
+        np.testing.assert_allclose(eg, eo, rtol=etol)
+
+
+def replica_set(M):
+    rng = np.random.default_rng(3)
+    reps, P_, V_ = [], [], []
+    specs = [(350, 4.5), (900, 9.0), (1700, 16.0), (2600, 24.0), (5200, 44.0)]
+    for k, (n, lx) in enumerate(specs):
+        box = [lx, 12.0, 12.0] if k % 2 else [lx, 14.0, 12.0]
+        at = float(rng.uniform(4.0, 14.0))
+        reps.append(replica(M, n, box, at, 1000 + k))
+        p, v = random_system(n, box, 40 + k)
+        P_.append(p)
+        V_.append(v)
+    return reps, np.concatenate(P_), np.concatenate(V_)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_replicas_bitwise_equal_alone(M, prec):
+    precision = M.PREC_FP64 if prec == "fp64" else M.PREC_MIXED
+    reps, pos, vel = replica_set(M)
+    tune = dict(threads_per_row=2, block_size=128, rebuild_interval=5, sort_every=2, graph_steps=10)
+    b = batch(M, reps, pos, vel, precision=precision, **tune)
+    steps = 23
+    eb = b.run(steps)
+    pb, vb, fb = b.state()
+    assert b.stats()["graph_launches"] == 2
+    for r, rep in enumerate(reps):
+        sl = b.replica_slice(r)
+        a = batch(M, [rep], pos[sl], vel[sl], precision=precision, **tune)
+        ea = a.run(steps)[:, 0]
+        pa, va, fa = a.state()
+        assert np.array_equal(pa, pb[sl]), f"replica {r} positions"
+        assert np.array_equal(va, vb[sl]), f"replica {r} velocities"
+        assert np.array_equal(fa, fb[sl]), f"replica {r} forces"
+        np.testing.assert_allclose(eb[:, r], ea, rtol=1e-11, atol=1e-9)
+        ta, _ = a.thermodynamic_force()
+        tb, _ = b.thermodynamic_force()
+        assert np.array_equal(ta[0], tb[r])
+
+
+def test_mixed_close_to_fp64(M):
+    reps, pos, vel = replica_set(M)
+    a = batch(M, reps, pos, vel, precision=M.PREC_FP64)
+    b = batch(M, reps, pos, vel, precision=M.PREC_MIXED)
+    # the first step's forces act on identical positions (the pre-force
+    # integration is FP64 in both forms)
+    a.run(1)
+    b.run(1)
+    pa, _, fa = a.state()
+    pb, _, fb = b.state()
+    assert np.array_equal(pa, pb)
+    rms = np.sqrt((fa ** 2).sum(axis=1).mean())
+    assert np.abs(fa - fb).max() / rms < 1e-6
+    a.run(5)
+    b.run(5)
+    pa, _, _ = a.state()
+    pb, _, _ = b.state()
+    assert np.abs(pa - pb).max() < 1e-7
+
+
+def test_capacity_overflow_recovery(M):
+    reps, pos, vel = replica_set(M)
+    tune = dict(rebuild_interval=5, sort_every=1, graph_steps=10)
+    a = batch(M, reps, pos, vel, **tune)
+    b = M.BatchSystem(reps, pos, vel, hybrid_diameter=P["hy"], rc=P["rc"], skin=P["skin"],
+                      capping_distance=P["cap"], dt=P["dt"], tf_sample_interval=P["S"], tf_update_interval=P["U"],
+                      threads_per_row=1, block_size=128, rebuild_interval=5, sort_every=1, graph_steps=10,
+                      initial_max_neighbors=6, initial_ghost_capacity=32)
+    a.run(20)
+    b.run(20)
+    assert b.stats()["recoveries"] >= 1
+    pa, va, _ = a.state()
+    pb, vb, _ = b.state()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_autotune_picks_a_candidate_and_keeps_the_state(M):
+    reps, pos, vel = replica_set(M)
+    b = batch(M, reps, pos, vel, rebuild_interval=5, sort_every=1, graph_steps=10)
+    b.run(10)
+    p0, v0, _ = b.state()
+    best, trials = b.autotune(trial_steps=10)
+    assert best in [t for t, _ in trials]
+    assert any(ms is not None for _, ms in trials)
+    p1, v1, _ = b.state()
+    assert np.array_equal(p0, p1) and np.array_equal(v0, v1)
+    assert b.stats()["steps"] == 10
+    b.run(20)
+    assert b.stats()["steps"] == 30
