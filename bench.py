@@ -422,7 +422,7 @@ def batch_main(args, rank, world, local_rank):
     ctx = M.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
     c = ADRESS
-    reps, pos, vel, geoms = batch_replicas(M)
+    reps, pos, vel, geoms = batch_replicas(M, args.replicas)
     n = len(pos)
     res = {}
     forces = {}
@@ -496,6 +496,7 @@ def main():
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--workload", choices=["lj", "adress", "batch"], default="lj")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
+    ap.add_argument("--replicas", type=int, default=None, help="batch workload: replica count (default 512)")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")

@@ -142,6 +142,7 @@ struct BDev
     RcSq rc2;
     double dt, zeta, temperature;
     double rlist, halfSkin;
+    double cgMargin;  // distance beyond the hybrid region that counts as staying coarse grained
     int64_t K, tfSampleInterval, tfUpdateInterval, compSampling, compUpdate;
     int32_t tfEnabled;
     double tfSigma, tfRange;
@@ -201,6 +202,7 @@ __global__ void k_b_pre(BDev B, int rebuild)
     if (tid < B.R) B.energyRing[(int64_t)(st % (unsigned long long)B.ring) * B.R + tid] = 0.0;
     double m2 = 0.0;
     const double dtHalf = 0.5 * B.dt;
+    OUCoef ou;
     for (int64_t i = tid; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
     {
         const RepDev& R = B.reps[B.slotRep[i]];
@@ -211,7 +213,8 @@ __global__ void k_b_pre(BDev B, int rebuild)
         drift(x, v, dtHalf);
         double g[3];
         normal3(R.seed, st, (uint64_t)(i - R.lbase), g);
-        ornstein_uhlenbeck(v, B.dt, m, B.zeta, B.temperature, g);
+        ou.update(m, B.dt, B.zeta, B.temperature);
+        ornstein_uhlenbeck(v, ou, g);
         drift(x, v, dtHalf);
         {
             // Verlet criterion: displacement since the list was built
@@ -452,6 +455,12 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
         const double4 pi = B.pos[i];
         const float xi = (float)(pi.x - R.gmn[0]), yi = (float)(pi.y - R.gmn[1]), zi = (float)(pi.z - R.gmn[2]);
         const uint32_t myImg = B.imgFlags[i];
+        // molecules that stay coarse grained (ideal gas) until the next rebuild
+        // interact with no other such molecule: their pairs are left out
+        const float deepCG = (float)(R.slab.atHalf + R.slab.hy + B.cgMargin);
+        const float cxRel = (float)(R.slab.cx - R.gmn[0]);
+        const bool prune = R.consistent != 0;
+        const bool rowCG = prune && fabsf(xi - cxRel) > deepCG;
         const int32_t ci = B.cellOf[i] - R.cellBase;
         const int cz = ci % R.gn[2];
         const int cy = (ci / R.gn[2]) % R.gn[1];
@@ -469,6 +478,7 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
                     const float4 q = B.spos[s];
                     const int32_t j = __float_as_int(q.w);
                     if (j == i) continue;
+                    if (rowCG && fabsf(q.x - cxRel) > deepCG) continue;
                     const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
                     const float d2f = dx * dx + dy * dy + dz * dz;
                     if (d2f > B.listRsqHi) continue;
@@ -528,28 +538,20 @@ __device__ __forceinline__ bool is_hy_df(float2 v)
     return !at && !(v.x <= 0.0f);
 }
 
-// double-float energy of a non-capped pair: u3 (r^-6) * (ef1 u3 - ef2) - shift
+// double-float pair energy: u3 (ef1 u3 - ef2) - shift with u3 = r^-6, or
+// inside the cap E(r_cap) - (r - r_cap) capCoeff - shift
 __device__ __forceinline__ df energy_df(const df& r2, const LJDev& p)
 {
     if (r2.h >= p.capSqrf)
     {
         const df u = df_rcp(r2);
         const df u3 = df_mul(df_sqr(u), u);
-        const float ef1h = (float)p.ef1, ef2h = (float)p.ef2, sh = (float)p.shift;
-        const df ef1 = {ef1h, (float)(p.ef1 - (double)ef1h)};
-        const df ef2 = {ef2h, (float)(p.ef2 - (double)ef2h)};
-        const df t = df_add(df_mul(ef1, u3), df{-ef2.h, -ef2.l});
-        return df_add(df_mul(u3, t), df{-sh, -(float)(p.shift - (double)sh)});
+        const df t = df_add(df_mul(df{p.ef1f, p.ef1l}, u3), df{-p.ef2f, -p.ef2l});
+        return df_add(df_mul(u3, t), df{-p.shiftf, -p.shiftl});
     }
-    // capped: E(r_cap) - (r - r_cap) capCoeff - shift, r = sqrt(r2) to double-float
-    float s = sqrtf(r2.h);
-    const float res = __fmaf_rn(-s, s, r2.h) + r2.l;
-    const df dist = fast_two_sum(s, res / (2.0f * s));
-    const df t = df_add(dist, df{-(float)p.capDist, -(float)(p.capDist - (double)(float)p.capDist)});
-    const float cch = (float)p.capCoeff;
-    const df lin = df_mul(t, df{cch, (float)(p.capCoeff - (double)cch)});
-    const float eh = (float)(p.eCap - p.shift);
-    return df_add(df{eh, (float)((p.eCap - p.shift) - (double)eh)}, df{-lin.h, -lin.l});
+    const df t = df_add(df_sqrt(r2), df{-p.capDistf, -p.capDistl});
+    const df lin = df_mul(t, df{p.capCoeff_f, p.capCoeff_l});
+    return df_add(df{p.eCapShh, p.eCapShl}, df{-lin.h, -lin.l});
 }
 
 struct RowOut
@@ -597,17 +599,6 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             partModF = B.lamtf[j];
         else
             partMod = B.lamt[j];
-        double4 pj = make_double4(0.0, 0.0, 0.0, 0.0);
-        float4 hj, lj;
-        if (MIXED)
-        {
-            hj = B.hi[j];
-            lj = B.lo[j];
-        }
-        else
-        {
-            pj = B.pos[j];
-        }
         if (rev && !R.consistent)
         {
             // the pair acts with the weights of (source, image of i)
@@ -630,6 +621,7 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             const float2 ownF =
                 ownIsSelf ? ltA : make_float2((float)ownMod, (float)(ownMod - (double)(float)ownMod));
             if (ownF.x <= 0.0f && partModF.x <= 0.0f) continue;  // both coarse grained: ideal gas
+            const float4 hj = B.hi[j], lj = B.lo[j];
             PairMixed q;
             if (!pair_mixed(hi_i, lo_i, hj, lj, B.lj, B.rc2, q)) continue;
             const bool hyPair = is_hy_df(ownF) || is_hy_df(partModF);
@@ -674,6 +666,7 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
         else
         {
             if (ownMod <= 0.0 && partMod <= 0.0) continue;  // both coarse grained: ideal gas
+            const double4 pj = B.pos[j];
             const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const double distSqr = dx * dx + dy * dy + dz * dz;
             if (distSqr > B.rcSqr) continue;
@@ -1435,6 +1428,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     B.temperature = cfg->temperature;
     B.rlist = rlist;
     B.halfSkin = 0.5 * cfg->skin;
+    B.cgMargin = cfg->skin + 1e-3;  // twice the skin/2 a molecule may move between rebuilds
     B.K = cfg->tuning.rebuildInterval;
     B.tfEnabled = cfg->tfEnabled;
     B.tfSampleInterval = cfg->tfEnabled ? cfg->tfSampleInterval : 1;

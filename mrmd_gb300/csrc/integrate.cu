@@ -41,6 +41,7 @@ __global__ void k_langevin_pre(double4* __restrict__ pos, double4* __restrict__ 
 {
     // action/VelocityVerletLangevinThermostat.hpp:64-113
     double m2 = 0.0;
+    OUCoef ou;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
@@ -54,7 +55,8 @@ __global__ void k_langevin_pre(double4* __restrict__ pos, double4* __restrict__ 
         {
             double g[3];
             normal3(seed, step, (uint64_t)i, g);
-            ornstein_uhlenbeck(v, dt, m, zeta, temperature, g);
+            ou.update(m, dt, zeta, temperature);
+            ornstein_uhlenbeck(v, ou, g);
         }
         drift(x, v, dtHalf);
         pos[i] = x;

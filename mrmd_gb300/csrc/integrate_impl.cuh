@@ -65,37 +65,96 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
     }
 }
 
-// Three standard normals for (seed, step, atom): Philox block -> four
-// uniforms in (0,1) -> two Box-Muller pairs.
+// Standard normals from a Philox block by Box-Muller in FP32 (the thermostat
+// needs statistics, not digits).  ln and sin/cos are our own: a reduction to
+// a mantissa in [sqrt(1/2), sqrt(2)] with the series 2 atanh(t), t = (m-1)/(m+1),
+// and a quarter-turn reduction of the angle with Taylor polynomials on
+// [-pi/4, pi/4].  Every operation is a correctly rounded FP32 add, multiply,
+// divide, square root or FMA, so the host restatement computes the same bits.
+__device__ __forceinline__ float bm_log(float u)  // u in (0, 1)
+{
+    const int bits = __float_as_int(u);
+    int e = ((bits >> 23) & 0xff) - 127;
+    float m = __int_as_float((bits & 0x7fffff) | 0x3f800000);  // [1, 2)
+    if (m > 0x1.6a09e6p+0f)
+    {
+        m = __fmul_rn(m, 0.5f);
+        e += 1;
+    }
+    const float t = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float t2 = __fmul_rn(t, t);
+    float p = __fmaf_rn(t2, 0x1.c71c72p-4f, 0x1.24924ap-3f);  // 1/9, 1/7
+    p = __fmaf_rn(p, t2, 0x1.99999ap-3f);                      // 1/5
+    p = __fmaf_rn(p, t2, 0x1.555556p-2f);                      // 1/3
+    p = __fmaf_rn(p, t2, 1.0f);
+    return __fmaf_rn((float)e, 0x1.62e430p-1f, __fmul_rn(2.0f, __fmul_rn(t, p)));  // e ln2 + 2 atanh(t)
+}
+
+// cos and sin of 2 pi u, u in (0, 1)
+__device__ __forceinline__ void bm_sincos(float u, float& c, float& s)
+{
+    const float q = rintf(__fmul_rn(4.0f, u));
+    const float x = __fsub_rn(u, __fmul_rn(0.25f, q));  // exact, |x| <= 1/8
+    const float f = __fmul_rn(x, 0x1.921fb6p+2f);        // 2 pi x, |f| <= pi/4
+    const float f2 = __fmul_rn(f, f);
+    float ps = __fmaf_rn(f2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+    ps = __fmaf_rn(ps, f2, 0x1.111112p-7f);
+    ps = __fmaf_rn(ps, f2, -0x1.555556p-3f);
+    const float sn = __fmaf_rn(__fmul_rn(f, f2), ps, f);
+    float pc = __fmaf_rn(f2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+    pc = __fmaf_rn(pc, f2, -0x1.6c16c2p-10f);
+    pc = __fmaf_rn(pc, f2, 0x1.555556p-5f);
+    pc = __fmaf_rn(pc, f2, -0.5f);
+    const float cs = __fmaf_rn(pc, f2, 1.0f);
+    const int quadrant = ((int)q) & 3;  // angle = f + quadrant * pi/2
+    c = quadrant == 0 ? cs : (quadrant == 1 ? -sn : (quadrant == 2 ? -cs : sn));
+    s = quadrant == 0 ? sn : (quadrant == 1 ? cs : (quadrant == 2 ? -sn : -cs));
+}
+
+// Three standard normals for (seed, step, atom): one Philox block -> four
+// 23-bit uniforms in (0, 1) -> two Box-Muller pairs (the third value of the
+// second pair is unused).
 __device__ __forceinline__ void normal3(uint64_t seed, uint64_t step, uint64_t atom, double g[3])
 {
     uint32_t c[4] = {(uint32_t)atom, (uint32_t)(atom >> 32), (uint32_t)step, (uint32_t)(step >> 32)};
     philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    const double s = 2.3283064365386963e-10;  // 2^-32
-    const double u0 = ((double)c[0] + 0.5) * s;
-    const double u1 = ((double)c[1] + 0.5) * s;
-    const double u2 = ((double)c[2] + 0.5) * s;
-    const double u3 = ((double)c[3] + 0.5) * s;
-    const double twoPi = 6.283185307179586;
-    const double ra = sqrt(-2.0 * log(u0));
-    const double rb = sqrt(-2.0 * log(u2));
-    g[0] = ra * cos(twoPi * u1);
-    g[1] = ra * sin(twoPi * u1);
-    g[2] = rb * cos(twoPi * u3);
+    float u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = __fmul_rn(__fadd_rn((float)(c[k] >> 9), 0.5f), 0x1p-23f);
+    const float ra = __fsqrt_rn(__fmul_rn(-2.0f, bm_log(u[0])));
+    const float rb = __fsqrt_rn(__fmul_rn(-2.0f, bm_log(u[2])));
+    float ca, sa, cb, sb;
+    bm_sincos(u[1], ca, sa);
+    bm_sincos(u[3], cb, sb);
+    g[0] = (double)__fmul_rn(ra, ca);
+    g[1] = (double)__fmul_rn(ra, sa);
+    g[2] = (double)__fmul_rn(rb, cb);
 }
 
-// updateOrnsteinUhlenbeck (UpdateSteps.hpp:56-79)
-__device__ __forceinline__ void ornstein_uhlenbeck(double4& v, double dt, double m, double zeta, double T,
-                                                   const double g[3])
+// Ornstein-Uhlenbeck coefficients of one mass (UpdateSteps.hpp:56-79):
+// damping = exp(-zeta dt / m), sigma = sqrt(T / m (1 - exp(-2 zeta dt / m))).
+struct OUCoef
 {
-    const double dtm = __ddiv_rn(dt, m);
-    const double damping = exp(-zeta * dtm);
-    const double sigma = sqrt(T / m * (1.0 - exp(-2.0 * zeta * dtm)));
-    v.x = __dmul_rn(v.x, damping);
-    v.y = __dmul_rn(v.y, damping);
-    v.z = __dmul_rn(v.z, damping);
-    v.x = __dadd_rn(v.x, __dmul_rn(sigma, g[0]));
-    v.y = __dadd_rn(v.y, __dmul_rn(sigma, g[1]));
-    v.z = __dadd_rn(v.z, __dmul_rn(sigma, g[2]));
+    double m = -1.0, damping = 0.0, sigma = 0.0;
+
+    __device__ __forceinline__ void update(double mass, double dt, double zeta, double T)
+    {
+        if (mass == m) return;  // uniform masses: computed once per thread
+        const double dtm = __ddiv_rn(dt, mass);
+        damping = exp(-zeta * dtm);
+        sigma = sqrt(T / mass * (1.0 - exp(-2.0 * zeta * dtm)));
+        m = mass;
+    }
+};
+
+__device__ __forceinline__ void ornstein_uhlenbeck(double4& v, const OUCoef& k, const double g[3])
+{
+    v.x = __dmul_rn(v.x, k.damping);
+    v.y = __dmul_rn(v.y, k.damping);
+    v.z = __dmul_rn(v.z, k.damping);
+    v.x = __dadd_rn(v.x, __dmul_rn(k.sigma, g[0]));
+    v.y = __dadd_rn(v.y, __dmul_rn(k.sigma, g[1]));
+    v.z = __dadd_rn(v.z, __dmul_rn(k.sigma, g[2]));
 }
+
 }  // namespace mrmd_impl

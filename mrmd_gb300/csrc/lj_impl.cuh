@@ -17,6 +17,10 @@ struct LJDev
     float ff1h, ff1l, ff2h, ff2l;  // ff1 = ff1h + ff1l exactly to ~2^-48
     float ef1f, ef2f, shiftf, rcSqrf;
     float capSqrf, capCoeff_f, eCapf, capDistf;
+    float capCoeff_l;  // capCoeff = capCoeff_f + capCoeff_l to ~2^-48
+    // low parts of the energy factors (double-float energies of the mixed form)
+    float ef1l, ef2l, shiftl, capDistl;
+    float eCapShh, eCapShl;  // E(r_cap) - shift
 };
 
 inline LJDev to_dev(const mrmd_lj_params& p)
@@ -44,6 +48,15 @@ inline LJDev to_dev(const mrmd_lj_params& p)
     d.capCoeff_f = (float)p.cappingCoeff;
     d.eCapf = (float)p.energyAtCappingPoint;
     d.capDistf = (float)p.cappingDistance;
+    // low parts: each (hi, lo) pair holds the double to ~2^-48
+    d.capCoeff_l = (float)(p.cappingCoeff - (double)d.capCoeff_f);
+    d.ef1l = (float)(p.ef1 - (double)d.ef1f);
+    d.ef2l = (float)(p.ef2 - (double)d.ef2f);
+    d.shiftl = (float)(p.shift - (double)d.shiftf);
+    d.capDistl = (float)(p.cappingDistance - (double)d.capDistf);
+    const double ecs = p.energyAtCappingPoint - p.shift;
+    d.eCapShh = (float)ecs;
+    d.eCapShl = (float)(ecs - (double)d.eCapShh);
     return d;
 }
 
@@ -121,6 +134,14 @@ __device__ __forceinline__ df df_rcp(df a)
     float r = __fmaf_rn(-a.h, y, 1.0f);
     r = __fmaf_rn(-a.l, y, r);
     return fast_two_sum(y, y * r);
+}
+
+// sqrt(a) with one Newton correction on the exact FMA residual
+__device__ __forceinline__ df df_sqrt(df a)
+{
+    const float s = sqrtf(a.h);
+    const float r = __fmaf_rn(-s, s, a.h) + a.l;
+    return fast_two_sum(s, r / (2.0f * s));
 }
 
 // compensated accumulator (TwoSum), ~2^-48 relative to the final sum

@@ -75,9 +75,11 @@ __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_
     const float r2f = __fmaf_rn(fx, fx, __fmaf_rn(fy, fy, fz * fz));
     if (r2f > rc2.h * 1.0000005f) return false;
     // r^2 = sum (dh + dl)^2 as double-float: exact squares of the heads
-    // (FMA TwoProd), the 2*dh*dl cross terms in the low part
+    // (FMA TwoProd), the 2*dh*dl cross terms and dl^2 in the low part (dl^2
+    // matters for close contacts, where |dl| is not small against |dh|)
     const float px = o.dh.x * o.dh.x, py = o.dh.y * o.dh.y, pz = o.dh.z * o.dh.z;
-    float lo = __fmaf_rn(o.dh.x, o.dh.x, -px);
+    float lo = __fmaf_rn(o.dl.x, o.dl.x, __fmaf_rn(o.dl.y, o.dl.y, o.dl.z * o.dl.z));
+    lo += __fmaf_rn(o.dh.x, o.dh.x, -px);
     lo += __fmaf_rn(o.dh.y, o.dh.y, -py);
     lo += __fmaf_rn(o.dh.z, o.dh.z, -pz);
     lo = __fmaf_rn(2.0f * o.dh.x, o.dl.x, lo);
@@ -101,11 +103,12 @@ __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_
     }
     else
     {
-        // capped branch (action/LennardJones.hpp:70-77): |F| constant, no
-        // amplification of the r^2 error
-        const float dist = sqrtf(r2.h);
-        o.ff = df{p.capCoeff_f / dist, 0.0f};
-        o.e = p.eCapf - (dist - p.capDistf) * p.capCoeff_f - p.shiftf;
+        // capped branch (action/LennardJones.hpp:70-77): |F| = capCoeff is
+        // constant, so forceFactor = capCoeff / r carries the relative error
+        // of r straight into the force: r and 1/r as double-floats
+        const df dist = df_sqrt(r2);
+        o.ff = df_mul(df{p.capCoeff_f, p.capCoeff_l}, df_rcp(dist));
+        o.e = p.eCapf - (dist.h - p.capDistf) * p.capCoeff_f - p.shiftf;
     }
     return true;
 }

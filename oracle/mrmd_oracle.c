@@ -602,6 +602,54 @@ void orc_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out)
     out[3] = c3;
 }
 
+/* Box-Muller in FP32 with our own ln and sin/cos (the GPU's normal3 in
+ * mrmd_gb300/csrc/integrate_impl.cuh, operation for operation): ln(u) =
+ * e ln2 + 2 atanh(t), t = (m-1)/(m+1), m in [sqrt(1/2), sqrt(2)]; sin/cos of
+ * 2 pi u by a quarter-turn reduction and Taylor polynomials on [-pi/4, pi/4].
+ * Every step is a correctly rounded float operation or fmaf, so host and
+ * device agree bit for bit (the file is built with -ffp-contract=off). */
+static float bm_log(float u)
+{
+    uint32_t bits;
+    memcpy(&bits, &u, sizeof bits);
+    int e = (int)((bits >> 23) & 0xffu) - 127;
+    uint32_t mb = (bits & 0x7fffffu) | 0x3f800000u;
+    float m;
+    memcpy(&m, &mb, sizeof m);
+    if (m > 0x1.6a09e6p+0f)
+    {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float t = (m - 1.0f) / (m + 1.0f);
+    const float t2 = t * t;
+    float p = fmaf(t2, 0x1.c71c72p-4f, 0x1.24924ap-3f);
+    p = fmaf(p, t2, 0x1.99999ap-3f);
+    p = fmaf(p, t2, 0x1.555556p-2f);
+    p = fmaf(p, t2, 1.0f);
+    return fmaf((float)e, 0x1.62e430p-1f, 2.0f * (t * p));
+}
+
+static void bm_sincos(float u, float* c, float* s)
+{
+    const float q = rintf(4.0f * u);
+    const float x = u - 0.25f * q;
+    const float f = x * 0x1.921fb6p+2f;
+    const float f2 = f * f;
+    float ps = fmaf(f2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+    ps = fmaf(ps, f2, 0x1.111112p-7f);
+    ps = fmaf(ps, f2, -0x1.555556p-3f);
+    const float sn = fmaf(f * f2, ps, f);
+    float pc = fmaf(f2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+    pc = fmaf(pc, f2, -0x1.6c16c2p-10f);
+    pc = fmaf(pc, f2, 0x1.555556p-5f);
+    pc = fmaf(pc, f2, -0.5f);
+    const float cs = fmaf(pc, f2, 1.0f);
+    const int quadrant = ((int)q) & 3;
+    *c = quadrant == 0 ? cs : (quadrant == 1 ? -sn : (quadrant == 2 ? -cs : sn));
+    *s = quadrant == 0 ? sn : (quadrant == 1 ? cs : (quadrant == 2 ? -sn : -cs));
+}
+
 void orc_normal_from_counter(uint64_t seed, uint64_t step, uint64_t atom, double* out3)
 {
     uint32_t ctr[4] = {(uint32_t)atom, (uint32_t)(atom >> 32), (uint32_t)step,
@@ -609,18 +657,17 @@ void orc_normal_from_counter(uint64_t seed, uint64_t step, uint64_t atom, double
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     uint32_t r[4];
     orc_philox4x32_10(ctr, key, r);
-    /* uniforms in (0,1) from 32-bit words, then two Box-Muller pairs */
-    const double s = 2.3283064365386963e-10; /* 2^-32 */
-    double u0 = ((double)r[0] + 0.5) * s;
-    double u1 = ((double)r[1] + 0.5) * s;
-    double u2 = ((double)r[2] + 0.5) * s;
-    double u3 = ((double)r[3] + 0.5) * s;
-    const double twoPi = 6.283185307179586;
-    double ra = sqrt(-2.0 * log(u0));
-    double rb = sqrt(-2.0 * log(u2));
-    out3[0] = ra * cos(twoPi * u1);
-    out3[1] = ra * sin(twoPi * u1);
-    out3[2] = rb * cos(twoPi * u3);
+    /* 23-bit uniforms in (0,1), then two Box-Muller pairs */
+    float u[4];
+    for (int k = 0; k < 4; ++k) u[k] = ((float)(r[k] >> 9) + 0.5f) * 0x1p-23f;
+    const float ra = sqrtf(-2.0f * bm_log(u[0]));
+    const float rb = sqrtf(-2.0f * bm_log(u[2]));
+    float ca, sa, cb, sb;
+    bm_sincos(u[1], &ca, &sa);
+    bm_sincos(u[3], &cb, &sb);
+    out3[0] = (double)(ra * ca);
+    out3[1] = (double)(ra * sa);
+    out3[2] = (double)(rb * cb);
 }
 
 double orc_langevin_pre(orc_atoms* a, double dt, double zeta, double temperature, uint64_t seed,
