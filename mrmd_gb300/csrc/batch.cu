@@ -84,7 +84,22 @@ struct Scalars
     uint32_t overflow;          // ghost / list overflow of the rebuilds since the host cleared it
     uint32_t flags;             // sticky: a molecule moved skin/2 between rebuilds
     uint32_t done;              // tail-kernel block ticket
+    // decisions of the current step, set once per step (64-bit modulos are
+    // long instruction sequences; no per-thread kernel repeats them)
+    int32_t ringSlot;           // step % ring
+    int32_t sampleComp;         // run % compensation sampling interval == 0
+    int32_t sampleTf;           // TF enabled and step % TF sampling interval == 0
 };
+
+// the step decisions of (step, run)
+__host__ __device__ inline void set_step_flags(Scalars& s, unsigned long long step, unsigned long long run,
+                                               int32_t ring, int64_t compSampling, int32_t tfEnabled,
+                                               int64_t tfSampleInterval)
+{
+    s.ringSlot = (int32_t)(step % (unsigned long long)ring);
+    s.sampleComp = (run % (unsigned long long)compSampling) == 0;
+    s.sampleTf = tfEnabled && (step % (unsigned long long)tfSampleInterval) == 0;
+}
 
 // Everything the kernels read: pointers and run constants.
 struct BDev
@@ -103,6 +118,7 @@ struct BDev
     uint8_t* gShift;   // [gCap] 2 bits per axis: 1 = +L, 2 = -L
     uint8_t* imgFlags; // [N] bit 2d: has a +L image on axis d, bit 2d+1: has a -L image
     float4* ref;       // [N] position at the last rebuild, relative to the replica's grid origin
+    int2* xImg;        // [N] slots of the ghost images shifted by -L / +L in x only (-1: none)
     int32_t* gCount;   // [N + 1] images per local, then exclusive offsets
     double4* lam;      // [N + gCap] (lambda, modulated lambda, grad lambda x, 0)
     double* lamt;      // [N + gCap] modulated lambda
@@ -141,6 +157,8 @@ struct BDev
     double rcSqr;
     RcSq rc2;
     double dt, zeta, temperature;
+    double dtHalfOverMass;  // dt/2 / m (molecules have unit mass)
+    double ouDamping, ouSigma;  // Ornstein-Uhlenbeck coefficients of the unit mass (UpdateSteps.hpp:56-79)
     double rlist, halfSkin;
     double cgMargin;  // distance beyond the hybrid region that counts as staying coarse grained
     int64_t K, tfSampleInterval, tfUpdateInterval, compSampling, compUpdate;
@@ -160,6 +178,22 @@ __device__ __forceinline__ void set_coord(double4& p, int d, double v)
         p.y = v;
     else
         p.z = v;
+}
+
+// velocity-Verlet kick and drift with fused multiply-adds (the reference's
+// v += dt/2m F and x += dt v, each rounded once)
+__device__ __forceinline__ void kick_fma(double4& v, const double4& f, double dtfm)
+{
+    v.x = fma(dtfm, f.x, v.x);
+    v.y = fma(dtfm, f.y, v.y);
+    v.z = fma(dtfm, f.z, v.z);
+}
+
+__device__ __forceinline__ void drift_fma(double4& x, const double4& v, double dt)
+{
+    x.x = fma(dt, v.x, x.x);
+    x.y = fma(dt, v.y, x.y);
+    x.z = fma(dt, v.z, x.z);
 }
 
 // lambda, modulated lambda and grad lambda (x) of one slot, plus the mixed
@@ -199,23 +233,24 @@ __global__ void k_b_pre(BDev B, int rebuild)
 {
     const unsigned long long st = B.sc->step;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (tid < B.R) B.energyRing[(int64_t)(st % (unsigned long long)B.ring) * B.R + tid] = 0.0;
+    if (tid < B.R) B.energyRing[(int64_t)B.sc->ringSlot * B.R + tid] = 0.0;
     double m2 = 0.0;
     const double dtHalf = 0.5 * B.dt;
-    OUCoef ou;
     for (int64_t i = tid; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
     {
         const RepDev& R = B.reps[B.slotRep[i]];
         double4 x = B.pos[i], v = B.vel[i];
         const double4 f = B.force[i];
         const double m = B.mass[i];
-        kick(v, f, __ddiv_rn(dtHalf, m));
-        drift(x, v, dtHalf);
+        (void)m;  // unit masses: dt/2m and the OU coefficients are constants
+        kick_fma(v, f, B.dtHalfOverMass);
+        drift_fma(x, v, dtHalf);
         double g[3];
         normal3(R.seed, st, (uint64_t)(i - R.lbase), g);
-        ou.update(m, B.dt, B.zeta, B.temperature);
-        ornstein_uhlenbeck(v, ou, g);
-        drift(x, v, dtHalf);
+        v.x = fma(B.ouSigma, g[0], v.x * B.ouDamping);
+        v.y = fma(B.ouSigma, g[1], v.y * B.ouDamping);
+        v.z = fma(B.ouSigma, g[2], v.z * B.ouDamping);
+        drift_fma(x, v, dtHalf);
         {
             // Verlet criterion: displacement since the list was built
             const float4 r0 = B.ref[i];
@@ -356,6 +391,7 @@ __global__ void k_b_ghost_count(BDev B)
         }
         B.imgFlags[i] = (uint8_t)flags;
         B.gCount[i] = n - 1;
+        B.xImg[i] = make_int2(-1, -1);
         B.ref[i] = make_float4((float)(x.x - R.gmn[0]), (float)(x.y - R.gmn[1]), (float)(x.z - R.gmn[2]), 0.0f);
     }
 }
@@ -370,6 +406,7 @@ __global__ void k_b_ghost_write(BDev B)
         const uint32_t flags = B.imgFlags[i];
         const double4 x = B.pos[i];
         int32_t k = B.gCount[i];  // exclusive offset
+        int2 xImg = make_int2(-1, -1);
         // options per axis: 0 (no shift), 2 (-L) if x >= maxInner, 1 (+L) if x < minInner
         for (int ox = 0; ox < 3; ++ox)
         {
@@ -405,9 +442,15 @@ __global__ void k_b_ghost_write(BDev B)
                     B.gSrc[g] = i;
                     B.gShift[g] = (uint8_t)(cx | (cy << 2) | (cz << 4));
                     slot_derived<MIXED>(B, R, s, p);
+                    if (!cy && !cz)
+                    {
+                        if (cx == 2) xImg.x = (int32_t)s;
+                        if (cx == 1) xImg.y = (int32_t)s;
+                    }
                 }
             }
         }
+        B.xImg[i] = xImg;
     }
 }
 
@@ -554,13 +597,39 @@ __device__ __forceinline__ df energy_df(const df& r2, const LJDev& p)
     return df_add(df{p.eCapShh, p.eCapShl}, df{-lin.h, -lin.l});
 }
 
+// x of i's image: side 1 = x - L, side 2 = x + L
+__device__ __forceinline__ double image_x(double x, const RepDev& R, int side)
+{
+    return side == 1 ? __dsub_rn(x, R.L[0]) : __dadd_rn(x, R.L[0]);
+}
+
+// weights of i's image in x (side 1: -L, side 2: +L): those of i's ghost
+// with that pure x shift (lambda depends on x only)
+__device__ __forceinline__ void image_weights(const BDev& B, const RepDev& R, int32_t i, int side, double& l,
+                                              double& m, double& g)
+{
+    const int2 xi = B.xImg[i];
+    const int32_t slot = side == 1 ? xi.x : xi.y;
+    if (slot >= 0)
+    {
+        const double4 w = B.lam[slot];
+        l = w.x;
+        m = w.y;
+        g = w.z;
+        return;
+    }
+    slab_eval(R.slab, image_x(B.pos[i].x, R, side), l, m, g);
+}
+
 struct RowOut
 {
     double fx, fy, fz;  // pair force on the molecule
     double vsum;        // sum of V_ij of pairs with a hybrid member, own slot = the molecule itself
     double comp;        // the same, only pairs whose own slot is hybrid with a valid bin
-    double imgFx;       // drift force from pairs whose own slot is an image of the molecule
-    double energy;      // sum of e w over the row (each pair is seen from both sides)
+    double imgFx;       // drift force from pairs whose own slot is an image of the molecule (FP64 form)
+    double vImgM, vImgP;  // mixed form: V_ij sums of those pairs per image (-L, +L in x)
+    double energy;      // sum of e w over the row (each pair is seen from both sides), FP64 form
+    float fenergy;      // the same in the mixed form (FP32 pair energies)
 };
 
 // One row (local molecule i), lanes `sub` of TPR.  Returns this lane's
@@ -578,7 +647,20 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
         lo_i = B.lo[i];
     }
     const float2 ltA = MIXED ? B.lamtf[i] : make_float2(0.f, 0.f);
+    // weights of i's images in x (replicas whose slab reaches the ghost layer)
+    int2 xImg = make_int2(-1, -1);
+    float2 imgFM = ltA, imgFP = ltA;
+    if (!R.consistent)
+    {
+        xImg = B.xImg[i];
+        if (MIXED)
+        {
+            if (xImg.x >= 0) imgFM = B.lamtf[xImg.x];
+            if (xImg.y >= 0) imgFP = B.lamtf[xImg.y];
+        }
+    }
     df fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, vs{0.f, 0.f}, cs{0.f, 0.f};
+    df vImgM{0.f, 0.f}, vImgP{0.f, 0.f};  // mixed form: V_ij sums of pairs acting through i's -L / +L image
     double dfx = 0.0, dfy = 0.0, dfz = 0.0, dvs = 0.0, dcs = 0.0;
     double imgFx = 0.0, energy = 0.0;
     float fenergy = 0.0f;
@@ -599,27 +681,56 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             partModF = B.lamtf[j];
         else
             partMod = B.lamt[j];
+        float2 ownImgF = ltA;
+        int imgSide = 0;  // mixed form: 1 / 2 when the own slot is i's -L / +L image in x
         if (rev && !R.consistent)
         {
-            // the pair acts with the weights of (source, image of i)
+            // the pair acts with the weights of (source, image of i): the
+            // image's weights are those of i's ghost with the opposite shift
             const int32_t g = j - B.N;
             const int32_t src = B.gSrc[g];
             if (MIXED)
                 partModF = B.lamtf[src];
             else
                 partMod = B.lamt[src];
-            const uint32_t cx = B.gShift[g] & 3u;
-            if (cx != 0)
+            const uint32_t code = B.gShift[g];
+            if (code & 3u)
             {
-                const double xi = cx == 1 ? __dsub_rn(pi.x, R.L[0]) : __dadd_rn(pi.x, R.L[0]);
-                slab_eval(R.slab, xi, ownLam, ownMod, ownGx);
+                // the own slot is i's image with the opposite x shift
+                const int side = (code & 3u) == 1 ? 1 : 2;
+                const int32_t slot = side == 1 ? xImg.x : xImg.y;
+                if (MIXED)
+                {
+                    // double work stays out of the pair loop: the image's
+                    // drift term is summed per image and applied per row
+                    imgSide = side;
+                    if (slot >= 0)
+                    {
+                        ownImgF = side == 1 ? imgFM : imgFP;
+                    }
+                    else
+                    {
+                        slab_eval(R.slab, image_x(pi.x, R, side), ownLam, ownMod, ownGx);
+                        ownImgF = make_float2((float)ownMod, (float)(ownMod - (double)(float)ownMod));
+                    }
+                }
+                else if (slot >= 0)
+                {
+                    const double4 li = B.lam[slot];
+                    ownLam = li.x;
+                    ownMod = li.y;
+                    ownGx = li.z;
+                }
+                else
+                {
+                    slab_eval(R.slab, image_x(pi.x, R, side), ownLam, ownMod, ownGx);
+                }
                 ownIsSelf = false;
             }
         }
         if (MIXED)
         {
-            const float2 ownF =
-                ownIsSelf ? ltA : make_float2((float)ownMod, (float)(ownMod - (double)(float)ownMod));
+            const float2 ownF = ownImgF;
             if (ownF.x <= 0.0f && partModF.x <= 0.0f) continue;  // both coarse grained: ideal gas
             const float4 hj = B.hi[j], lj = B.lo[j];
             PairMixed q;
@@ -648,17 +759,13 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
                     vs = df_add(vs, V);
                     if (sampling && binAlpha != -1) cs = df_add(cs, V);
                 }
+                else if (imgSide == 1)
+                {
+                    vImgM = df_add(vImgM, V);  // drift and sampling of the image: per row, below
+                }
                 else
                 {
-                    const double Vd = to_d(V);
-                    imgFx += -Vd * ownGx;
-                    if (sampling && is_hy(ownMod))
-                    {
-                        const int b = comp_bin(ownLam);
-                        if (b != -1)
-                            atomicAdd(reinterpret_cast<unsigned long long*>(B.compEnergy + B.slotRep[i] * COMP_BINS + b),
-                                      (unsigned long long)llrint(Vd * COMP_SCALE));
-                    }
+                    vImgP = df_add(vImgP, V);
                 }
             }
             fenergy = __fmaf_rn(q.e, bothAT ? 1.0f : 0.5f * (ownF.x + partModF.x), fenergy);
@@ -713,13 +820,16 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             fz = df_add(fz, df_shfl_xor(fz, off));
             vs = df_add(vs, df_shfl_xor(vs, off));
             cs = df_add(cs, df_shfl_xor(cs, off));
+            vImgM = df_add(vImgM, df_shfl_xor(vImgM, off));
+            vImgP = df_add(vImgP, df_shfl_xor(vImgP, off));
         }
+        o.vImgM = to_d(vImgM);
+        o.vImgP = to_d(vImgP);
         o.fx = to_d(fx);
         o.fy = to_d(fy);
         o.fz = to_d(fz);
         o.vsum = to_d(vs);
-        o.comp = to_d(cs);
-        energy = (double)fenergy;
+        o.comp = sampling ? to_d(cs) : 0.0;
     }
     else
     {
@@ -737,15 +847,21 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
         o.fz = dfz;
         o.vsum = dvs;
         o.comp = dcs;
+        o.vImgM = 0.0;
+        o.vImgP = 0.0;
     }
 #pragma unroll
     for (int off = 1; off < TPR; off <<= 1)
     {
         imgFx += __shfl_xor_sync(0xffffffffu, imgFx, off);
-        energy += __shfl_xor_sync(0xffffffffu, energy, off);
+        if (MIXED)
+            fenergy += __shfl_xor_sync(0xffffffffu, fenergy, off);
+        else
+            energy += __shfl_xor_sync(0xffffffffu, energy, off);
     }
     o.imgFx = imgFx;
     o.energy = energy;
+    o.fenergy = fenergy;
     return o;
 }
 
@@ -756,16 +872,13 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
 template <bool MIXED, int TPR>
 __global__ void k_b_force(BDev B)
 {
-    const unsigned long long st = B.sc->step;
-    const unsigned long long run = B.sc->run;
-    const bool sampling = (run % (unsigned long long)B.compSampling) == 0;
-    const bool tfSample = B.tfEnabled && (st % (unsigned long long)B.tfSampleInterval) == 0;
+    const bool sampling = B.sc->sampleComp != 0;
+    const bool tfSample = B.sc->sampleTf != 0;
     const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int32_t i = (int32_t)(gtid / TPR);
     const int sub = (int)(gtid % TPR);
     const bool valid = i < B.N;
     RowOut o = row_force<MIXED, TPR>(B, valid ? i : 0, sub, sampling && valid);
-    if (!valid) o.energy = 0.0;
     int32_t r = valid ? B.slotRep[i] : -1;
     if (valid && sub == 0)
     {
@@ -773,6 +886,27 @@ __global__ void k_b_force(BDev B)
         const double4 la = B.lam[i];
         // molecule force: drift (-V_ij grad lambda) and compensation
         double fmx = -o.vsum * la.z + o.imgFx;
+        if (MIXED && (o.vImgM != 0.0 || o.vImgP != 0.0))
+        {
+            // pairs acting through i's images: drift force -V grad lambda of the
+            // image and, on sampling runs, V into the image's compensation bin
+#pragma unroll
+            for (int side = 1; side <= 2; ++side)
+            {
+                const double v = side == 1 ? o.vImgM : o.vImgP;
+                if (v == 0.0) continue;
+                double l, m, g;
+                image_weights(B, R, i, side, l, m, g);
+                fmx += -v * g;
+                if (sampling && is_hy(m))
+                {
+                    const int b = comp_bin(l);
+                    if (b != -1)
+                        atomicAdd(reinterpret_cast<unsigned long long*>(B.compEnergy + r * COMP_BINS + b),
+                                  (unsigned long long)llrint(v * COMP_SCALE));
+                }
+            }
+        }
         if (is_hy(la.y))
         {
             const int b = comp_bin(la.x);
@@ -800,23 +934,41 @@ __global__ void k_b_force(BDev B)
             }
         }
         double4 v = B.vel[i];
-        kick(v, f, __ddiv_rn(0.5 * B.dt, B.mass[i]));
+        kick_fma(v, f, B.dtHalfOverMass);
         B.vel[i] = v;
         B.force[i] = f;
     }
     // energy per replica: one atomic per warp when the warp's rows share a replica
-    double e = (sub == 0) ? 0.5 * o.energy : 0.0;
     const int lane = threadIdx.x & 31;
     const int32_t r0 = __shfl_sync(0xffffffffu, r, 0);
-    double* ring = B.energyRing + (int64_t)(st % (unsigned long long)B.ring) * B.R;
-    if (__all_sync(0xffffffffu, r == r0 || r == -1))
+    double* ring = B.energyRing + (int64_t)B.sc->ringSlot * B.R;
+    const bool oneReplica = __all_sync(0xffffffffu, r == r0 || r == -1);
+    if (MIXED)
     {
-        e = mrmd_dev::warp_sum(e);
-        if (lane == 0 && r0 >= 0) atomicAdd(ring + r0, e);
+        float e = (sub == 0 && valid) ? 0.5f * o.fenergy : 0.0f;
+        if (oneReplica)
+        {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) e += __shfl_down_sync(0xffffffffu, e, off);
+            if (lane == 0 && r0 >= 0) atomicAdd(ring + r0, (double)e);
+        }
+        else if (r >= 0 && e != 0.0f)
+        {
+            atomicAdd(ring + r, (double)e);
+        }
     }
-    else if (r >= 0 && e != 0.0)
+    else
     {
-        atomicAdd(ring + r, e);
+        double e = (sub == 0 && valid) ? 0.5 * o.energy : 0.0;
+        if (oneReplica)
+        {
+            e = mrmd_dev::warp_sum(e);
+            if (lane == 0 && r0 >= 0) atomicAdd(ring + r0, e);
+        }
+        else if (r >= 0 && e != 0.0)
+        {
+            atomicAdd(ring + r, e);
+        }
     }
 }
 
@@ -827,17 +979,20 @@ __global__ void k_b_force(BDev B)
 __global__ void k_b_tail(BDev B, int rebuild)
 {
     __shared__ unsigned long long sStep, sRun, sSamples;
+    __shared__ int sCompUpdate, sTfUpdate;
     if (threadIdx.x == 0)
     {
         sStep = B.sc->step;
         sRun = B.sc->run;
-        sSamples = B.sc->tfSamples;
+        sSamples = B.sc->tfSamples + (unsigned long long)(B.sc->sampleTf != 0);  // including this step's sample
+        sCompUpdate = (sRun % (unsigned long long)B.compUpdate) == 0;
+        sTfUpdate = B.tfEnabled && ((sStep + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && sSamples > 0;
     }
     __syncthreads();
     const unsigned long long st = sStep, run = sRun;
     const int r = blockIdx.x;
     const RepDev& R = B.reps[r];
-    if ((run % (unsigned long long)B.compUpdate) == 0)
+    if (sCompUpdate)
     {
         for (int k = threadIdx.x; k < COMP_BINS; k += blockDim.x)
         {
@@ -850,10 +1005,9 @@ __global__ void k_b_tail(BDev B, int rebuild)
             B.compCounter[q] = 0;
         }
     }
-    if (B.tfEnabled)
+    if (sTfUpdate)
     {
-        const unsigned long long samples = sSamples + ((st % (unsigned long long)B.tfSampleInterval) == 0 ? 1 : 0);
-        if (((st + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && samples > 0)
+        const unsigned long long samples = sSamples;
         {
             double* d = B.tfWork + R.tfBase;
             for (int k = threadIdx.x; k < R.tfBins; k += blockDim.x)
@@ -892,10 +1046,7 @@ __global__ void k_b_tail(BDev B, int rebuild)
         {
             __threadfence();
             Scalars* s = B.sc;
-            unsigned long long samples = sSamples;
-            if (B.tfEnabled && (st % (unsigned long long)B.tfSampleInterval) == 0) ++samples;
-            if (B.tfEnabled && ((st + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && samples > 0) samples = 0;
-            s->tfSamples = samples;
+            s->tfSamples = sTfUpdate ? 0ull : sSamples;
             // on a rebuild step the pre-force displacement is measured against
             // the previous list, which this step no longer uses
             if (rebuild)
@@ -911,6 +1062,7 @@ __global__ void k_b_tail(BDev B, int rebuild)
             s->dispStep = 0.0;
             s->run = run + 1;
             s->step = st + 1;
+            set_step_flags(*s, st + 1, run + 1, B.ring, B.compSampling, B.tfEnabled, B.tfSampleInterval);
             s->done = 0u;
         }
     }
@@ -1259,6 +1411,16 @@ int run_graph(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
     }
 }
 
+// the step decisions of the current device step (after creation, a restored
+// state or a new ring size)
+int refresh_step_flags(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    MRMD_TRY(d2h(ctx, b->hSc, b->B.sc, sizeof(Scalars)));
+    set_step_flags(*b->hSc, b->hSc->step, b->hSc->run, b->B.ring, b->B.compSampling, b->B.tfEnabled,
+                   b->B.tfSampleInterval);
+    return h2d(ctx, b->B.sc, b->hSc, sizeof(Scalars));
+}
+
 int validate_tuning(mrmd_ctx* ctx, const mrmd_batch_tuning& t)
 {
     MRMD_CHECK_ARG(t.threadsPerRow == 1 || t.threadsPerRow == 2 || t.threadsPerRow == 4 || t.threadsPerRow == 8, ctx,
@@ -1293,7 +1455,7 @@ void free_all(mrmd_batch* b)
 {
     drop_graph(b);
     BDev& B = b->B;
-    void* ptrs[] = {B.pos, B.vel, B.force, B.mass, B.orig, B.slotRep, B.gSrc, B.gShift, B.imgFlags, B.ref, B.gCount,
+    void* ptrs[] = {B.pos, B.vel, B.force, B.mass, B.orig, B.slotRep, B.gSrc, B.gShift, B.imgFlags, B.ref, B.xImg, B.gCount,
                     B.lam, B.lamt, B.lamtf, B.hi, B.lo, B.cellOf, B.cellStart, B.cursor, B.unordered, B.sorted,
                     B.spos, B.counts, B.nbrs, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce, B.tfDensity, B.tfWork,
                     B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc, b->dReps, b->dTfFF};
@@ -1424,6 +1586,9 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
         B.rc2 = make_rcsq(B.rcSqr);
     }
     B.dt = cfg->dt;
+    B.dtHalfOverMass = 0.5 * cfg->dt / 1.0;  // molecules have unit mass (UpdateSteps.hpp:25-39 with m = 1)
+    B.ouDamping = std::exp(-cfg->gamma * cfg->dt);
+    B.ouSigma = std::sqrt(cfg->temperature * (1.0 - std::exp(-2.0 * cfg->gamma * cfg->dt)));
     B.zeta = cfg->gamma;
     B.temperature = cfg->temperature;
     B.rlist = rlist;
@@ -1457,6 +1622,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     alloc(B.orig, N);
     alloc(B.imgFlags, N);
     alloc(B.ref, N);
+    alloc(B.xImg, N);
     alloc(B.gCount, N + 1);
     alloc(B.counts, N);
     alloc(B.sPos, N);
@@ -1567,7 +1733,7 @@ int mrmd_batch_run(mrmd_ctx* ctx, mrmd_batch* b, int64_t nsteps, double* energie
     const int oldSync = ctx->sync;
     ctx->sync = 0;
     const int64_t P = b->cfg.tuning.graphSteps;
-    int rc = MRMD_OK;
+    int rc = refresh_step_flags(ctx, b);
     int64_t k = 0;
     while (rc == MRMD_OK && k < nsteps)
     {
@@ -1702,6 +1868,7 @@ namespace
 // without energies
 int advance(mrmd_ctx* ctx, mrmd_batch* b, int64_t n)
 {
+    MRMD_TRY(refresh_step_flags(ctx, b));
     const int64_t P = b->cfg.tuning.graphSteps;
     int64_t k = 0;
     while (k < n)

@@ -127,21 +127,26 @@ __device__ __forceinline__ df df_add(df a, df b)
     return fast_two_sum(s.h, s.l);
 }
 
-// 1/a with one Newton step on the double-float residual
+// 1/a with one Newton step on the double-float residual.  The seed is the
+// hardware's approximate reciprocal (a correctly rounded one would cost a
+// multi-instruction sequence and gains nothing: the Newton step squares
+// the seed's ~2^-23 error).
 __device__ __forceinline__ df df_rcp(df a)
 {
-    const float y = __frcp_rn(a.h);
+    const float y = __fdividef(1.0f, a.h);
     float r = __fmaf_rn(-a.h, y, 1.0f);
     r = __fmaf_rn(-a.l, y, r);
     return fast_two_sum(y, y * r);
 }
 
-// sqrt(a) with one Newton correction on the exact FMA residual
+// sqrt(a) from the approximate reciprocal square root and one Newton
+// correction on the exact FMA residual (a > 0)
 __device__ __forceinline__ df df_sqrt(df a)
 {
-    const float s = sqrtf(a.h);
+    const float q = rsqrtf(a.h);
+    const float s = a.h * q;
     const float r = __fmaf_rn(-s, s, a.h) + a.l;
-    return fast_two_sum(s, r / (2.0f * s));
+    return fast_two_sum(s, r * (0.5f * q));
 }
 
 // compensated accumulator (TwoSum), ~2^-48 relative to the final sum

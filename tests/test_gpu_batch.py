@@ -109,7 +109,9 @@ def test_replicas_bitwise_equal_alone(M, prec):
         assert np.array_equal(pa, pb[sl]), f"replica {r} positions"
         assert np.array_equal(va, vb[sl]), f"replica {r} velocities"
         assert np.array_equal(fa, fb[sl]), f"replica {r} forces"
-        np.testing.assert_allclose(eb[:, r], ea, rtol=1e-11, atol=1e-9)
+        # energies are diagnostics summed with atomics (FP32 warp sums in the
+        # mixed form), so they agree to rounding, not bitwise
+        np.testing.assert_allclose(eb[:, r], ea, rtol=1e-11 if prec == "fp64" else 1e-5, atol=1e-9)
         ta, _ = a.thermodynamic_force()
         tb, _ = b.thermodynamic_force()
         assert np.array_equal(ta[0], tb[r])
