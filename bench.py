@@ -488,13 +488,85 @@ def batch_main(args, rank, world, local_rank):
     print(json.dumps(out), flush=True)
 
 
+DIFF = dict(n=65536, box=(256.0, 16.0, 32.0), center=(128.0, 8.0, 16.0), at=30.0, hy=10.0, steps=500, window=100,
+            ckpt=25, loss_bins=128, loss_sigma=1.0, tf_bins=100, K=5)
+DIFF_WORKLOAD = ("AdResS trajectory gradient: 65,536 single-site molecules in 256x16x32 (density 0.5), slab 30 / hybrid "
+                 "10, Langevin T=1 gamma=1 with counter-based noise, rc 2.5 with force cap 1000, 500 steps, loss = "
+                 "squared deviation from uniform of the sigma_b=1 Gaussian-smoothed 128-bin x-density averaged over "
+                 "the last 100 steps; gradient w.r.t. the 100 thermodynamic-force coefficients and LJ epsilon, sigma "
+                 "by the hand-written adjoint with a checkpoint every 25 steps")
+
+
+def diff_main(args, rank, world, local_rank):
+    """Config-5 differentiation: forward + adjoint of a 500-step AdResS trajectory."""
+    import torch
+
+    import mrmd_gb300 as M
+
+    torch.cuda.set_device(local_rank)
+    ctx = M.Context(local_rank)
+    c, g = ADRESS, DIFF
+    rng = np.random.default_rng(5 + rank)
+    n = g["n"]
+    pos = rng.uniform(0.0, 1.0, (n, 3)) * np.asarray(g["box"])
+    vel = mb_velocities(n, c["T"], 6 + rank)
+    rep = M.Replica(n, [0, 0, 0], list(g["box"]), list(g["center"]), g["at"], 1234)
+    table = np.zeros(g["tf_bins"])
+    res = {}
+    for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        d = M.DiffSystem(rep, pos, vel, hybrid_diameter=g["hy"], steps=g["steps"], window=g["window"],
+                         checkpoint_interval=g["ckpt"], loss_bins=g["loss_bins"], loss_sigma=g["loss_sigma"],
+                         capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
+                         temperature=c["T"], tf_bin_width=g["box"][0] / g["tf_bins"], rebuild_interval=g["K"], ctx=ctx)
+        d.forward(table, 1.0, 1.0)  # warm-up (allocations, first rebuilds)
+        d.backward()
+        l0 = ctx.launches
+        with ClockSampler(local_rank) as clk:
+            t0 = time.perf_counter()
+            loss = d.forward(table, 1.0, 1.0)
+            t1 = time.perf_counter()
+            gt, ge, gs = d.backward()
+            t2 = time.perf_counter()
+        res[form] = dict(loss=loss, fwd=t1 - t0, bwd=t2 - t1, launches=ctx.launches - l0, clocks=clk.summary(),
+                         grad_eps=ge, grad_sigma=gs, grad_table_norm=float(np.linalg.norm(gt)))
+        d.close()
+    cpu = None
+    if not args.no_cpu:
+        ncores, model = cpu_info()
+        geo = dict(box=g["box"], center=g["center"], at=g["at"], hy=g["hy"], K=g["K"])
+        cv, done, ctime = run_adress_cpu(pos, vel, 10 ** 6, 1, args.cpu_budget, ncores, geo)
+        cpu = {"value": cv, "unit": METRIC, "cores": ncores, "kind": "port",
+               "sample": f"forward only: {done} steps of the {n}-molecule system by the oracle loop, "
+                         f"{ncores} OpenMP threads ({model}); the reference has no adjoint"}
+    head = "mixed" if "mixed" in res else next(iter(res))
+    r = res[head]
+    steps = g["steps"]
+    value = n * steps / (r["fwd"] + r["bwd"])
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": steps, "warmup": 1,
+        "ms_per_step": 1e3 * (r["fwd"] + r["bwd"]) / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f64 state, f32 double-float pair arithmetic",
+        "data": "synthetic (seeded uniform positions, Maxwell-Boltzmann velocities)",
+        "config": {"workload": DIFF_WORKLOAD, "molecules": n, "form": head,
+                   "note": "value = molecules x steps / (forward + adjoint wall time) of one gradient",
+                   "forms": {f: {"forward_s": res[f]["fwd"], "backward_s": res[f]["bwd"], "loss": res[f]["loss"],
+                                 "atom_steps_per_s_forward": n * steps / res[f]["fwd"],
+                                 "atom_steps_per_s_gradient": n * steps / (res[f]["fwd"] + res[f]["bwd"]),
+                                 "dL_depsilon": res[f]["grad_eps"], "dL_dsigma": res[f]["grad_sigma"],
+                                 "norm_dL_dtable": res[f]["grad_table_norm"], "kernel_launches": res[f]["launches"]}
+                             for f in res}},
+        "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["lj", "adress", "batch"], default="lj")
+    ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff"], default="lj")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
     ap.add_argument("--replicas", type=int, default=None, help="batch workload: replica count (default 512)")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
@@ -516,6 +588,9 @@ def main():
         return
     if args.workload == "batch":
         batch_main(args, rank, world, local_rank)
+        return
+    if args.workload == "diff":
+        diff_main(args, rank, world, local_rank)
         return
 
     import torch

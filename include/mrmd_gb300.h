@@ -495,7 +495,8 @@ typedef struct {
     int64_t nu;
     double gamma, temperature;
     int32_t tfEnabled;
-    int32_t reserved0;
+    int32_t compFrozen;       /* 1: no drift-compensation sampling or update; the mean
+                                 compensation energies keep their set values (zero) */
     double tfBinWidth, tfTargetDensity, tfModulation, tfSmoothingSigma, tfSmoothingRange;
     int64_t tfSampleInterval, tfUpdateInterval;
     int64_t compSamplingInterval; /* LJ_IdealGas intervals; 0 = the reference's 200 */
@@ -519,6 +520,7 @@ int mrmd_batch_get_tf(mrmd_ctx* ctx, mrmd_batch* b, double* force, double* densi
 int mrmd_batch_set_tf(mrmd_ctx* ctx, mrmd_batch* b, const double* force);
 /* Mean drift-compensation energies [numReplicas][200]. */
 int mrmd_batch_get_compensation(mrmd_ctx* ctx, mrmd_batch* b, double* mean);
+int mrmd_batch_set_compensation(mrmd_ctx* ctx, mrmd_batch* b, const double* mean);
 int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t);
 int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning* t);
 /* Time each candidate tuning (lanes per row, block size, rebuild interval)
@@ -535,6 +537,47 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
  * [8] ghost capacity, [9] flags (1 ghost overflow, 2 list overflow,
  * 4 a molecule moved skin/2 from its position at the last rebuild) */
 int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10);
+
+/* ------------------------------------------------- differentiation -- */
+/* Gradient of a trajectory loss of one AdResS system (the batched engine with
+ * one replica) by a hand-written adjoint of the weighted pair force
+ * (LJ_IdealGas.cpp:52-225, drift and compensation forces included), of the
+ * thermodynamic force (ThermodynamicForce.hpp:98-122) and of the Langevin
+ * velocity-Verlet step, with a checkpoint every checkpointInterval steps and
+ * recomputation.  The loss is sum_b (rho_b - rho_uniform)^2 of the x-density
+ * smoothed by a Gaussian of width lossSigma on lossBins bin centres and
+ * averaged over the last `window` steps.  The compensation means are held
+ * fixed and the TF table is not updated inside the trajectory; the table and
+ * the LJ epsilon and sigma are the parameters.  The reference has no
+ * differentiation. */
+typedef struct mrmd_diff mrmd_diff;
+typedef struct {
+    int64_t steps;
+    int64_t window;
+    int64_t checkpointInterval; /* a multiple of the rebuild interval */
+    int64_t lossBins;
+    double lossSigma;
+} mrmd_diff_config;
+
+int mrmd_diff_create(mrmd_ctx* ctx, mrmd_diff** out, const mrmd_batch_config* cfg, const mrmd_replica_desc* replica,
+                     const double* pos3, const double* vel3, const mrmd_diff_config* dc);
+int mrmd_diff_destroy(mrmd_ctx* ctx, mrmd_diff* d);
+int mrmd_diff_num_bins(const mrmd_diff* d, int64_t* tfBins);
+/* Replace the initial state (positions, velocities; forces start at zero). */
+int mrmd_diff_set_state(mrmd_ctx* ctx, mrmd_diff* d, const double* pos3, const double* vel3);
+/* Run the trajectory with the given TF table (NULL keeps the current one),
+ * epsilon and sigma; returns the loss and keeps the checkpoints. */
+int mrmd_diff_forward(mrmd_ctx* ctx, mrmd_diff* d, const double* tfTable, double epsilon, double sigma,
+                      double* loss);
+/* dLoss/dtable [tfBins], dLoss/depsilon, dLoss/dsigma of the last forward. */
+int mrmd_diff_backward(mrmd_ctx* ctx, mrmd_diff* d, double* gradTable, double* gradEpsilon, double* gradSigma);
+/* One force evaluation at the initial state and its vector-Jacobian product
+ * with adjoint3: force3 = F, xbar3 = (dF/dx)^T a, grads = (dF/dtheta)^T a. */
+int mrmd_diff_force_vjp(mrmd_ctx* ctx, mrmd_diff* d, const double* tfTable, double epsilon, double sigma,
+                        const double* adjoint3, double* force3, double* xbar3, double* gradTable,
+                        double* gradEpsilon, double* gradSigma);
+/* State at the end of the last forward run (input order). */
+int mrmd_diff_get_state(mrmd_ctx* ctx, mrmd_diff* d, double* pos3, double* vel3);
 
 #ifdef __cplusplus
 }

@@ -820,7 +820,7 @@ class BatchSystem:
                  epsilon=1.0, capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
                  gamma=1.0, temperature=1.0, tf=True, tf_bin_width=1.2, tf_target_density=0.5,
                  tf_modulation=1.0, tf_sigma=2.4, tf_range=3.0, tf_sample_interval=1,
-                 tf_update_interval=1000, comp_sampling_interval=0, comp_update_interval=0,
+                 tf_update_interval=1000, comp_sampling_interval=0, comp_update_interval=0, comp_frozen=False,
                  threads_per_row=1, block_size=128, rebuild_interval=10, sort_every=5, graph_steps=50,
                  initial_max_neighbors=0, initial_ghost_capacity=0, ctx: Context | None = None):
         self.ctx = ctx or default_context()
@@ -845,6 +845,7 @@ class BatchSystem:
         c.tfSmoothingSigma, c.tfSmoothingRange = tf_sigma, tf_range
         c.tfSampleInterval, c.tfUpdateInterval = int(tf_sample_interval), int(tf_update_interval)
         c.compSamplingInterval, c.compUpdateInterval = int(comp_sampling_interval), int(comp_update_interval)
+        c.compFrozen = int(bool(comp_frozen))
         c.initialMaxNeighbors, c.initialGhostCapacity = int(initial_max_neighbors), int(initial_ghost_capacity)
         c.tuning = _tuning_struct(dict(threads_per_row=threads_per_row, block_size=block_size,
                                        rebuild_interval=rebuild_interval, sort_every=sort_every,
@@ -892,6 +893,10 @@ class BatchSystem:
         self.ctx.check(self.ctx.lib.mrmd_batch_get_compensation(self.ctx.h, self.h, _dp(m)), "compensation")
         return m
 
+    def set_compensation(self, mean):
+        m = _f64(np.broadcast_to(mean, (self.num_replicas, 200)).copy())
+        self.ctx.check(self.ctx.lib.mrmd_batch_set_compensation(self.ctx.h, self.h, _dp(m)), "set compensation")
+
     @property
     def tuning(self):
         t = _abi.BatchTuningS()
@@ -925,6 +930,92 @@ class BatchSystem:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.mrmd_batch_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DiffSystem:
+    """One AdResS system with the adjoint of its trajectory loss (mrmd_diff_*).
+
+    forward(table, epsilon, sigma) runs `steps` steps from the initial state and
+    returns the loss: sum_b (rho_b - rho_uniform)^2 of the Gaussian-smoothed
+    (loss_sigma, loss_bins) x-density averaged over the last `window` steps.
+    backward() returns (dL/dtable, dL/depsilon, dL/dsigma) of that run.  The
+    compensation means are held fixed and the TF table is not updated inside
+    the trajectory."""
+
+    def __init__(self, replica, pos, vel, hybrid_diameter, steps=500, window=100, checkpoint_interval=25,
+                 loss_bins=128, loss_sigma=1.0, nu=1, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
+                 capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005, gamma=1.0,
+                 temperature=1.0, tf_bin_width=1.2, rebuild_interval=5, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        pos = _f64(pos)
+        vel = _f64(vel)
+        self.n = len(pos)
+        c = _abi.BatchConfigS()
+        c.rc, c.skin, c.sigma, c.epsilon = rc, skin, sigma, epsilon
+        c.cappingDistance = capping_distance
+        c.shifted = int(bool(shifted))
+        c.precision = int(precision)
+        c.dt = dt
+        c.hybridDiameter, c.nu = hybrid_diameter, int(nu)
+        c.gamma, c.temperature = gamma, temperature
+        c.tfEnabled = 1
+        c.tfBinWidth, c.tfTargetDensity, c.tfModulation = tf_bin_width, 0.5, 1.0
+        c.tfSmoothingSigma, c.tfSmoothingRange = 1.0, 1.0
+        c.tfSampleInterval, c.tfUpdateInterval = 1, int(steps) + 1
+        c.tuning = _tuning_struct(dict(threads_per_row=1, block_size=128, rebuild_interval=rebuild_interval,
+                                       sort_every=0, graph_steps=0))
+        dc = _abi.DiffConfigS(int(steps), int(window), int(checkpoint_interval), int(loss_bins), float(loss_sigma))
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.mrmd_diff_create(self.ctx.h, C.byref(h), C.byref(c), C.byref(replica._struct()),
+                                                     _dp(pos), _dp(vel), C.byref(dc)), "DiffSystem")
+        self.h = h
+        nb = C.c_int64()
+        self.ctx.lib.mrmd_diff_num_bins(self.h, C.byref(nb))
+        self.num_bins = int(nb.value)
+
+    def set_state(self, pos, vel):
+        self.ctx.check(self.ctx.lib.mrmd_diff_set_state(self.ctx.h, self.h, _dp(_f64(pos)), _dp(_f64(vel))),
+                       "set_state")
+
+    def forward(self, table, epsilon, sigma):
+        loss = C.c_double()
+        t = None if table is None else _f64(table)
+        self.ctx.check(self.ctx.lib.mrmd_diff_forward(self.ctx.h, self.h, _dp(t), float(epsilon), float(sigma),
+                                                      C.byref(loss)), "forward")
+        return float(loss.value)
+
+    def backward(self):
+        gt = np.zeros(max(self.num_bins, 1))
+        ge, gs = C.c_double(), C.c_double()
+        self.ctx.check(self.ctx.lib.mrmd_diff_backward(self.ctx.h, self.h, _dp(gt), C.byref(ge), C.byref(gs)),
+                       "backward")
+        return gt[:self.num_bins], float(ge.value), float(gs.value)
+
+    def force_vjp(self, table, epsilon, sigma, adjoint):
+        f, xb = np.zeros((self.n, 3)), np.zeros((self.n, 3))
+        gt = np.zeros(max(self.num_bins, 1))
+        ge, gs = C.c_double(), C.c_double()
+        t = None if table is None else _f64(table)
+        self.ctx.check(self.ctx.lib.mrmd_diff_force_vjp(self.ctx.h, self.h, _dp(t), float(epsilon), float(sigma),
+                                                        _dp(_f64(adjoint, (self.n, 3))), _dp(f), _dp(xb), _dp(gt),
+                                                        C.byref(ge), C.byref(gs)), "force_vjp")
+        return f, xb, gt[:self.num_bins], float(ge.value), float(gs.value)
+
+    def state(self):
+        p, v = np.zeros((self.n, 3)), np.zeros((self.n, 3))
+        self.ctx.check(self.ctx.lib.mrmd_diff_get_state(self.ctx.h, self.h, _dp(p), _dp(v)), "state")
+        return p, v
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.mrmd_diff_destroy(self.ctx.h, self.h)
             self.h = None
 
     def __del__(self):

@@ -118,12 +118,17 @@ class BatchConfigS(C.Structure):
                 ("cappingDistance", C.c_double), ("shifted", C.c_int32), ("precision", C.c_int32),
                 ("dt", C.c_double), ("hybridDiameter", C.c_double), ("nu", C.c_int64),
                 ("gamma", C.c_double), ("temperature", C.c_double), ("tfEnabled", C.c_int32),
-                ("reserved0", C.c_int32), ("tfBinWidth", C.c_double), ("tfTargetDensity", C.c_double),
+                ("compFrozen", C.c_int32), ("tfBinWidth", C.c_double), ("tfTargetDensity", C.c_double),
                 ("tfModulation", C.c_double), ("tfSmoothingSigma", C.c_double),
                 ("tfSmoothingRange", C.c_double), ("tfSampleInterval", C.c_int64),
                 ("tfUpdateInterval", C.c_int64), ("compSamplingInterval", C.c_int64),
                 ("compUpdateInterval", C.c_int64), ("initialMaxNeighbors", C.c_int64),
                 ("initialGhostCapacity", C.c_int64), ("tuning", BatchTuningS)]
+
+
+class DiffConfigS(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("window", C.c_int64), ("checkpointInterval", C.c_int64),
+                ("lossBins", C.c_int64), ("lossSigma", C.c_double)]
 
 
 P = C.POINTER
@@ -227,10 +232,21 @@ SIGNATURES = {
     "mrmd_batch_get_tf": (_i, [_v, _v, c_double_p, c_double_p, c_int64_p]),
     "mrmd_batch_set_tf": (_i, [_v, _v, c_double_p]),
     "mrmd_batch_get_compensation": (_i, [_v, _v, c_double_p]),
+    "mrmd_batch_set_compensation": (_i, [_v, _v, c_double_p]),
     "mrmd_batch_get_tuning": (_i, [_v, P(BatchTuningS)]),
     "mrmd_batch_set_tuning": (_i, [_v, _v, P(BatchTuningS)]),
     "mrmd_batch_autotune": (_i, [_v, _v, _i64, P(BatchTuningS), c_double_p, P(BatchTuningS), c_int64_p]),
     "mrmd_batch_stats": (_i, [_v, _v, c_int64_p]),
+    "mrmd_diff_create": (_i, [_v, P(_v), P(BatchConfigS), P(ReplicaS), c_double_p, c_double_p,
+                              P(DiffConfigS)]),
+    "mrmd_diff_destroy": (_i, [_v, _v]),
+    "mrmd_diff_num_bins": (_i, [_v, c_int64_p]),
+    "mrmd_diff_set_state": (_i, [_v, _v, c_double_p, c_double_p]),
+    "mrmd_diff_forward": (_i, [_v, _v, c_double_p, _d, _d, c_double_p]),
+    "mrmd_diff_backward": (_i, [_v, _v, c_double_p, c_double_p, c_double_p]),
+    "mrmd_diff_force_vjp": (_i, [_v, _v, c_double_p, _d, _d, c_double_p, c_double_p, c_double_p, c_double_p,
+                                 c_double_p, c_double_p]),
+    "mrmd_diff_get_state": (_i, [_v, _v, c_double_p, c_double_p]),
     "mrmd_md_atoms": (P(AtomsS), [_v]),
     "mrmd_md_nlist": (P(NListS), [_v]),
 }

@@ -36,193 +36,13 @@
 #include "lj_mixed.cuh"
 #include "nlist_impl.cuh"
 #include "thermo_impl.cuh"
+#include "batch_impl.cuh"
 
 using namespace mrmd_impl;
+using namespace mrmd_batch_impl;
 
 namespace
 {
-constexpr int TB = 256;
-constexpr double COMP_SCALE = 4294967296.0;  // 2^32: fixed point of the compensation histogram
-
-// list entries with this bit refer to a ghost whose pair instance in the
-// reference's half list is (ghost's source, image of the row molecule)
-constexpr int32_t REVERSED = (int32_t)0x80000000u;
-
-enum : uint32_t
-{
-    FLAG_GHOST_OVERFLOW = 1u,
-    FLAG_LIST_OVERFLOW = 2u,
-    FLAG_UNSAFE_INTERVAL = 4u,
-};
-
-// Per-replica constants.
-struct RepDev
-{
-    double lo[3], mx[3], L[3], minIn[3], maxIn[3];  // box corners, lengths, inner corners
-    double gmn[3], grdx[3];  // ghost-inclusive cell grid
-    int32_t gn[3];
-    int32_t cellBase;
-    double splitScale, splitInv;  // mixed form: coordinates split relative to gmn
-    SlabDev slab;
-    int32_t consistent;  // slab weights of every image equal those of its real molecule
-    int32_t lbase, n;
-    int32_t tfBase, tfBins;
-    double tfMin, tfBinSize, tfInvBin, tfBinVolume;
-    uint64_t seed;
-};
-
-// Device scalars (one struct, snapshotted with the state).
-struct Scalars
-{
-    unsigned long long step;    // global step number of the next step
-    unsigned long long tfSamples;
-    unsigned long long run;     // LJ_IdealGas run counter
-    double maxDisp;             // largest displacement of any molecule since the last rebuild
-    double dispStep;            // max |x - x_rebuild|^2 of the current step
-    int32_t numGhost;           // total ghosts written at the last rebuild (true count on overflow)
-    int32_t maxCount;           // largest list row seen (true count on overflow)
-    uint32_t overflow;          // ghost / list overflow of the rebuilds since the host cleared it
-    uint32_t flags;             // sticky: a molecule moved skin/2 between rebuilds
-    uint32_t done;              // tail-kernel block ticket
-    // decisions of the current step, set once per step (64-bit modulos are
-    // long instruction sequences; no per-thread kernel repeats them)
-    int32_t ringSlot;           // step % ring
-    int32_t sampleComp;         // run % compensation sampling interval == 0
-    int32_t sampleTf;           // TF enabled and step % TF sampling interval == 0
-};
-
-// the step decisions of (step, run)
-__host__ __device__ inline void set_step_flags(Scalars& s, unsigned long long step, unsigned long long run,
-                                               int32_t ring, int64_t compSampling, int32_t tfEnabled,
-                                               int64_t tfSampleInterval)
-{
-    s.ringSlot = (int32_t)(step % (unsigned long long)ring);
-    s.sampleComp = (run % (unsigned long long)compSampling) == 0;
-    s.sampleTf = tfEnabled && (step % (unsigned long long)tfSampleInterval) == 0;
-}
-
-// Everything the kernels read: pointers and run constants.
-struct BDev
-{
-    const RepDev* reps;
-    int32_t R, N, gCap;
-    int32_t listCap;
-    int64_t totalCells;
-    double4* pos;  // [N + gCap]
-    double4* vel;  // [N]
-    double4* force;
-    double* mass;
-    int32_t* orig;
-    int32_t* slotRep;  // [N + gCap]
-    int32_t* gSrc;     // [gCap]
-    uint8_t* gShift;   // [gCap] 2 bits per axis: 1 = +L, 2 = -L
-    uint8_t* imgFlags; // [N] bit 2d: has a +L image on axis d, bit 2d+1: has a -L image
-    float4* ref;       // [N] position at the last rebuild, relative to the replica's grid origin
-    int2* xImg;        // [N] slots of the ghost images shifted by -L / +L in x only (-1: none)
-    int32_t* gCount;   // [N + 1] images per local, then exclusive offsets
-    double4* lam;      // [N + gCap] (lambda, modulated lambda, grad lambda x, 0)
-    double* lamt;      // [N + gCap] modulated lambda
-    float2* lamtf;     // [N + gCap] modulated lambda as a double-float
-    float4* hi;        // mixed split coordinates [N + gCap]
-    float4* lo;
-    // cells
-    int32_t* cellOf;
-    int32_t* cellStart;  // [totalCells + 1]
-    int32_t* cursor;
-    int32_t* unordered;
-    int32_t* sorted;
-    float4* spos;
-    // list (32-row tiles)
-    int32_t* counts;
-    int32_t* nbrs;
-    // shadow for the cell sort of locals
-    double4* sPos;
-    double4* sVel;
-    double* sMass;
-    int32_t* sOrig;
-    // thermodynamic force and compensation energy
-    double* tfForce;                   // [sum bins]
-    unsigned long long* tfDensity;     // [sum bins] counts
-    double* tfWork;                    // [3 * sum bins]: density, smoothed, gradient
-    const double* tfFF;                // modulation / target density
-    int64_t totalBins;
-    long long* compEnergy;             // [R][200] fixed point
-    unsigned long long* compCounter;   // [R][200]
-    double* compMean;                  // [R][200]
-    double* energyRing;                // [ring][R]
-    int32_t ring;
-    Scalars* sc;
-    // physics
-    LJDev lj;
-    double rcSqr;
-    RcSq rc2;
-    double dt, zeta, temperature;
-    double dtHalfOverMass;  // dt/2 / m (molecules have unit mass)
-    double ouDamping, ouSigma;  // Ornstein-Uhlenbeck coefficients of the unit mass (UpdateSteps.hpp:56-79)
-    double rlist, halfSkin;
-    double cgMargin;  // distance beyond the hybrid region that counts as staying coarse grained
-    int64_t K, tfSampleInterval, tfUpdateInterval, compSampling, compUpdate;
-    int32_t tfEnabled;
-    double tfSigma, tfRange;
-    double listRsq;
-    float listRsqLo, listRsqHi;
-};
-
-__device__ __forceinline__ double coord(const double4& p, int d) { return d == 0 ? p.x : (d == 1 ? p.y : p.z); }
-
-__device__ __forceinline__ void set_coord(double4& p, int d, double v)
-{
-    if (d == 0)
-        p.x = v;
-    else if (d == 1)
-        p.y = v;
-    else
-        p.z = v;
-}
-
-// velocity-Verlet kick and drift with fused multiply-adds (the reference's
-// v += dt/2m F and x += dt v, each rounded once)
-__device__ __forceinline__ void kick_fma(double4& v, const double4& f, double dtfm)
-{
-    v.x = fma(dtfm, f.x, v.x);
-    v.y = fma(dtfm, f.y, v.y);
-    v.z = fma(dtfm, f.z, v.z);
-}
-
-__device__ __forceinline__ void drift_fma(double4& x, const double4& v, double dt)
-{
-    x.x = fma(dt, v.x, x.x);
-    x.y = fma(dt, v.y, x.y);
-    x.z = fma(dt, v.z, x.z);
-}
-
-// lambda, modulated lambda and grad lambda (x) of one slot, plus the mixed
-// form's split coordinates (UpdateMolecules.hpp:39-69 for a single site).
-template <bool MIXED>
-__device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int64_t s, const double4& x)
-{
-    double l, m, g;
-    slab_eval(R.slab, x.x, l, m, g);
-    B.lam[s] = make_double4(l, m, g, 0.0);
-    B.lamt[s] = m;
-    if (MIXED)
-    {
-        const float h = (float)m;
-        B.lamtf[s] = make_float2(h, (float)(m - (double)h));
-        SplitParams sp;
-        sp.scale = R.splitScale;
-        sp.invScale = R.splitInv;
-        float4 hv, lv;
-        split_one(x.x - R.gmn[0], sp, hv.x, lv.x);
-        split_one(x.y - R.gmn[1], sp, hv.y, lv.y);
-        split_one(x.z - R.gmn[2], sp, hv.z, lv.z);
-        hv.w = 0.0f;
-        lv.w = 0.0f;
-        B.hi[s] = hv;
-        B.lo[s] = lv;
-    }
-}
-
 // ------------------------------------------------------------------ pre --
 // B(dt/2) A(dt/2) O(dt) A(dt/2) (VelocityVerletLangevinThermostat.hpp:64-113)
 // with noise keyed by (replica seed, step, index inside the replica); on a
@@ -275,6 +95,14 @@ __global__ void k_b_pre(BDev B, int rebuild)
     }
     m2 = mrmd_dev::warp_max(m2);
     if ((threadIdx.x & 31) == 0) mrmd_dev::atomic_max_nonneg(&B.sc->dispStep, m2);
+}
+
+// weights and split coordinates of the locals at their current positions
+template <bool MIXED>
+__global__ void k_b_derive(BDev B)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
+        slot_derived<MIXED>(B, B.reps[B.slotRep[i]], i, B.pos[i]);
 }
 
 // ----------------------------------------------------------------- cells --
@@ -985,7 +813,7 @@ __global__ void k_b_tail(BDev B, int rebuild)
         sStep = B.sc->step;
         sRun = B.sc->run;
         sSamples = B.sc->tfSamples + (unsigned long long)(B.sc->sampleTf != 0);  // including this step's sample
-        sCompUpdate = (sRun % (unsigned long long)B.compUpdate) == 0;
+        sCompUpdate = B.compUpdate > 0 && (sRun % (unsigned long long)B.compUpdate) == 0;
         sTfUpdate = B.tfEnabled && ((sStep + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && sSamples > 0;
     }
     __syncthreads();
@@ -1071,60 +899,8 @@ __global__ void k_b_tail(BDev B, int rebuild)
 
 // ================================================================== host ==
 
-// Everything a step changes (positions, velocities, forces, the order of
-// the locals, the TF and compensation tables, the device scalars).
-struct Snap
+namespace mrmd_batch_impl
 {
-    double4 *pos = nullptr, *vel = nullptr, *force = nullptr;
-    double* mass = nullptr;
-    int32_t* orig = nullptr;
-    double* tfForce = nullptr;
-    unsigned long long* tfDensity = nullptr;
-    long long* compE = nullptr;
-    unsigned long long* compC = nullptr;
-    double* compM = nullptr;
-    Scalars* sc = nullptr;
-};
-
-struct mrmd_batch
-{
-    mrmd_batch_config cfg{};
-    int32_t R = 0, N = 0;
-    std::vector<RepDev> reps;
-    std::vector<int64_t> offsets;  // [R + 1] molecule offsets
-    int64_t totalCells = 0, totalBins = 0;
-    double listExtent = 0.0;
-    BDev B{};
-    RepDev* dReps = nullptr;
-    double* dTfFF = nullptr;
-    Snap sn;  // state before the running graph (overflow roll-back)
-    Scalars* hSc = nullptr;    // pinned
-    double* hRing = nullptr;   // pinned [ring][R]
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int64_t graphKernels = 0;
-    int64_t steps = 0, rebuilds = 0, graphLaunches = 0, recoveries = 0;
-    bool needRebuild = true;  // ghosts and list do not match the locals (new tuning, restored state)
-};
-
-namespace
-{
-template <typename T>
-int grow(mrmd_ctx* ctx, T*& p, int64_t oldCount, int64_t newCount)
-{
-    T* q = nullptr;
-    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&q), sizeof(T) * (size_t)(newCount > 0 ? newCount : 1)));
-    if (p && oldCount > 0)
-    {
-        const int64_t c = oldCount < newCount ? oldCount : newCount;
-        MRMD_CUDA(ctx, cudaMemcpyAsync(q, p, sizeof(T) * (size_t)c, cudaMemcpyDeviceToDevice, ctx->stream));
-        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    }
-    dfree(p);
-    p = q;
-    return MRMD_OK;
-}
-
 void drop_graph(mrmd_batch* b)
 {
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -1242,6 +1018,54 @@ bool is_sort(const mrmd_batch* b, int64_t st)
     return se > 0 && is_rebuild(b, st) && (st / b->cfg.tuning.rebuildInterval) % se == 0;
 }
 
+int derive_locals(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    const unsigned g = grid_for(ctx, b->N, TB);
+    if (b->cfg.precision == MRMD_PREC_MIXED)
+        k_b_derive<true><<<g, TB, 0, ctx->stream>>>(b->B);
+    else
+        k_b_derive<false><<<g, TB, 0, ctx->stream>>>(b->B);
+    return after_launch(ctx, "batch derive");
+}
+
+int update_ghosts(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    const unsigned g = grid_for(ctx, b->B.gCap, TB);
+    if (b->cfg.precision == MRMD_PREC_MIXED)
+        k_b_ghost_update<true><<<g, TB, 0, ctx->stream>>>(b->B);
+    else
+        k_b_ghost_update<false><<<g, TB, 0, ctx->stream>>>(b->B);
+    return after_launch(ctx, "batch ghost_update");
+}
+
+int eval_forces(mrmd_ctx* ctx, mrmd_batch* b)
+{
+    MRMD_TRY(derive_locals(ctx, b));
+    MRMD_TRY(rebuild_checked(ctx, b, false));
+    return b->cfg.precision == MRMD_PREC_MIXED ? force_m<true>(ctx, b) : force_m<false>(ctx, b);
+}
+
+int rebuild_checked(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
+{
+    BDev& B = b->B;
+    for (int attempt = 0;; ++attempt)
+    {
+        MRMD_CUDA(ctx, cudaMemsetAsync(&B.sc->overflow, 0, sizeof(uint32_t), ctx->stream));
+        MRMD_TRY(rebuild(ctx, b, sort));
+        MRMD_CUDA(ctx, cudaMemcpyAsync(b->hSc, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const uint32_t f = b->hSc->overflow;
+        if (!f) return MRMD_OK;
+        if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
+        int32_t gCap = B.gCap, lCap = B.listCap;
+        if (f & FLAG_GHOST_OVERFLOW) gCap = b->hSc->numGhost + b->hSc->numGhost / 4 + 1024;
+        if (f & FLAG_LIST_OVERFLOW) lCap = b->hSc->maxCount + b->hSc->maxCount / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
+        b->recoveries++;
+        sort = false;  // the locals are already in cell order
+    }
+}
+
 // One step, asynchronously.  With checkRebuild the rebuild is verified on the
 // host (one synchronisation) and repeated with larger buffers on overflow.
 int step(mrmd_ctx* ctx, mrmd_batch* b, int64_t st, bool checkRebuild)
@@ -1258,25 +1082,10 @@ int step(mrmd_ctx* ctx, mrmd_batch* b, int64_t st, bool checkRebuild)
     MRMD_TRY(after_launch(ctx, "batch pre"));
     if (reb)
     {
-        bool sort = is_sort(b, st);
-        for (int attempt = 0;; ++attempt)
-        {
-            if (checkRebuild)
-                MRMD_CUDA(ctx, cudaMemsetAsync(&B.sc->overflow, 0, sizeof(uint32_t), ctx->stream));
-            MRMD_TRY(rebuild(ctx, b, sort));
-            if (!checkRebuild) break;
-            MRMD_CUDA(ctx, cudaMemcpyAsync(b->hSc, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
-            MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            const uint32_t f = b->hSc->overflow;
-            if (!f) break;
-            if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
-            int32_t gCap = B.gCap, lCap = B.listCap;
-            if (f & FLAG_GHOST_OVERFLOW) gCap = b->hSc->numGhost + b->hSc->numGhost / 4 + 1024;
-            if (f & FLAG_LIST_OVERFLOW) lCap = b->hSc->maxCount + b->hSc->maxCount / 5 + 8;
-            MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
-            b->recoveries++;
-            sort = false;  // the locals are already in cell order
-        }
+        if (checkRebuild)
+            MRMD_TRY(rebuild_checked(ctx, b, is_sort(b, st)));
+        else
+            MRMD_TRY(rebuild(ctx, b, is_sort(b, st)));
         b->rebuilds++;
     }
     else
@@ -1464,7 +1273,7 @@ void free_all(mrmd_batch* b)
     if (b->hSc) cudaFreeHost(b->hSc);
     if (b->hRing) cudaFreeHost(b->hRing);
 }
-}  // namespace
+}  // namespace mrmd_batch_impl
 
 extern "C" {
 
@@ -1598,8 +1407,8 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     B.tfEnabled = cfg->tfEnabled;
     B.tfSampleInterval = cfg->tfEnabled ? cfg->tfSampleInterval : 1;
     B.tfUpdateInterval = cfg->tfEnabled ? cfg->tfUpdateInterval : 1;
-    B.compSampling = b->cfg.compSamplingInterval;
-    B.compUpdate = b->cfg.compUpdateInterval;
+    B.compSampling = cfg->compFrozen ? 0 : b->cfg.compSamplingInterval;
+    B.compUpdate = cfg->compFrozen ? 0 : b->cfg.compUpdateInterval;
     B.tfSigma = cfg->tfSmoothingSigma;
     B.tfRange = cfg->tfSmoothingRange;
     {
@@ -1817,6 +1626,13 @@ int mrmd_batch_get_compensation(mrmd_ctx* ctx, mrmd_batch* b, double* mean)
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     MRMD_TRY(d2h(ctx, mean, b->B.compMean, sizeof(double) * (size_t)b->R * COMP_BINS));
     return MRMD_OK;
+}
+
+int mrmd_batch_set_compensation(mrmd_ctx* ctx, mrmd_batch* b, const double* mean)
+{
+    if (!ctx || !b || !mean) return MRMD_ERR_ARG;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return h2d(ctx, b->B.compMean, mean, sizeof(double) * (size_t)b->R * COMP_BINS);
 }
 
 int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t)

@@ -14,9 +14,13 @@ def random_system(n, box, seed):
     return pos, vel
 
 
-def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_min=(0.0, 0.0, 0.0)):
+def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_min=(0.0, 0.0, 0.0),
+                tf_table=None, comp_frozen=False, on_step=None):
     """Returns positions, velocities, per-step energies, the TF table and the
-    LJ_IdealGas mean compensation energies after nsteps."""
+    LJ_IdealGas mean compensation energies after nsteps.  tf_table sets the
+    initial thermodynamic-force table; comp_frozen starts LJ_IdealGas at run 1
+    so that its compensation means stay zero; on_step(st, positions) sees the
+    positions after every step."""
     n = len(pos)
     lo = np.asarray(box_min, dtype=np.float64)
     hi = lo + np.asarray(box, dtype=np.float64)
@@ -31,7 +35,11 @@ def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_
     center = slab_center if slab_center is not None else list((lo + hi) / 2)
     slab = orc.slab(center, p["at"], p["hy"], p["nu"])
     ljig = orc.LJIdealGas(p["cap"], p["rc"], p["sigma"], p["epsilon"], True)
+    if comp_frozen:
+        ljig.s.runCounter = 1
     tf = orc.ThermodynamicForce([p["rho"]], sd, p["binw"], [p["mod"]], False, True)
+    if tf_table is not None:
+        tf.force[:, 0] = tf_table
     energies = []
     corr = co = no = None
     sd_seed = p["seed"] if seed is None else seed
@@ -59,5 +67,7 @@ def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_
             tf.sample(a)
         if (st + 1) % p["U"] == 0:
             tf.update(p["tfs"], p["tfr"])
+        if on_step is not None:
+            on_step(st, a.pos[:n])
     return (a.pos[:n].copy(), a.vel[:n].copy(), np.array(energies), tf.force[:, 0].copy(),
             ljig.mean[:, 0].copy())
