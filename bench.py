@@ -489,9 +489,10 @@ def batch_main(args, rank, world, local_rank):
 
 
 DIFF = dict(n=65536, box=(256.0, 16.0, 32.0), center=(128.0, 8.0, 16.0), at=30.0, hy=10.0, steps=500, window=100,
-            ckpt=25, loss_bins=128, loss_sigma=1.0, tf_bins=100, K=5)
+            ckpt=25, loss_bins=128, loss_sigma=1.0, tf_bins=100, K=5, relax=2000)
 DIFF_WORKLOAD = ("AdResS trajectory gradient: 65,536 single-site molecules in 256x16x32 (density 0.5), slab 30 / hybrid "
-                 "10, Langevin T=1 gamma=1 with counter-based noise, rc 2.5 with force cap 1000, 500 steps, loss = "
+                 "10, Langevin T=1 gamma=1 with counter-based noise, rc 2.5 with force cap 1000, relaxed for 2000 "
+                 "steps from a uniform placement, then 500 differentiated steps, loss = "
                  "squared deviation from uniform of the sigma_b=1 Gaussian-smoothed 128-bin x-density averaged over "
                  "the last 100 steps; gradient w.r.t. the 100 thermodynamic-force coefficients and LJ epsilon, sigma "
                  "by the hand-written adjoint with a checkpoint every 25 steps")
@@ -511,6 +512,13 @@ def diff_main(args, rank, world, local_rank):
     pos = rng.uniform(0.0, 1.0, (n, 3)) * np.asarray(g["box"])
     vel = mb_velocities(n, c["T"], 6 + rank)
     rep = M.Replica(n, [0, 0, 0], list(g["box"]), list(g["center"]), g["at"], 1234)
+    # relax the uniform placement with the capped potential under the thermostat
+    relax = M.BatchSystem([rep], pos, vel, hybrid_diameter=g["hy"], capping_distance=c["cap"], dt=c["dt"],
+                          gamma=c["gamma"], temperature=c["T"], tf=False, rebuild_interval=g["K"], sort_every=0,
+                          graph_steps=50, ctx=ctx)
+    relax.run(g["relax"], energies=False)
+    pos, vel, _ = relax.state()
+    relax.close()
     table = np.zeros(g["tf_bins"])
     res = {}
     for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
