@@ -229,6 +229,23 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest rank's time: every rank's replica must be done before the job is."""
+    if dist is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, steps, world, seconds):
+    """Whole-job throughput of independent replicas (one per rank): all units
+    of all ranks over the slowest rank's time."""
+    return units_per_rank * steps * world / seconds
+
+
 def time_run(torch, M, sysm, steps, stream):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -364,18 +381,33 @@ def adress_main(args, rank, world, local_rank):
         res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
                          stats=s.stats())
         s.close()
+        # the same system on the batched engine (one replica): four launches per step, 50-step graphs
+        rep = M.Replica(n, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], 1234)
+        b = M.BatchSystem([rep], pos, vel, hybrid_diameter=c["hy"], nu=c["nu"], rc=c["rc"], skin=c["skin"],
+                          capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
+                          temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
+                          tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
+                          tf_update_interval=c["U"], rebuild_interval=c["K"], sort_every=5, graph_steps=50, ctx=ctx)
+        b.run(max(args.warmup, 50), energies=False)
+        with ClockSampler(local_rank) as clk:
+            ms, wall, e, launches = time_run(torch, M, b, args.steps, stream)
+        st = b.stats()
+        res[form + "_batch_engine"] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches,
+                                           clocks=clk.summary(), stats={"pairs": st["pairs"],
+                                                                        "ghost_molecules": st["ghost_molecules"]})
+        b.close()
     cpu = None
     if not args.no_cpu:
         ncores, model = cpu_info()
         cv, done, ctime = run_adress_cpu(pos, vel, 10 ** 6, 3, args.cpu_budget, ncores)
         cpu = {"value": cv, "unit": METRIC, "cores": ncores, "kind": "port",
                "sample": f"{done} steps of the {n}-molecule system, {ncores} OpenMP threads ({model})"}
-    head = "mixed" if "mixed" in res else next(iter(res))
+    head = max(res, key=lambda f: res[f]["value"])
     r = res[head]
     print(json.dumps({
         "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f64 state, f32 double-float pair arithmetic",
+        "vs_baseline": None, "dtype": "f64" if head.startswith("fp64") else "f64 state, f32 double-float pair arithmetic",
         "data": "synthetic (seeded uniform positions, Maxwell-Boltzmann velocities)",
         "config": {"workload": ADRESS_WORKLOAD, "molecules": n, "form": head,
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
@@ -633,17 +665,14 @@ def main():
         with ClockSampler(local_rank) as clk:
             ms, wall, e, launches = time_run(torch, M, sysm, args.steps, stream)
         _, v1, _ = sysm.state()
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         # NVE drift over the timed steps: potential energy of the last step of
         # each run with the full-step velocities of the same positions
         e_start = ew[-1, 0] + kinetic(v0)
         e_end = e[-1, 0] + kinetic(v1)
         tau = args.steps * 0.005
         res[form] = dict(ms=ms, wall=wall, launches=launches,
-                         value=n * args.steps * world / (ms * 1e-3),
+                         value=replica_throughput(n, args.steps, world, ms * 1e-3),
                          drift=(e_end - e_start) / n / tau * 1000.0,
                          clocks=clk.summary(), stats=sysm.stats())
         systems[form] = sysm
@@ -696,11 +725,8 @@ def main():
     e2e_sys.run(args.steps)
     e2e_sys.state(out=outs)
     e2e_wall = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_wall], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_wall = float(t.item())
-    e2e_value = n * args.steps * world / e2e_wall
+    e2e_wall = max_over_ranks(e2e_wall, dist, "cuda")
+    e2e_value = replica_throughput(n, args.steps, world, e2e_wall)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
