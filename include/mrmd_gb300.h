@@ -370,6 +370,40 @@ int mrmd_tf_set_force(mrmd_ctx* ctx, mrmd_tf* tf, const double* in);
 int mrmd_tf_get_density(mrmd_ctx* ctx, const mrmd_tf* tf, double* out, int64_t* samples);
 /* getMuLeft / getMuRight (ThermodynamicForce.cpp:98-130), host [numTypes]. */
 int mrmd_tf_mu(mrmd_ctx* ctx, const mrmd_tf* tf, double* muLeft, double* muRight);
+/* createGrid(getForce()): the bin centres min + (i + 0.5) binSize
+ * (data/MultiHistogram.cpp:214-227, MultiHistogram.hpp:68-74), host [numBins]. */
+int mrmd_tf_grid(const mrmd_tf* tf, double* grid);
+
+/* ------------------------------------- thermodynamic-force table text -- */
+/* The text format of io/DumpThermoForce.cpp and io/RestoreThermoForce.cpp:
+ * line 1 the bin centres, then one line of forces per type; values separated
+ * by one space, written with std::ostream's default formatting (6 significant
+ * digits); every line ends with a newline.  The two table calls are host-only
+ * and take ctx only for the error message (it may be NULL). */
+
+/* dumpThermoForce(filename, tf, typeId) (io/DumpThermoForce.cpp:24-40) and
+ * dumpThermoForce(filename, tf) (:42-64) over host arrays grid[numBins] and
+ * force[numBins][numTypes]; typeId < 0 writes every type. */
+int mrmd_tf_write_table(mrmd_ctx* ctx, const char* path, int64_t numBins, const double* grid,
+                        int64_t numTypes, const double* force, int64_t typeId);
+/* The parser of restoreThermoForce (io/RestoreThermoForce.cpp:34-73): the grid
+ * line must hold >= 2 values, there may be at most maxNumForces force lines,
+ * each as long as the grid line (MRMD_ERR_ARG otherwise).  Returns the shape
+ * and binWidth = grid[1] - grid[0]; grid (numBins) and force
+ * ([numBins][numForces], `capacity` doubles) may be NULL to query the shape. */
+int mrmd_tf_read_table(mrmd_ctx* ctx, const char* path, int64_t maxNumForces, int64_t* numBins,
+                       int64_t* numForces, double* binWidth, double* grid, double* force,
+                       int64_t capacity);
+/* dumpThermoForce of a device table (io/DumpThermoForce.cpp:24-64). */
+int mrmd_tf_dump(mrmd_ctx* ctx, const mrmd_tf* tf, const char* path, int64_t typeId);
+/* restoreThermoForce(filename, subdomain, targetDensities, modulations,
+ * enforceSymmetry, usePeriodicity, maxNumForces) (io/RestoreThermoForce.cpp:24-90):
+ * a new table with the file's bin width, its forces uploaded.  The file must
+ * hold numTypes force lines of ceil(diameter / binWidth) values, the extents
+ * setForce's deep_copy requires (ThermodynamicForce.hpp:55). */
+int mrmd_tf_restore(mrmd_ctx* ctx, mrmd_tf** out, const char* path, const mrmd_subdomain* sd,
+                    int64_t numTypes, const double* targetDensity, const double* modulation,
+                    int enforceSymmetry, int usePeriodicity, int64_t maxNumForces);
 
 /* ---------------------------------------------- fused LJ NVE stepper -- */
 /* The examples/02_LennardJones_NVE time loop (02_LennardJones_NVE.cpp:135-216)

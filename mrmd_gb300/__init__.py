@@ -553,6 +553,17 @@ class ThermodynamicForce:
             self.ctx.h, C.byref(h), len(td), _dp(td), C.byref(subdomain.s),
             float(requested_bin_width), _dp(mod), int(bool(enforce_symmetry)),
             int(bool(use_periodicity))), "ThermodynamicForce")
+        self._adopt_handle(h)
+
+    @classmethod
+    def _adopt(cls, h, ctx: Context):
+        """Wrap a table made by the library (restoreThermoForce)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self._adopt_handle(h)
+        return self
+
+    def _adopt_handle(self, h):
         self.h = h
         nb, bs, nt = C.c_int64(), C.c_double(), C.c_int64()
         self.ctx.lib.mrmd_tf_shape(h, C.byref(nb), C.byref(bs), C.byref(nt))
@@ -603,6 +614,12 @@ class ThermodynamicForce:
     def getNumberOfDensityProfileSamples(self):
         self.getDensityProfile()
         return self.samples
+
+    def getGrid(self):
+        """createGrid(getForce()): the bin centres."""
+        out = np.zeros(self.num_bins)
+        self.ctx.check(self.ctx.lib.mrmd_tf_grid(self.h, _dp(out)), "grid")
+        return out
 
     def getMu(self):
         left, right = np.zeros(self.num_types), np.zeros(self.num_types)

@@ -210,6 +210,13 @@ SIGNATURES = {
     "mrmd_tf_set_force": (_i, [_v, _v, c_double_p]),
     "mrmd_tf_get_density": (_i, [_v, _v, c_double_p, c_int64_p]),
     "mrmd_tf_mu": (_i, [_v, _v, c_double_p, c_double_p]),
+    "mrmd_tf_grid": (_i, [_v, c_double_p]),
+    "mrmd_tf_write_table": (_i, [_v, C.c_char_p, _i64, c_double_p, _i64, c_double_p, _i64]),
+    "mrmd_tf_read_table": (_i, [_v, C.c_char_p, _i64, c_int64_p, c_int64_p, c_double_p, c_double_p,
+                                c_double_p, _i64]),
+    "mrmd_tf_dump": (_i, [_v, _v, C.c_char_p, _i64]),
+    "mrmd_tf_restore": (_i, [_v, P(_v), C.c_char_p, P(SubdomainS), _i64, c_double_p, c_double_p, _i, _i,
+                             _i64]),
     "mrmd_md_create": (_i, [_v, P(_v), P(MDConfigS), _i64, c_double_p, c_double_p, c_double_p]),
     "mrmd_md_destroy": (_i, [_v, _v]),
     "mrmd_md_run": (_i, [_v, _v, _i64, c_double_p]),

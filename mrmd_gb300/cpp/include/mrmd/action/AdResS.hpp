@@ -127,6 +127,11 @@ public:
                              std::vector<real_t>{thermodynamicForceModulation}, enforceSymmetry, usePeriodicity)
     {
     }
+    // Takes ownership of a table the library made (io::restoreThermoForce).
+    explicit ThermodynamicForce(mrmd_tf* adopted) : tf_(adopted)
+    {
+        mrmd_tf_shape(tf_, &numBins_, &binSize_, &numTypes_);
+    }
     ~ThermodynamicForce() { mrmd_tf_destroy(impl::context(), tf_); }
     ThermodynamicForce(const ThermodynamicForce&) = delete;
     ThermodynamicForce& operator=(const ThermodynamicForce&) = delete;
@@ -171,6 +176,15 @@ public:
     std::vector<real_t> getMuLeft() const { return mu().first; }
     std::vector<real_t> getMuRight() const { return mu().second; }
     idx_t numBins() const { return numBins_; }
+    idx_t numTypes() const { return numTypes_; }
+    // createGrid(getForce()): the bin centres.
+    std::vector<real_t> getGrid() const
+    {
+        std::vector<real_t> g(numBins_);
+        impl::check(mrmd_tf_grid(tf_, g.data()), "getGrid");
+        return g;
+    }
+    const mrmd_tf* raw() const { return tf_; }
 
 private:
     std::pair<std::vector<real_t>, std::vector<real_t>> mu() const

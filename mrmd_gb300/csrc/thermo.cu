@@ -194,6 +194,14 @@ int mrmd_tf_shape(const mrmd_tf* tf, int64_t* numBins, double* binSize, int64_t*
     return MRMD_OK;
 }
 
+int mrmd_tf_grid(const mrmd_tf* tf, double* grid)
+{
+    // data/MultiHistogram.cpp:214-227 with getBinPosition (MultiHistogram.hpp:68-74)
+    if (!tf || !grid) return MRMD_ERR_ARG;
+    for (int64_t i = 0; i < tf->numBins; ++i) grid[i] = tf->min + ((double)i + 0.5) * tf->binSize;
+    return MRMD_OK;
+}
+
 int mrmd_tf_sample(mrmd_ctx* ctx, mrmd_tf* tf, const mrmd_atoms* a)
 {
     // ThermodynamicForce.cpp:74-86

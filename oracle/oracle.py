@@ -593,6 +593,57 @@ class ThermodynamicForce:
         return l, r
 
 
+# ------------------------------------------------ thermodynamic-force text --
+
+def tf_grid(min_x, max_x, num_bins):
+    """createGrid: bin centres min + (i + 0.5) binSize (data/MultiHistogram.cpp:214-227,
+    MultiHistogram.hpp:40-41, 68-74)."""
+    bin_size = (max_x - min_x) / num_bins
+    return np.array([min_x + (i + 0.5) * bin_size for i in range(num_bins)])
+
+
+def tf_table_text(grid, force, type_id=None):
+    """dumpThermoForce (io/DumpThermoForce.cpp:24-64) through DumpProfile::dumpScalarView
+    (io/DumpProfile.cpp:25-35): values joined by one space, each formatted like a
+    default std::ostream (printf %g, 6 significant digits), every line ended by a newline."""
+    force = np.asarray(force, dtype=np.float64).reshape(len(grid), -1)
+    types = range(force.shape[1]) if type_id is None else [type_id]
+    lines = [" ".join("%g" % v for v in grid)]
+    lines += [" ".join("%g" % v for v in force[:, t]) for t in types]
+    return "".join(line + "\n" for line in lines)
+
+
+def tf_table_parse(text, max_num_forces=10):
+    """restoreThermoForce's reader (io/RestoreThermoForce.cpp:34-73): returns
+    (grid, force [numBins][numForces], binWidth = grid[1] - grid[0]).  Raises
+    ValueError where the reference asserts (fewer than two bins, more than
+    max_num_forces lines) and on lines whose length differs from the grid's."""
+    lines = text.split("\n")
+    if lines and lines[-1] == "":
+        lines.pop()
+    if not lines:
+        raise ValueError("empty table")
+    grid = [float(w) for w in lines[0].split()]
+    if len(grid) < 2:
+        raise ValueError("fewer than two bins")
+    rows = []
+    for line in lines[1:]:
+        row = [float(w) for w in line.split()]
+        if len(row) != len(grid):
+            raise ValueError("ragged force line")
+        rows.append(row)
+        if len(rows) > max_num_forces:
+            raise ValueError("too many force lines")
+    force = np.array(rows, dtype=np.float64).T.reshape(len(grid), len(rows))
+    return np.array(grid), force, grid[1] - grid[0]
+
+
+def tf_num_bins(sd: Subdomain, bin_width):
+    """ceil(diameter / binWidth), the bin count of ThermodynamicForce's constructor
+    (action/ThermodynamicForce.cpp:34)."""
+    return int(lib().orc_tf_num_bins(C.byref(sd), float(bin_width)))
+
+
 # --------------------------------------------------------- canonical pairs --
 
 def canonical_pairs(counts, nbrs, corr, n_local):

@@ -29,3 +29,17 @@ def test_cpp_espp_driver(tmp_path, espp):
     assert out["ghost"] == g["num_ghost"]
     assert out["pairs"] == g["num_pairs"]
     assert out["failures"] == 0
+
+
+def test_cpp_thermo_force_io(tmp_path):
+    """io/ThermoForce.test.cpp (dumpSingleForce, dumpMultipleForces) through
+    the drop-in io::dumpThermoForce / io::restoreThermoForce."""
+    from mrmd_gb300 import build as B
+
+    B.build()
+    exe = os.path.join(ROOT, "mrmd_gb300", "_build", "thermo_force_io")
+    assert os.path.exists(exe)
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert json.loads(r.stdout.strip().splitlines()[-1])["failures"] == 0
+    assert (tmp_path / "dummyMultipleForces.txt").read_text().count("\n") == 6
