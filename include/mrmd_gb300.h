@@ -343,6 +343,18 @@ int mrmd_ljig_get_compensation(mrmd_ctx* ctx, const mrmd_ljig* s, double* mean, 
                                double* counter, int64_t* runCounter);
 int mrmd_ljig_set_compensation(mrmd_ctx* ctx, mrmd_ljig* s, const double* mean);
 
+/* ------------------------------------------------------------ analysis -- */
+/* Deterministic device sums (fixed grid and order; same bits on every run). */
+/* analysis::getKineticEnergy (analysis/KineticEnergy.hpp:26-39): 0.5 sum m v.v
+ * over the local atoms. */
+int mrmd_kinetic_energy(mrmd_ctx* ctx, const mrmd_atoms* a, double* out);
+/* analysis::getSystemMomentum (analysis/SystemMomentum.cpp:21-48): the sum of
+ * the local atoms' velocities (the reference applies no mass factor). */
+int mrmd_system_momentum(mrmd_ctx* ctx, const mrmd_atoms* a, double* out3);
+/* analysis::getPressure (analysis/Pressure.cpp:23-51): sum over local and
+ * ghost atoms of m v.v + F.x, divided by 3 * Subdomain::getVolume. */
+int mrmd_pressure(mrmd_ctx* ctx, const mrmd_atoms* a, const mrmd_subdomain* sd, double* out);
+
 /* ------------------------------------------------ thermodynamic force -- */
 typedef struct mrmd_tf mrmd_tf;
 /* ThermodynamicForce(targetDensity[], subdomain, binWidth, modulation[],
@@ -426,6 +438,8 @@ typedef struct {
     int32_t useGraph;        /* capture the steps between rebuilds as a CUDA graph */
     int32_t sortAtoms;       /* k > 0: permute atoms into cell order at every k-th rebuild; 0: never */
     int64_t maxNeighbors;    /* initial list capacity (grown on overflow) */
+    int32_t observe;         /* record kinetic energy and momentum of every step */
+    int32_t reserved0;
 } mrmd_md_config;
 
 int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int64_t n,
@@ -434,6 +448,13 @@ int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md);
 /* Advance nsteps; energies (may be NULL) receives the LJ energy and virial
  * of every step as [nsteps][2] (read back from pinned memory at the end). */
 int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies);
+/* As mrmd_md_run for a stepper created with observe = 1; records receives
+ * [nsteps][6]: LJ energy, LJ virial, kinetic energy (analysis/KineticEnergy.hpp:26-39)
+ * and the velocity sum of getSystemMomentum (analysis/SystemMomentum.cpp:21-48)
+ * at the end of every step, with full-step velocities.  They are summed on the
+ * device inside the step's own kernels (deterministic order); the only host
+ * transfer is the one copy of all records at the end of the run. */
+int mrmd_md_run_observed(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* records);
 /* Current state in the ORIGINAL atom order (host [n][3] arrays, NULL skips). */
 int mrmd_md_get_state(mrmd_ctx* ctx, mrmd_md* md, double* pos3, double* vel3, double* force3);
 /* Replace positions/velocities (original order) and force a rebuild. */

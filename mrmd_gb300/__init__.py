@@ -633,13 +633,43 @@ class ThermodynamicForce:
             pass
 
 
+def getKineticEnergy(atoms: Atoms) -> float:
+    """analysis::getKineticEnergy (analysis/KineticEnergy.hpp:26-39)."""
+    out = C.c_double()
+    atoms.ctx.check(atoms.ctx.lib.mrmd_kinetic_energy(atoms.ctx.h, C.byref(atoms.s), C.byref(out)),
+                    "getKineticEnergy")
+    return out.value
+
+
+def getMeanKineticEnergy(atoms: Atoms) -> float:
+    """analysis::getMeanKineticEnergy (analysis/KineticEnergy.hpp:44-47)."""
+    return getKineticEnergy(atoms) / float(atoms.numLocalAtoms)
+
+
+def getSystemMomentum(atoms: Atoms):
+    """analysis::getSystemMomentum (analysis/SystemMomentum.cpp:21-48): the
+    velocity sum of the local atoms."""
+    out = np.zeros(3)
+    atoms.ctx.check(atoms.ctx.lib.mrmd_system_momentum(atoms.ctx.h, C.byref(atoms.s), _dp(out)),
+                    "getSystemMomentum")
+    return out
+
+
+def getPressure(atoms: Atoms, subdomain: Subdomain) -> float:
+    """analysis::getPressure (analysis/Pressure.cpp:23-51)."""
+    out = C.c_double()
+    atoms.ctx.check(atoms.ctx.lib.mrmd_pressure(atoms.ctx.h, C.byref(atoms.s), C.byref(subdomain.s),
+                                                C.byref(out)), "getPressure")
+    return out.value
+
+
 class LJSystem:
     """Fused device-resident LJ NVE stepper (mrmd_md_*), the examples/02 loop."""
 
     def __init__(self, pos, vel, box_min, box_max, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
                  capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
                  rebuild_interval=10, use_graph=True, sort_atoms=True, max_neighbors=0, mass=None,
-                 ctx: Context | None = None):
+                 observe=False, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -656,6 +686,7 @@ class LJSystem:
         cfg.useGraph = int(bool(use_graph))
         cfg.sortAtoms = int(bool(sort_atoms))
         cfg.maxNeighbors = int(max_neighbors)
+        cfg.observe = int(bool(observe))
         self.cfg = cfg
         h = C.c_void_p()
         m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())
@@ -667,6 +698,15 @@ class LJSystem:
         e = np.zeros((max(nsteps, 1), 2)) if energies else None
         self.ctx.check(self.ctx.lib.mrmd_md_run(self.ctx.h, self.h, int(nsteps), _dp(e)), "run")
         return e[:nsteps] if energies else None
+
+    def run_observed(self, nsteps: int):
+        """Advance nsteps (stepper created with observe=True); returns the
+        per-step records [nsteps, 6]: LJ energy, LJ virial, kinetic energy,
+        momentum (velocity sum) x, y, z, summed on the device."""
+        r = np.zeros((max(nsteps, 1), 6))
+        self.ctx.check(self.ctx.lib.mrmd_md_run_observed(self.ctx.h, self.h, int(nsteps), _dp(r)),
+                       "run_observed")
+        return r[:nsteps]
 
     def state(self, out=None):
         """(pos, vel, force) in the original atom order; `out` may supply three

@@ -86,7 +86,8 @@ class MDConfigS(C.Structure):
                 ("skin", C.c_double), ("sigma", C.c_double), ("epsilon", C.c_double),
                 ("cappingDistance", C.c_double), ("shifted", C.c_int32),
                 ("precision", C.c_int32), ("dt", C.c_double), ("rebuildInterval", C.c_int64),
-                ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64)]
+                ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64),
+                ("observe", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class AdResSConfigS(C.Structure):
@@ -220,6 +221,10 @@ SIGNATURES = {
     "mrmd_md_create": (_i, [_v, P(_v), P(MDConfigS), _i64, c_double_p, c_double_p, c_double_p]),
     "mrmd_md_destroy": (_i, [_v, _v]),
     "mrmd_md_run": (_i, [_v, _v, _i64, c_double_p]),
+    "mrmd_md_run_observed": (_i, [_v, _v, _i64, c_double_p]),
+    "mrmd_kinetic_energy": (_i, [_v, P(AtomsS), c_double_p]),
+    "mrmd_system_momentum": (_i, [_v, P(AtomsS), c_double_p]),
+    "mrmd_pressure": (_i, [_v, P(AtomsS), P(SubdomainS), c_double_p]),
     "mrmd_md_get_state": (_i, [_v, _v, c_double_p, c_double_p, c_double_p]),
     "mrmd_md_set_state": (_i, [_v, _v, c_double_p, c_double_p]),
     "mrmd_md_stats": (_i, [_v, c_int64_p]),

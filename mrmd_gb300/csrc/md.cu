@@ -20,29 +20,69 @@
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
 #include "nlist_impl.cuh"
+#include "reduce_impl.cuh"
 
 using namespace mrmd_impl;
 
 namespace
 {
 constexpr int TB = 256;
+// Per-step record: LJ energy, LJ virial, kinetic energy, momentum x, y, z.
+constexpr int REC = 6;
 
-__global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
-                                   const double* __restrict__ mass, int64_t n, double dtHalf, double dt, int postKick)
+// Kinetic energy (analysis/KineticEnergy.hpp:26-39) and the velocity sum of
+// getSystemMomentum (analysis/SystemMomentum.cpp:21-48) of one atom.
+__device__ __forceinline__ void observe_add(double (&o)[4], const double4& v, double m)
 {
+    o[0] += 0.5 * (m * (v.x * v.x + v.y * v.y + v.z * v.z));
+    o[1] += v.x;
+    o[2] += v.y;
+    o[3] += v.z;
+}
+
+// OBS: the velocities after the post-kick are the full-step velocities of
+// the previous step; their kinetic energy and momentum go to rec[2..5] of
+// that step's record (deterministic grid sum).
+template <bool OBS>
+__global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
+                                   const double* __restrict__ mass, int64_t n, double dtHalf, double dt, int postKick,
+                                   double* partial, unsigned* ticket, double* rec)
+{
+    double o[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
         double4 v = vel[i], x = pos[i];
         const double4 f = force[i];
-        const double dtfm = __ddiv_rn(dtHalf, mass[i]);
+        const double m = mass[i];
+        const double dtfm = __ddiv_rn(dtHalf, m);
         if (postKick) kick(v, f, dtfm);  // VelocityVerlet::postForceIntegrate of the previous step
+        if (OBS) observe_add(o, v, m);
         kick(v, f, dtfm);                // preForceIntegrate
         drift(x, v, dt);
         pos[i] = x;
         vel[i] = v;
         force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
     }
+    if (OBS) grid_sum<4>(o, partial, ticket, rec + 2);
+}
+
+// The record of the last step of a run: full-step velocities formed on the
+// fly (v + dt/2 F/m), nothing stored.
+__global__ void k_observe_post(const double4* __restrict__ vel, const double4* __restrict__ force,
+                               const double* __restrict__ mass, int64_t n, double dtHalf, int postKick,
+                               double* partial, unsigned* ticket, double* rec)
+{
+    double o[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        double4 v = vel[i];
+        const double m = mass[i];
+        if (postKick) kick(v, force[i], __ddiv_rn(dtHalf, m));
+        observe_add(o, v, m);
+    }
+    grid_sum<4>(o, partial, ticket, rec + 2);
 }
 
 __global__ void k_post_kick(double4* __restrict__ vel, const double4* __restrict__ force,
@@ -116,9 +156,11 @@ struct mrmd_md
     float4* split = nullptr;     // [2][capacity] hi, lo
     int64_t splitCap = 0;
     SplitParams sp{};
-    double* dEnergy = nullptr;   // [energyCap][2]
+    double* dEnergy = nullptr;   // [energyCap][REC] per-step records
     int64_t energyCap = 0;
     double* hEnergy = nullptr;   // pinned
+    double* dPartial = nullptr;  // per-block partial sums of the step observables
+    unsigned* dTicket = nullptr;
     int64_t n = 0;
     int64_t steps = 0, rebuilds = 0;
     bool forceValid = false;     // force array holds F(x) of the current positions
@@ -187,16 +229,33 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
     return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
 }
 
-// One step without rebuild, for capture: kick/drift, ghost update, forces.
-int md_plain_step(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool postKick)
+// Kick / drift / force reset of one step; prevRec (may be null) receives the
+// observables of the previous step when the stepper records them.
+int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec)
 {
     mrmd_atoms* a = &md->atoms;
-    k_fused_kick_drift<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(
-        reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel), reinterpret_cast<double4*>(a->force),
-        a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0);
-    MRMD_TRY(after_launch(ctx, "fused_kick_drift"));
+    const unsigned grid = grid_for(ctx, md->n, TB);
+    if (md->cfg.observe && postKick && prevRec)
+        k_fused_kick_drift<true><<<grid, TB, 0, ctx->stream>>>(
+            reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
+            reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, 1, md->dPartial,
+            md->dTicket, prevRec);
+    else
+        k_fused_kick_drift<false><<<grid, TB, 0, ctx->stream>>>(
+            reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
+            reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0,
+            nullptr, nullptr, nullptr);
+    return after_launch(ctx, "fused_kick_drift");
+}
+
+// One step without rebuild, for capture: kick/drift, ghost update, forces
+// into this step's record rec; prevRec (may be null) is the previous step's.
+int md_plain_step(mrmd_ctx* ctx, mrmd_md* md, double* rec, double* prevRec, bool postKick)
+{
+    mrmd_atoms* a = &md->atoms;
+    MRMD_TRY(md_kick_drift(ctx, md, postKick, prevRec));
     MRMD_TRY(mrmd_ghost_update(ctx, &md->ghosts, a, &md->sd));
-    return md_forces(ctx, md, ev);
+    return md_forces(ctx, md, rec);
 }
 
 int ensure_energy(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps)
@@ -208,8 +267,8 @@ int ensure_energy(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps)
     md->dEnergy = nullptr;
     md->hEnergy = nullptr;
     const int64_t c = nsteps + 64;
-    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->dEnergy), sizeof(double) * 2 * (size_t)c));
-    MRMD_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&md->hEnergy), sizeof(double) * 2 * (size_t)c));
+    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->dEnergy), sizeof(double) * REC * (size_t)c));
+    MRMD_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&md->hEnergy), sizeof(double) * REC * (size_t)c));
     md->energyCap = c;
     // any captured graph referenced the old buffer
     if (md->exec)
@@ -238,7 +297,8 @@ int capture_steps(mrmd_ctx* ctx, mrmd_md* md, int64_t count, int64_t slot0)
     MRMD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = MRMD_OK;
     const int64_t launches0 = ctx->launches;
-    for (int64_t k = 0; k < count && rc == MRMD_OK; ++k) rc = md_plain_step(ctx, md, md->dEnergy + 2 * (slot0 + k), true);
+    for (int64_t k = 0; k < count && rc == MRMD_OK; ++k)
+        rc = md_plain_step(ctx, md, md->dEnergy + REC * (slot0 + k), md->dEnergy + REC * (slot0 + k - 1), true);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     // captured kernels run when the graph is launched: count them there
     md->graphLaunches = ctx->launches - launches0;
@@ -317,6 +377,17 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->origTmp), sizeof(int32_t) * (size_t)n);
     if (rc == MRMD_OK)
     {
+        // one partial per block of the fused kernel, then the ticket
+        const size_t parts = (size_t)grid_for(ctx, n, TB) * 4;
+        rc = dmalloc(ctx, reinterpret_cast<void**>(&md->dPartial), sizeof(double) * parts + 256);
+        if (rc == MRMD_OK)
+        {
+            md->dTicket = reinterpret_cast<unsigned*>(md->dPartial + parts);
+            rc = dzero(ctx, md->dTicket, sizeof(unsigned));
+        }
+    }
+    if (rc == MRMD_OK)
+    {
         k_iota<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(md->orig, n);
         rc = after_launch(ctx, "iota");
     }
@@ -346,19 +417,27 @@ int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md)
     dfree(md->origTmp);
     dfree(md->split);
     dfree(md->dEnergy);
+    dfree(md->dPartial);
     if (md->hEnergy) cudaFreeHost(md->hEnergy);
     delete md;
     return MRMD_OK;
 }
 
-int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
+}  // extern "C"
+
+namespace
+{
+// The time loop; out (may be NULL) receives the first `cols` values of every
+// step's record, [nsteps][cols].
+int md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* out, int cols)
 {
     if (!ctx || !md || nsteps < 0) return MRMD_ERR_ARG;
     if (nsteps == 0) return MRMD_OK;
     MRMD_TRY(ensure_energy(ctx, md, nsteps));
     const int oldSync = ctx->sync;
     ctx->sync = 0;
-    int rc = check_cuda(ctx, cudaMemsetAsync(md->dEnergy, 0, sizeof(double) * 2 * (size_t)(nsteps + 1), ctx->stream),
+    double* rec = md->dEnergy;
+    int rc = check_cuda(ctx, cudaMemsetAsync(rec, 0, sizeof(double) * REC * (size_t)(nsteps + 1), ctx->stream),
                         "energy clear");
     mrmd_atoms* a = &md->atoms;
     const int64_t K = md->cfg.rebuildInterval;
@@ -367,9 +446,12 @@ int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
     {
         rc = md_rebuild(ctx, md);
         if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, a, a->numLocal + a->numGhost, 0.0);
-        if (rc == MRMD_OK) rc = md_forces(ctx, md, md->dEnergy + 2 * nsteps);  // scratch slot
+        if (rc == MRMD_OK) rc = md_forces(ctx, md, rec + REC * nsteps);  // scratch slot
         md->forceValid = true;
     }
+    // the previous step's record, for the kinetic energy its post-kick yields;
+    // none for the first step of a run (the last run's end recorded it)
+    auto prev = [&](int64_t slot) { return slot > 0 ? rec + REC * (slot - 1) : nullptr; };
     int64_t s = 0;
     while (rc == MRMD_OK && s < nsteps)
     {
@@ -377,14 +459,10 @@ int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
         if (md->needRebuild || global % K == 0)
         {
             // rebuild step, eager: kick/drift, rebuild, forces
-            k_fused_kick_drift<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(
-                reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
-                reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt,
-                global > 0 ? 1 : 0);
-            rc = after_launch(ctx, "fused_kick_drift");
+            rc = md_kick_drift(ctx, md, global > 0, prev(s));
             if (rc == MRMD_OK) rc = md_rebuild(ctx, md);
             if (rc == MRMD_OK) rc = mrmd_atoms_set_force(ctx, a, a->numLocal + a->numGhost, 0.0);
-            if (rc == MRMD_OK) rc = md_forces(ctx, md, md->dEnergy + 2 * s);
+            if (rc == MRMD_OK) rc = md_forces(ctx, md, rec + REC * s);
             ++s;
             // the steps up to the next rebuild, as one graph (or eagerly)
             const int64_t nextRebuild = ((md->steps + s + K - 1) / K) * K;
@@ -407,31 +485,53 @@ int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
                 else
                 {
                     for (int64_t k = 0; k < count && rc == MRMD_OK; ++k)
-                        rc = md_plain_step(ctx, md, md->dEnergy + 2 * (s + k), true);
+                        rc = md_plain_step(ctx, md, rec + REC * (s + k), prev(s + k), true);
                 }
                 s += count;
             }
         }
         else
         {
-            rc = md_plain_step(ctx, md, md->dEnergy + 2 * s, true);
+            rc = md_plain_step(ctx, md, rec + REC * s, prev(s), true);
             ++s;
         }
     }
     md->steps += s;
-    ctx->sync = oldSync;
-    if (rc != MRMD_OK) return rc;
     // The stored velocities stay half-kicked: the post-kick of the last step
     // is applied by the first fused kernel of the next run (and to a copy by
-    // mrmd_md_get_state).
-    if (energies)
+    // mrmd_md_get_state and here).
+    if (rc == MRMD_OK && md->cfg.observe)
     {
-        MRMD_CUDA(ctx, cudaMemcpyAsync(md->hEnergy, md->dEnergy, sizeof(double) * 2 * (size_t)nsteps,
+        k_observe_post<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(
+            reinterpret_cast<const double4*>(a->vel), reinterpret_cast<const double4*>(a->force), a->mass, md->n,
+            0.5 * md->cfg.dt, md->steps > 0 ? 1 : 0, md->dPartial, md->dTicket, rec + REC * (nsteps - 1));
+        rc = after_launch(ctx, "observe_post");
+    }
+    ctx->sync = oldSync;
+    if (rc != MRMD_OK) return rc;
+    if (out)
+    {
+        MRMD_CUDA(ctx, cudaMemcpyAsync(md->hEnergy, rec, sizeof(double) * REC * (size_t)nsteps,
                                        cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        std::memcpy(energies, md->hEnergy, sizeof(double) * 2 * (size_t)nsteps);
+        for (int64_t k = 0; k < nsteps; ++k)
+            for (int c = 0; c < cols; ++c) out[k * cols + c] = md->hEnergy[k * REC + c];
     }
     return finish(ctx, "md_run");
+}
+}  // namespace
+
+extern "C" {
+
+int mrmd_md_run(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* energies)
+{
+    return md_run(ctx, md, nsteps, energies, 2);
+}
+
+int mrmd_md_run_observed(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* records)
+{
+    if (md && !md->cfg.observe) return set_error(ctx, MRMD_ERR_STATE, "the stepper was created without observe");
+    return md_run(ctx, md, nsteps, records, REC);
 }
 
 int mrmd_md_get_state(mrmd_ctx* ctx, mrmd_md* md, double* pos3, double* vel3, double* force3)
@@ -509,7 +609,7 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
     if (!ctx || !md || (what != 0 && what != 1)) return MRMD_ERR_ARG;
     mrmd_atoms* a = &md->atoms;
     MRMD_TRY(ensure_energy(ctx, md, 1));
-    double* ev = md->dEnergy + 2 * (md->energyCap - 1);
+    double* ev = md->dEnergy + REC * (md->energyCap - 1);
     if (what == 1)
     {
         if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");

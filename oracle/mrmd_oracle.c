@@ -574,6 +574,45 @@ void orc_vv_post(orc_atoms* a, double dt)
     }
 }
 
+double orc_kinetic_energy(const orc_atoms* a)
+{
+    /* analysis/KineticEnergy.hpp:26-39 */
+    double velSqr = 0.0;
+    for (int64_t idx = 0; idx < a->numLocal; ++idx)
+    {
+        const double* v = &a->vel[3 * idx];
+        velSqr += a->mass[idx] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+    return 0.5 * velSqr;
+}
+
+void orc_system_momentum(const orc_atoms* a, double* out3)
+{
+    /* analysis/SystemMomentum.cpp:21-48: one reduction per component */
+    for (int d = 0; d < 3; ++d)
+    {
+        double sum = 0.0;
+        for (int64_t idx = 0; idx < a->numLocal; ++idx) sum += a->vel[3 * idx + d];
+        out3[d] = sum;
+    }
+}
+
+double orc_pressure(const orc_atoms* a, const orc_subdomain* sd)
+{
+    /* analysis/Pressure.cpp:23-51 */
+    double pressure = 0.0;
+    for (int64_t idx = 0; idx < a->numLocal + a->numGhost; ++idx)
+    {
+        const double* v = &a->vel[3 * idx];
+        const double* x = &a->pos[3 * idx];
+        const double* F = &a->force[3 * idx];
+        pressure += a->mass[idx] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        pressure += F[0] * x[0] + F[1] * x[1] + F[2] * x[2];
+    }
+    const double volume = sd->diameter[0] * sd->diameter[1] * sd->diameter[2];
+    return pressure / (3.0 * volume);
+}
+
 /* Philox4x32-10 as published by Salmon et al., "Parallel random numbers: as
  * easy as 1, 2, 3", SC'11: multipliers 0xD2511F53 / 0xCD9E8D57, Weyl key
  * increments 0x9E3779B9 / 0xBB67AE85. */

@@ -178,6 +178,17 @@ double orc_vv_pre(orc_atoms* atoms, double dt);
 /* VelocityVerlet::postForceIntegrate, action/VelocityVerlet.cpp:69-90 */
 void orc_vv_post(orc_atoms* atoms, double dt);
 
+/* ------------------------------------------------------------ analysis -- */
+/* analysis::getKineticEnergy (analysis/KineticEnergy.hpp:26-39):
+ * 0.5 * sum over local atoms of m (vx^2 + vy^2 + vz^2), serial in index order. */
+double orc_kinetic_energy(const orc_atoms* atoms);
+/* analysis::getSystemMomentum (analysis/SystemMomentum.cpp:21-48): the sum
+ * of the local atoms' velocities per component (no mass factor). */
+void orc_system_momentum(const orc_atoms* atoms, double* out3);
+/* analysis::getPressure (analysis/Pressure.cpp:23-51): sum over local AND
+ * ghost atoms of m v.v + F.x, divided by 3 * subdomain volume. */
+double orc_pressure(const orc_atoms* atoms, const orc_subdomain* sd);
+
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), key (k0,k1), counter c[4]. */
 void orc_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 /* Standard normal pair from one Philox block (Box-Muller). */

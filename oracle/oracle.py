@@ -129,6 +129,11 @@ def lib():
         L.orc_vv_pre.argtypes = [C.POINTER(AtomsS), C.c_double]
         L.orc_vv_pre.restype = C.c_double
         L.orc_vv_post.argtypes = [C.POINTER(AtomsS), C.c_double]
+        L.orc_kinetic_energy.argtypes = [C.POINTER(AtomsS)]
+        L.orc_kinetic_energy.restype = C.c_double
+        L.orc_system_momentum.argtypes = [C.POINTER(AtomsS), c_double_p]
+        L.orc_pressure.argtypes = [C.POINTER(AtomsS), C.POINTER(Subdomain)]
+        L.orc_pressure.restype = C.c_double
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32)]
         L.orc_normal_from_counter.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, c_double_p]
@@ -405,6 +410,23 @@ def vv_pre(atoms: Atoms, dt):
 def vv_post(atoms: Atoms, dt):
     s = atoms.s()
     lib().orc_vv_post(C.byref(s), float(dt))
+
+
+def kinetic_energy(atoms: Atoms):
+    s = atoms.s()
+    return lib().orc_kinetic_energy(C.byref(s))
+
+
+def system_momentum(atoms: Atoms):
+    s = atoms.s()
+    out = np.zeros(3)
+    lib().orc_system_momentum(C.byref(s), _p(out))
+    return out
+
+
+def pressure(atoms: Atoms, sd: Subdomain):
+    s = atoms.s()
+    return lib().orc_pressure(C.byref(s), C.byref(sd))
 
 
 def philox(ctr, key):

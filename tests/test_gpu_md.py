@@ -28,8 +28,10 @@ def mb_velocities(n, T, seed):
     return v
 
 
-def oracle_run(orc, pos, vel, L, nsteps, rc=2.5, skin=0.3, dt=0.005, K=10):
-    """examples/02_LennardJones_NVE.cpp:135-216 with a fixed rebuild interval."""
+def oracle_run(orc, pos, vel, L, nsteps, rc=2.5, skin=0.3, dt=0.005, K=10, observe=False):
+    """examples/02_LennardJones_NVE.cpp:135-216 with a fixed rebuild interval.
+    observe: each energy row also holds getKineticEnergy and getSystemMomentum
+    after the step."""
     sd = orc.subdomain([0, 0, 0], [L] * 3, rc + skin)
     a = orc.Atoms.from_positions(pos, capacity=len(pos) * 4)
     a.vel[: len(pos)] = vel
@@ -56,7 +58,10 @@ def oracle_run(orc, pos, vel, L, nsteps, rc=2.5, skin=0.3, dt=0.005, K=10):
         E, W = orc.lj_apply(tab, rc * rc, a, co, no)
         orc.ghost_to_real(a, corr)
         orc.vv_post(a, dt)
-        energies.append((E, W))
+        if observe:
+            energies.append((E, W, orc.kinetic_energy(a), *orc.system_momentum(a)))
+        else:
+            energies.append((E, W))
     n = len(pos)
     return a.pos[:n].copy(), a.vel[:n].copy(), a.force[:n].copy(), np.array(energies)
 

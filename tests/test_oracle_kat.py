@@ -432,3 +432,27 @@ def test_normal_generator_accuracy_and_moments(orc):
     assert np.all(np.abs(v.mean(axis=0)) < 0.03)
     assert np.all(np.abs(v.var(axis=0) - 1.0) < 0.03)
     assert np.all(np.abs((v ** 4).mean(axis=0) / v.var(axis=0) ** 2 - 3.0) < 0.15)
+
+
+def test_analysis_kats(orc):
+    """analysis/KineticEnergy.test.cpp:22-50 and SystemMomentum.test.cpp:22-45,
+    and getPressure (analysis/Pressure.cpp:23-51) on a hand-computed case."""
+    a = orc.Atoms(3)
+    a.vel[:3] = [[2, 0, 0], [-0.0, -8, -0.0], [0, 0, 16]]
+    a.mass[:3] = [1.0, 2.0, 0.5]
+    a.numLocal = 3
+    expect_float_eq(orc.kinetic_energy(a), (4 + 2 * 64 + 0.5 * 256) * 0.5)
+    b = orc.Atoms(2)
+    b.vel[:2] = [[2, 3, 4], [-4, -8, -16]]
+    b.numLocal = 2
+    for got, want in zip(orc.system_momentum(b), (-2, -5, -12)):
+        expect_float_eq(got, want)
+    # pressure: one local and one ghost atom, volume 2 * 3 * 4
+    c = orc.Atoms(2)
+    c.pos[:2] = [[1, 2, 3], [0.5, 0, 0]]
+    c.vel[:2] = [[1, 0, 0], [0, 2, 0]]
+    c.force[:2] = [[1, 1, 1], [4, 0, 0]]
+    c.mass[:2] = [2.0, 1.0]
+    c.numLocal, c.numGhost = 1, 1
+    sd = orc.subdomain([0, 0, 0], [2, 3, 4], 0.5)
+    assert orc.pressure(c, sd) == (2.0 + 6.0 + 4.0 + 2.0) / (3 * 24.0)
