@@ -68,7 +68,8 @@ def test_observables_vs_oracle(M, orc, n_local, n_ghost):
 def test_fused_step_observables_match_oracle(M, orc, graph):
     """Kinetic energy and momentum recorded inside the FP64 step equal the
     oracle loop's getKineticEnergy / getSystemMomentum after every step, and the
-    LJ energy / virial columns equal those of the stepper without recording."""
+    LJ energy / virial columns equal those of the stepper without recording
+    (to the last bits of the energy sum)."""
     pos, L = fcc(6)
     rng = np.random.default_rng(5)
     pos = pos + rng.normal(0, 0.02, pos.shape)
@@ -79,7 +80,8 @@ def test_fused_step_observables_match_oracle(M, orc, graph):
     rec = np.vstack([s.run_observed(10), s.run_observed(steps - 10)])
     plain = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64, use_graph=graph)
     e = np.vstack([plain.run(10), plain.run(steps - 10)])
-    np.testing.assert_array_equal(rec[:, :2], e)
+    # (the FP64 pair kernel adds block energies with atomics: order-dependent last bits)
+    np.testing.assert_allclose(rec[:, :2], e, rtol=1e-13)
     np.testing.assert_allclose(rec[:, :2], eo[:, :2], rtol=1e-10, atol=1e-9)
     np.testing.assert_allclose(rec[:, 2], eo[:, 2], rtol=1e-10)
     assert np.abs(rec[:, 3:] - eo[:, 3:]).max() <= 1e-10 * np.abs(vel).sum()
