@@ -343,6 +343,26 @@ int mrmd_ljig_get_compensation(mrmd_ctx* ctx, const mrmd_ljig* s, double* mean, 
                                double* counter, int64_t* runCounter);
 int mrmd_ljig_set_compensation(mrmd_ctx* ctx, mrmd_ljig* s, const double* mean);
 
+/* --------------------------------------------------------- Coulomb DSF -- */
+/* impl::CoulombDSF (action/CoulombDSF.hpp:39-83): damped shifted force
+ * Coulomb, pair function with util::approxErfc (util/math.hpp:57-76). */
+typedef struct {
+    double alpha, rc, rcSqr, forceShift, energyShift;
+} mrmd_coulomb_dsf_params;
+/* CoulombDSF(rc, alpha) (CoulombDSF.hpp:76-83): the shifts, with the exact erfc. */
+int mrmd_coulomb_dsf_init(mrmd_coulomb_dsf_params* out, double rc, double alpha);
+/* computeForce / computeEnergy (CoulombDSF.hpp:52-74) evaluated on the device
+ * for n (distSqr, q1, q2) host triples; force is the reference's
+ * force / distSqr factor. */
+int mrmd_coulomb_dsf_eval(mrmd_ctx* ctx, const mrmd_coulomb_dsf_params* c, int64_t n,
+                          const double* distSqr, const double* q1, const double* q2,
+                          double* force, double* energy);
+/* The pair force on a half list with the atoms' charges, in the loop of
+ * LennardJones::apply (action/LennardJones.hpp:135-206): forces added to i
+ * and j (ghosts included), energy and virial (-1/2 sum ff r^2) summed. */
+int mrmd_coulomb_dsf_apply(mrmd_ctx* ctx, const mrmd_coulomb_dsf_params* c, mrmd_atoms* a,
+                           const mrmd_nlist* nl, double* energy, double* virial);
+
 /* ------------------------------------------------------------ analysis -- */
 /* Deterministic device sums (fixed grid and order; same bits on every run). */
 /* analysis::getKineticEnergy (analysis/KineticEnergy.hpp:26-39): 0.5 sum m v.v

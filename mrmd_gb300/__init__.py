@@ -411,6 +411,51 @@ class LennardJones:
             pass
 
 
+class CoulombDSF:
+    """impl::CoulombDSF (action/CoulombDSF.hpp:39-83) with a half-list pair force."""
+
+    def __init__(self, rc, alpha, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.c = _abi.CoulombDSFS()
+        rc_ = self.ctx.lib.mrmd_coulomb_dsf_init(C.byref(self.c), float(rc), float(alpha))
+        if rc_ != 0:
+            raise MrmdError(rc_, "CoulombDSF: rc and alpha must be > 0")
+        self.energy = self.virial = 0.0
+
+    def _eval(self, dist_sqr, q1, q2):
+        d, a, b = np.broadcast_arrays(np.asarray(dist_sqr, dtype=np.float64), np.asarray(q1, dtype=np.float64),
+                                      np.asarray(q2, dtype=np.float64))
+        shape = d.shape
+        d, a, b = (np.ascontiguousarray(x).ravel() for x in (d, a, b))
+        f, e = np.zeros(d.size), np.zeros(d.size)
+        self.ctx.check(self.ctx.lib.mrmd_coulomb_dsf_eval(self.ctx.h, C.byref(self.c), d.size, _dp(d), _dp(a),
+                                                          _dp(b), _dp(f), _dp(e)), "CoulombDSF")
+        return f.reshape(shape), e.reshape(shape)
+
+    def computeForce(self, dist_sqr, q1, q2):
+        """Force / distSqr, evaluated on the device (scalars or arrays)."""
+        f = self._eval(dist_sqr, q1, q2)[0]
+        return float(f) if f.ndim == 0 else f
+
+    def computeEnergy(self, dist_sqr, q1, q2):
+        e = self._eval(dist_sqr, q1, q2)[1]
+        return float(e) if e.ndim == 0 else e
+
+    def apply(self, atoms: Atoms, verlet_list: "HalfVerletList"):
+        E, W = C.c_double(), C.c_double()
+        self.ctx.check(self.ctx.lib.mrmd_coulomb_dsf_apply(self.ctx.h, C.byref(self.c), C.byref(atoms.s),
+                                                           C.byref(verlet_list.s), C.byref(E), C.byref(W)),
+                       "CoulombDSF.apply")
+        self.energy, self.virial = E.value, W.value
+        return self.energy
+
+    def getEnergy(self):
+        return self.energy
+
+    def getVirial(self):
+        return self.virial
+
+
 class VelocityVerlet:
     """action::VelocityVerlet (action/VelocityVerlet.hpp:26-31)."""
 

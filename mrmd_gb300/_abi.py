@@ -81,6 +81,10 @@ class SlabS(C.Structure):
                 ("interfaceType", C.c_int32), ("pad", C.c_int32)]
 
 
+class CoulombDSFS(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("alpha", "rc", "rcSqr", "forceShift", "energyShift")]
+
+
 class MDConfigS(C.Structure):
     _fields_ = [("boxMin", C.c_double * 3), ("boxMax", C.c_double * 3), ("rc", C.c_double),
                 ("skin", C.c_double), ("sigma", C.c_double), ("epsilon", C.c_double),
@@ -222,6 +226,10 @@ SIGNATURES = {
     "mrmd_md_destroy": (_i, [_v, _v]),
     "mrmd_md_run": (_i, [_v, _v, _i64, c_double_p]),
     "mrmd_md_run_observed": (_i, [_v, _v, _i64, c_double_p]),
+    "mrmd_coulomb_dsf_init": (_i, [P(CoulombDSFS), _d, _d]),
+    "mrmd_coulomb_dsf_eval": (_i, [_v, P(CoulombDSFS), _i64, c_double_p, c_double_p, c_double_p, c_double_p,
+                                   c_double_p]),
+    "mrmd_coulomb_dsf_apply": (_i, [_v, P(CoulombDSFS), P(AtomsS), P(NListS), c_double_p, c_double_p]),
     "mrmd_kinetic_energy": (_i, [_v, P(AtomsS), c_double_p]),
     "mrmd_system_momentum": (_i, [_v, P(AtomsS), c_double_p]),
     "mrmd_pressure": (_i, [_v, P(AtomsS), P(SubdomainS), c_double_p]),

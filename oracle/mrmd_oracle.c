@@ -211,6 +211,95 @@ void orc_lj_apply(const orc_lj_params* table, int64_t numTypesIndex, double rcSq
     *virialOut = virial;
 }
 
+/* -------------------------------------------------------- Coulomb DSF --- */
+
+#define ORC_INV_SQRTPI 0.56418958354775628695 /* 1 / sqrt(pi) */
+#define ORC_COULOMB_PREFACTOR 138.935458       /* CoulombDSF.hpp:57 */
+
+double orc_approx_erfc(double x, double* expX2)
+{
+    /* util/math.hpp:57-70: erfc(x) ~ t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-x^2),
+     * t = 1 / (1 + p x) (Abramowitz & Stegun 7.1.26) */
+    const double p = 0.3275911;
+    const double a1 = 0.254829592;
+    const double a2 = -0.284496736;
+    const double a3 = 1.421413741;
+    const double a4 = -1.453152027;
+    const double a5 = 1.061405429;
+    double t = 1.0 / (1.0 + p * x);
+    *expX2 = exp(-x * x);
+    return t * (a1 + t * (a2 + t * (a3 + t * (a4 + t * a5)))) * *expX2;
+}
+
+void orc_coulomb_dsf_init(orc_coulomb_dsf* c, double rc, double alpha)
+{
+    /* CoulombDSF.hpp:76-83 (exact erfc for the shifts) */
+    c->alpha = alpha;
+    c->rc = rc;
+    c->rcSqr = rc * rc;
+    double e = erfc(alpha * rc);
+    double x = exp(-alpha * alpha * c->rcSqr);
+    c->forceShift = -(e / c->rcSqr + 2.0 * ORC_INV_SQRTPI * alpha * x / rc);
+    c->energyShift = e / rc;
+}
+
+double orc_coulomb_dsf_force(const orc_coulomb_dsf* c, double distSqr, double q1, double q2)
+{
+    /* CoulombDSF.hpp:52-62 (eq 16), divided by r^2 as the reference returns it */
+    double r = sqrt(distSqr);
+    double prefac = ORC_COULOMB_PREFACTOR * q1 * q2;
+    double expX2;
+    double e = orc_approx_erfc(c->alpha * r, &expX2);
+    double force = prefac * (e / r + 2.0 * c->alpha * ORC_INV_SQRTPI * expX2 + r * c->forceShift);
+    return force / distSqr;
+}
+
+double orc_coulomb_dsf_energy(const orc_coulomb_dsf* c, double distSqr, double q1, double q2)
+{
+    /* CoulombDSF.hpp:64-74 (eq 15) */
+    double r = sqrt(distSqr);
+    double prefac = ORC_COULOMB_PREFACTOR * q1 * q2;
+    double expX2;
+    double e = orc_approx_erfc(c->alpha * r, &expX2);
+    return prefac * (e / r - c->energyShift - c->forceShift * (r - c->rc));
+}
+
+void orc_coulomb_dsf_apply(const orc_coulomb_dsf* c, orc_atoms* atoms, const int32_t* counts,
+                           const int32_t* nbrs, int64_t cap, double* energyOut, double* virialOut)
+{
+    double* pos = atoms->pos;
+    double* force = atoms->force;
+    const double* q = atoms->charge;
+    double energy = 0.0, virial = 0.0;
+    for (int64_t idx = 0; idx < atoms->numLocal; ++idx)
+    {
+        double forceTmp[3] = {0.0, 0.0, 0.0};
+        for (int64_t k = 0; k < counts[idx]; ++k)
+        {
+            int64_t jdx = nbrs[idx * cap + k];
+            double dx = pos[3 * idx + 0] - pos[3 * jdx + 0];
+            double dy = pos[3 * idx + 1] - pos[3 * jdx + 1];
+            double dz = pos[3 * idx + 2] - pos[3 * jdx + 2];
+            double distSqr = dx * dx + dy * dy + dz * dz;
+            if (distSqr > c->rcSqr) continue;
+            double ff = orc_coulomb_dsf_force(c, distSqr, q[idx], q[jdx]);
+            energy += orc_coulomb_dsf_energy(c, distSqr, q[idx], q[jdx]);
+            virial -= 0.5 * ff * distSqr;
+            forceTmp[0] += dx * ff;
+            forceTmp[1] += dy * ff;
+            forceTmp[2] += dz * ff;
+            force[3 * jdx + 0] -= dx * ff;
+            force[3 * jdx + 1] -= dy * ff;
+            force[3 * jdx + 2] -= dz * ff;
+        }
+        force[3 * idx + 0] += forceTmp[0];
+        force[3 * idx + 1] += forceTmp[1];
+        force[3 * idx + 2] += forceTmp[2];
+    }
+    *energyOut = energy;
+    *virialOut = virial;
+}
+
 /* -------------------------------------------------------- ghost layer --- */
 
 void orc_map_into_domain(orc_atoms* atoms, const orc_subdomain* sd)

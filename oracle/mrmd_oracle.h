@@ -178,6 +178,23 @@ double orc_vv_pre(orc_atoms* atoms, double dt);
 /* VelocityVerlet::postForceIntegrate, action/VelocityVerlet.cpp:69-90 */
 void orc_vv_post(orc_atoms* atoms, double dt);
 
+/* --------------------------------------------------------- Coulomb DSF -- */
+/* impl::CoulombDSF (action/CoulombDSF.hpp:39-83): damped shifted force
+ * Coulomb (Fennell & Gezelter; DOI 10.1140/epjst/e2016-60151-6, eqs 15-16),
+ * with util::approxErfc (util/math.hpp:57-76, Abramowitz & Stegun 7.1.26). */
+typedef struct {
+    double alpha, rc, rcSqr, forceShift, energyShift;
+} orc_coulomb_dsf;
+
+void orc_coulomb_dsf_init(orc_coulomb_dsf* c, double rc, double alpha);
+double orc_approx_erfc(double x, double* expX2);
+double orc_coulomb_dsf_force(const orc_coulomb_dsf* c, double distSqr, double q1, double q2);
+double orc_coulomb_dsf_energy(const orc_coulomb_dsf* c, double distSqr, double q1, double q2);
+/* The half-list loop of LennardJones::apply (action/LennardJones.hpp:135-206)
+ * with the DSF pair function and the atoms' charges (cutoff rc). */
+void orc_coulomb_dsf_apply(const orc_coulomb_dsf* c, orc_atoms* atoms, const int32_t* counts,
+                           const int32_t* nbrs, int64_t cap, double* energyOut, double* virialOut);
+
 /* ------------------------------------------------------------ analysis -- */
 /* analysis::getKineticEnergy (analysis/KineticEnergy.hpp:26-39):
  * 0.5 * sum over local atoms of m (vx^2 + vy^2 + vz^2), serial in index order. */

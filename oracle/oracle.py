@@ -55,6 +55,10 @@ class LJParams(C.Structure):
         "cappingCoeff", "shift", "energyAtCappingPoint")]
 
 
+class CoulombDSFS(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("alpha", "rc", "rcSqr", "forceShift", "energyShift")]
+
+
 class Pred(C.Structure):
     _fields_ = [("kind", C.c_int32), ("axis", C.c_int32), ("center", C.c_double),
                 ("slabMin", C.c_double), ("slabMax", C.c_double), ("tolerance", C.c_double)]
@@ -129,6 +133,14 @@ def lib():
         L.orc_vv_pre.argtypes = [C.POINTER(AtomsS), C.c_double]
         L.orc_vv_pre.restype = C.c_double
         L.orc_vv_post.argtypes = [C.POINTER(AtomsS), C.c_double]
+        L.orc_coulomb_dsf_init.argtypes = [C.POINTER(CoulombDSFS), C.c_double, C.c_double]
+        L.orc_approx_erfc.argtypes = [C.c_double, c_double_p]
+        L.orc_approx_erfc.restype = C.c_double
+        for f in ("orc_coulomb_dsf_force", "orc_coulomb_dsf_energy"):
+            getattr(L, f).argtypes = [C.POINTER(CoulombDSFS), C.c_double, C.c_double, C.c_double]
+            getattr(L, f).restype = C.c_double
+        L.orc_coulomb_dsf_apply.argtypes = [C.POINTER(CoulombDSFS), C.POINTER(AtomsS), c_int32_p,
+                                            c_int32_p, C.c_int64, c_double_p, c_double_p]
         L.orc_kinetic_energy.argtypes = [C.POINTER(AtomsS)]
         L.orc_kinetic_energy.restype = C.c_double
         L.orc_system_momentum.argtypes = [C.POINTER(AtomsS), c_double_p]
@@ -410,6 +422,34 @@ def vv_pre(atoms: Atoms, dt):
 def vv_post(atoms: Atoms, dt):
     s = atoms.s()
     lib().orc_vv_post(C.byref(s), float(dt))
+
+
+class CoulombDSF:
+    """impl::CoulombDSF (action/CoulombDSF.hpp:39-83)."""
+
+    def __init__(self, rc, alpha):
+        self.c = CoulombDSFS()
+        lib().orc_coulomb_dsf_init(C.byref(self.c), float(rc), float(alpha))
+
+    def computeForce(self, dist_sqr, q1, q2):
+        return lib().orc_coulomb_dsf_force(C.byref(self.c), float(dist_sqr), float(q1), float(q2))
+
+    def computeEnergy(self, dist_sqr, q1, q2):
+        return lib().orc_coulomb_dsf_energy(C.byref(self.c), float(dist_sqr), float(q1), float(q2))
+
+    def apply(self, atoms: Atoms, counts, nbrs):
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        nbrs = np.ascontiguousarray(nbrs, dtype=np.int32)
+        s = atoms.s()
+        E, W = C.c_double(), C.c_double()
+        lib().orc_coulomb_dsf_apply(C.byref(self.c), C.byref(s), _p(counts, c_int32_p), _p(nbrs, c_int32_p),
+                                    nbrs.shape[1] if nbrs.ndim == 2 else 1, C.byref(E), C.byref(W))
+        return E.value, W.value
+
+
+def approx_erfc(x):
+    e = C.c_double()
+    return lib().orc_approx_erfc(float(x), C.byref(e))
 
 
 def kinetic_energy(atoms: Atoms):
