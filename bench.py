@@ -702,8 +702,9 @@ def main():
     st = sysm.stats()
     nbar = st["pairs"] / n
     if head == "mixed":
-        bytes_per_atom = 32 + 24 + 4 * (1 + nbar)  # split coords read, F written, full list
-        kname = "lj_mixed_full"
+        # split coords read, F written, full list in near and far rows (two counts)
+        bytes_per_atom = 32 + 24 + 4 * (2 + nbar)
+        kname = "lj_mixed_split"
     else:
         bytes_per_atom = 24 + 24 + 4 * (1 + nbar)  # positions read, F written, half list
         kname = "lj_fp64"

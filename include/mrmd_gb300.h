@@ -479,14 +479,16 @@ int mrmd_md_run_observed(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps, double* rec
 int mrmd_md_get_state(mrmd_ctx* ctx, mrmd_md* md, double* pos3, double* vel3, double* force3);
 /* Replace positions/velocities (original order) and force a rebuild. */
 int mrmd_md_set_state(mrmd_ctx* ctx, mrmd_md* md, const double* pos3, const double* vel3);
-/* Counters: [0] steps, [1] rebuilds, [2] list pairs, [3] ghosts, [4] list capacity. */
+/* Counters: [0] steps, [1] rebuilds, [2] list pairs, [3] ghosts, [4] list
+ * capacity (near + far rows for the mixed form). */
 int mrmd_md_stats(const mrmd_md* md, int64_t* out5);
 /* what = 0: forces of the current positions (rebuilding ghosts and list when
  * the state was replaced), energy/virial into ev2 (host, may be NULL);
  * what = 1: launch only the pair-force kernel on the current list and split
  * coordinates, asynchronously (for timing the kernel alone). */
 int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2);
-/* Access to the internal atoms / list for profiling and tests. */
+/* Access to the internal atoms / list for profiling and tests (the mixed
+ * form's list is split by distance; this is its near part). */
 const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md);
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
 

@@ -177,7 +177,117 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
         atomicAdd(ev + 1, w);
     }
 }
+// Full list split into near and far rows: the near rows (pairs closer than
+// r_split + skin at the rebuild) take the double-float path unless the pair
+// has since moved beyond r_split; the far rows take the FP32 path unless it
+// has come closer.  Per-lane decisions keep every pair on the right path;
+// the split only keeps the warps' lanes on the same path.
+template <bool ACCUM>
+__global__ void __launch_bounds__(MX_TB) k_lj_mixed_split(
+    const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
+    RcSq rc2, float rsplitSq, const int32_t* __restrict__ countsN, const int32_t* __restrict__ nbrsN, int64_t capN,
+    const int32_t* __restrict__ countsF, const int32_t* __restrict__ nbrsF, int64_t capF, int64_t n,
+    double* __restrict__ ev)
+{
+    __shared__ double red[64];
+    Acc acc;
+    FarAcc fa;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const float4 hi_i = hi[i], lo_i = lo[i];
+        {
+            const int32_t cnt = countsN[i];
+            const int32_t* __restrict__ col = nbrsN + mrmd_dev::nbr_row(i, capN);
+            for (int32_t k = 0; k < cnt; ++k)
+            {
+                const int32_t j = __ldg(col + 32 * (int64_t)k);
+                const float4 h = __ldg(hi + j), l = __ldg(lo + j);
+                if (pair_far(hi_i, lo_i, h, l, p, rc2, rsplitSq, fa) == 2)
+                {
+                    PairMixed q;
+                    if (pair_mixed(hi_i, lo_i, h, l, p, rc2, q)) acc.add(q);
+                }
+            }
+        }
+        {
+            const int32_t cnt = countsF[i];
+            const int32_t* __restrict__ col = nbrsF + mrmd_dev::nbr_row(i, capF);
+            int32_t k = 0;
+            for (; k + 1 < cnt; k += 2)
+            {
+                const int32_t j0 = __ldg(col + 32 * (int64_t)k);
+                const int32_t j1 = __ldg(col + 32 * (int64_t)(k + 1));
+                const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
+                const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
+                if (pair_far(hi_i, lo_i, h0, l0, p, rc2, rsplitSq, fa) == 2)
+                {
+                    PairMixed q;
+                    if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
+                }
+                if (pair_far(hi_i, lo_i, h1, l1, p, rc2, rsplitSq, fa) == 2)
+                {
+                    PairMixed q;
+                    if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, q)) acc.add(q);
+                }
+            }
+            if (k < cnt)
+            {
+                const int32_t j0 = __ldg(col + 32 * (int64_t)k);
+                const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
+                if (pair_far(hi_i, lo_i, h0, l0, p, rc2, rsplitSq, fa) == 2)
+                {
+                    PairMixed q;
+                    if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
+                }
+            }
+        }
+        df_acc(acc.fx, fa.fx);
+        df_acc(acc.fy, fa.fy);
+        df_acc(acc.fz, fa.fz);
+        df_acc(acc.e, fa.e);
+        df_acc(acc.w, fa.w);
+        double4 f = make_double4((double)acc.fx.h + (double)acc.fx.l, (double)acc.fy.h + (double)acc.fy.l,
+                                 (double)acc.fz.h + (double)acc.fz.l, 0.0);
+        if (ACCUM)
+        {
+            const double4 o = force[i];
+            f.x += o.x;
+            f.y += o.y;
+            f.z += o.z;
+        }
+        force[i] = f;
+    }
+    double e = 0.5 * ((double)acc.e.h + (double)acc.e.l), w = 0.5 * ((double)acc.w.h + (double)acc.w.l);
+    mrmd_dev::block_sum2(e, w, red);
+    if (threadIdx.x == 0)
+    {
+        atomicAdd(ev + 0, e);
+        atomicAdd(ev + 1, w);
+    }
+}
 }  // namespace
+
+int lj_mixed_split(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
+                   double rsplit, const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate)
+{
+    const int64_t n = nearList->rows;
+    if (n == 0) return MRMD_OK;
+    const unsigned grid = (unsigned)div_up(n, MX_TB);
+    const RcSq rc2 = make_rcsq(rcSqr);
+    const float rsplitSq = (float)(rsplit * rsplit);
+#define SPLIT_LAUNCH(A)                                                                                              \
+    k_lj_mixed_split<A><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,         \
+                                                         rsplitSq, nearList->counts, nearList->nbrs,                 \
+                                                         nearList->maxNeighbors, farList->counts, farList->nbrs,     \
+                                                         farList->maxNeighbors, n, ev)
+    if (accumulate)
+        SPLIT_LAUNCH(true);
+    else
+        SPLIT_LAUNCH(false);
+#undef SPLIT_LAUNCH
+    return after_launch(ctx, "lj_mixed_split");
+}
 
 int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
                   const mrmd_nlist* nl, double* ev, bool accumulate)

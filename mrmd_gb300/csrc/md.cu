@@ -147,7 +147,9 @@ struct mrmd_md
     mrmd_atoms atoms{};
     mrmd_atoms shadow{};
     mrmd_ghost_layer ghosts{};
-    mrmd_nlist list{};
+    mrmd_nlist list{};           // FP64: half list; mixed: near rows of the split full list
+    mrmd_nlist farList{};        // mixed: far rows of the split full list
+    double rsplit = 0;           // mixed: pairs beyond it are evaluated in FP32
     mrmd_lj* lj = nullptr;
     CellList sortCells;
     CellGrid grid{};
@@ -197,8 +199,20 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
     const int64_t nAll = a->numLocal + a->numGhost;
     const bool full = md->cfg.precision == MRMD_PREC_MIXED;
     const double rlist = md->cfg.rc + md->cfg.skin;
-    MRMD_TRY(build_half_list(ctx, &md->list, a->pos, nAll, 0, a->numLocal, rlist, md->grid,
-                             md->list.maxNeighbors > 0 ? md->list.maxNeighbors : md->cfg.maxNeighbors, full));
+    if (full)
+    {
+        // near rows: closer than r_split + skin, so that no far pair can come
+        // within r_split before the next rebuild (displacement < skin / 2)
+        if (md->farList.maxNeighbors == 0) md->farList.maxNeighbors = md->cfg.maxNeighbors;
+        MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
+                                  md->rsplit + md->cfg.skin, md->grid));
+        MRMD_TRY(list_total_pairs(ctx, &md->farList));
+    }
+    else
+    {
+        MRMD_TRY(build_half_list(ctx, &md->list, a->pos, nAll, 0, a->numLocal, rlist, md->grid,
+                                 md->list.maxNeighbors > 0 ? md->list.maxNeighbors : md->cfg.maxNeighbors, false));
+    }
     MRMD_TRY(list_total_pairs(ctx, &md->list));
     if (full && nAll > md->splitCap)
     {
@@ -222,8 +236,8 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
     {
         const int64_t nAll = a->numLocal + a->numGhost;
         MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + md->splitCap));
-        return lj_mixed_full(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
-                             &md->list, ev, false);
+        return lj_mixed_split(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
+                              md->rsplit, &md->list, &md->farList, ev, false);
     }
     MRMD_TRY(lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev));
     return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
@@ -368,6 +382,8 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     if (rc == MRMD_OK) rc = mrmd_atoms_alloc(ctx, &md->shadow, cap);
     if (rc == MRMD_OK) rc = mrmd_ghost_layer_alloc(ctx, &md->ghosts, cap);
     if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->list);
+    if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->farList);
+    md->rsplit = lj_split_radius(cfg->sigma, cfg->cappingDistance);
     if (rc == MRMD_OK)
     {
         const double c = cfg->cappingDistance, r = cfg->rc, s = cfg->sigma, e = cfg->epsilon;
@@ -411,6 +427,7 @@ int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md)
     mrmd_atoms_free(ctx, &md->shadow);
     mrmd_ghost_layer_free(ctx, &md->ghosts);
     mrmd_nlist_free(ctx, &md->list);
+    mrmd_nlist_free(ctx, &md->farList);
     mrmd_lj_destroy(ctx, md->lj);
     md->sortCells.release();
     dfree(md->orig);
@@ -598,9 +615,9 @@ int mrmd_md_stats(const mrmd_md* md, int64_t* out5)
     if (!md || !out5) return MRMD_ERR_ARG;
     out5[0] = md->steps;
     out5[1] = md->rebuilds;
-    out5[2] = md->list.totalPairs;
+    out5[2] = md->list.totalPairs + (md->cfg.precision == MRMD_PREC_MIXED ? md->farList.totalPairs : 0);
     out5[3] = md->atoms.numGhost;
-    out5[4] = md->list.maxNeighbors;
+    out5[4] = md->list.maxNeighbors + (md->cfg.precision == MRMD_PREC_MIXED ? md->farList.maxNeighbors : 0);
     return MRMD_OK;
 }
 
@@ -614,8 +631,8 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
     {
         if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
         if (md->cfg.precision == MRMD_PREC_MIXED)
-            return lj_mixed_full(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
-                                 &md->list, ev, false);
+            return lj_mixed_split(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
+                                  md->rsplit, &md->list, &md->farList, ev, false);
         return lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev);
     }
     const int oldSync = ctx->sync;

@@ -104,12 +104,18 @@ __device__ __forceinline__ bool lex_above(const double4& pi, const double4& pj)
     return (pj.x > pi.x) || ((pj.x == pi.x) && ((pj.y > pi.y) || ((pj.y == pi.y) && (pj.z > pi.z))));
 }
 
-template <bool FULL>
+// SPLIT (full lists only): pairs with an FP32 distance below sqrt(nearSqF)
+// go to the first list, the others to the second (`capFar`, `countsFar`,
+// `nbrsFar`, overflow in maxCount[1]).  The split is a placement choice, not
+// a cutoff: every kept pair is in exactly one of the two lists.
+template <bool FULL, bool SPLIT = false>
 __global__ void __launch_bounds__(128) k_build_list(
     const double4* __restrict__ pos, const int32_t* __restrict__ cellOf,
     const int32_t* __restrict__ cellStart, const float4* __restrict__ spos, CellGrid g,
     int64_t begin, int64_t end, double rsq, float rsqLo, float rsqHi, int64_t cap,
-    int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount)
+    int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount,
+    float nearSqF = 0.0f, int64_t capFar = 0, int32_t* __restrict__ countsFar = nullptr,
+    int32_t* __restrict__ nbrsFar = nullptr)
 {
     for (int64_t i = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < end;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(128) k_build_list(
         const int cz = ci % g.n.z;
         const int cy = (ci / g.n.z) % g.n.y;
         const int cx = ci / (g.n.z * g.n.y);
-        int32_t cnt = 0;
+        int32_t cnt = 0, cntFar = 0;
         const int64_t row = i - begin;
         const int axEnd = min(cx + 1, g.n.x - 1);
         const int az0 = max(cz - 1, 0), az1 = min(cz + 1, g.n.z - 1);
@@ -157,6 +163,12 @@ __global__ void __launch_bounds__(128) k_build_list(
                             keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
                         }
                         if (!keep) continue;
+                        if (SPLIT && d2f >= nearSqF)
+                        {
+                            if (cntFar < capFar) nbrsFar[mrmd_dev::nbr_row(row, capFar) + 32 * (int64_t)cntFar] = j;
+                            ++cntFar;
+                            continue;
+                        }
                         if (cnt < cap) nbrs[mrmd_dev::nbr_row(row, cap) + 32 * (int64_t)cnt] = j;
                         ++cnt;
                     }
@@ -165,6 +177,11 @@ __global__ void __launch_bounds__(128) k_build_list(
         }
         counts[row] = cnt < cap ? cnt : (int32_t)cap;
         if (cnt > cap) atomicMax(maxCount, cnt);
+        if (SPLIT)
+        {
+            countsFar[row] = cntFar < capFar ? cntFar : (int32_t)capFar;
+            if (cntFar > capFar) atomicMax(maxCount + 1, cntFar);
+        }
     }
 }
 
@@ -313,6 +330,50 @@ __global__ void k_count_sum(const int32_t* __restrict__ counts, int64_t n, unsig
         s += (unsigned long long)counts[i];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
+                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid)
+{
+    CellList* cl = static_cast<CellList*>(nearList->cells);
+    MRMD_TRY(cl->build(ctx, pos4, nPos, grid));
+    const int64_t rows = end - begin;
+    // the same FP32 error band as build_half_list
+    const double delta = std::ldexp(grid.extent, -22);
+    const double band = 6.0 * rlist * delta + 3.0 * delta * delta + std::ldexp(rlist * rlist, -20);
+    const double rsq = rlist * rlist;
+    const float rsqLo = (float)std::fmax(0.0, (rsq - 2.0 * band) * (1.0 - 1e-6));
+    const float rsqHi = (float)((rsq + 2.0 * band) * (1.0 + 1e-6));
+    const float nearSqF = (float)(rnear * rnear);
+    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
+    int64_t capN = nearList->maxNeighbors > 0 ? nearList->maxNeighbors : 32;
+    int64_t capF = farList->maxNeighbors > 0 ? farList->maxNeighbors : 64;
+    for (int attempt = 0; attempt < 4; ++attempt)
+    {
+        MRMD_TRY(ensure_list_storage(ctx, nearList, rows, capN));
+        MRMD_TRY(ensure_list_storage(ctx, farList, rows, capF));
+        MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 2 * sizeof(int32_t), ctx->stream));
+        if (rows > 0)
+        {
+            k_build_list<true, true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
+                reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin, end,
+                rsq, rsqLo, rsqHi, capN, nearList->counts, nearList->nbrs, maxCount, nearSqF, capF,
+                farList->counts, farList->nbrs);
+            MRMD_TRY(after_launch(ctx, "build_split_list"));
+        }
+        int32_t hMax[2] = {0, 0};
+        MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hMax[0] <= capN && hMax[1] <= capF)
+        {
+            nearList->rows = farList->rows = rows;
+            nearList->begin = farList->begin = begin;
+            return MRMD_OK;
+        }
+        if (hMax[0] > capN) capN = hMax[0] + hMax[0] / 8 + 4;
+        if (hMax[1] > capF) capF = hMax[1] + hMax[1] / 8 + 4;
+    }
+    return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
 }
 
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl)

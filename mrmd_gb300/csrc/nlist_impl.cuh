@@ -57,6 +57,11 @@ struct CellList
 // (each pair twice, used by the mixed form so that no j-force is scattered).
 int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t nPos, int64_t begin,
                     int64_t end, double rlist, const CellGrid& grid, int64_t maxNeighbors, bool full);
+// Full list split by distance at build time: pairs closer than rnear (FP32
+// distance) in nearList, the rest within rlist in farList; the cell list of
+// nearList is used.  Each pair appears in exactly one of the two lists.
+int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
+                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid);
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl);
 int permute_atoms(mrmd_ctx* ctx, mrmd_atoms* a, mrmd_atoms* shadow, const int32_t* perm, int64_t n);
 }  // namespace mrmd_impl

@@ -183,6 +183,48 @@ def test_fp64_apply_if_random(M, orc, cap, shifted, pkind):
     assert abs(lj.getVirial() - Wo) <= FP64_RTOL * max(abs(Wo), 1.0)
 
 
+@pytest.mark.parametrize("num_types_index", [1, 3])
+def test_fp64_multi_type_random(M, orc, num_types_index):
+    """Three atom types with per-pair parameters.  num_types_index 1 is the
+    reference's type index (LennardJones.cpp:52 sets numTypes_ to 1, so the
+    pair (i, j) reads entry type_i + type_j); 3 is the full table."""
+    L, rc, skin = 12.0, 2.5, 0.3
+    pos = random_fluid(1500, L, 21)
+    rng = np.random.default_rng(21)
+    types = rng.integers(0, 3, len(pos))
+    sig = np.array([[1.0, 1.1, 0.9], [1.1, 1.2, 1.0], [0.9, 1.0, 0.8]]).ravel()
+    eps = np.array([[1.0, 0.7, 1.3], [0.7, 0.5, 0.9], [1.3, 0.9, 1.6]]).ravel()
+    cap = np.full(9, 0.8)
+    rcs = np.full(9, rc)
+    sd_o = orc.subdomain([0, 0, 0], [L] * 3, rc + skin)
+    sd_g = M.Subdomain([0, 0, 0], [L] * 3, rc + skin)
+    ao = orc.Atoms.from_positions(pos, capacity=9000)
+    ao.type[: len(pos)] = types
+    corr = orc.create_ghosts(ao, sd_o)
+    co, no = orc.build_half_list(ao.pos, ao.n, 0, ao.numLocal, rc + skin, sd_o.minGhostCorner,
+                                 sd_o.maxGhostCorner, 1.0, 96)
+    tab = orc.lj_table(cap, rcs, sig, eps, 3, True)
+    ao.force[:] = 0
+    Eo, Wo = orc.lj_apply(tab, rc * rc, ao, co, no, None, num_types_index)
+    ag = M.Atoms.from_arrays(pos, capacity=9000, type=types)
+    gl = M.GhostLayer()
+    gl.createGhostAtoms(ag, sd_g)
+    vl = M.HalfVerletList()
+    vl.build(ag, 0, ag.numLocalAtoms, rc + skin, 1.0, sd_g.minGhostCorner, sd_g.maxGhostCorner, 60)
+    lj = M.LennardJones(rcs, sig, eps, cap, num_types=3, is_shifted=True, num_types_index=num_types_index)
+    for k, p in enumerate(lj.params()):
+        assert (p.ff1, p.ff2, p.shift) == (tab[k].ff1, tab[k].ff2, tab[k].shift)
+    ag.setForce(0.0)
+    lj.apply(ag, vl)
+    Fg = ag.getForce()
+    scale = np.abs(ao.force[: ao.n]).max()
+    assert np.abs(Fg - ao.force[: ao.n]).max() <= FP64_RTOL * scale
+    assert abs(lj.getEnergy() - Eo) <= FP64_RTOL * max(abs(Eo), 1.0)
+    assert abs(lj.getVirial() - Wo) <= FP64_RTOL * max(abs(Wo), 1.0)
+    with pytest.raises(M.MrmdError):
+        lj.apply(ag, vl, precision=M.PREC_MIXED)
+
+
 def test_mixed_precision_force_error(M, orc, espp):
     """Mixed form on the ESPP system: max |dF| / rms|F| <= 1e-6."""
     g, pos, L, rc, skin, sd_o, sd_g = espp_setup(M, orc, espp)
