@@ -460,6 +460,9 @@ typedef struct {
     int64_t maxNeighbors;    /* initial list capacity (grown on overflow) */
     int32_t observe;         /* record kinetic energy and momentum of every step */
     int32_t reserved0;
+    double splitRadius;      /* mixed form: pairs beyond it are evaluated in FP32, closer
+                                ones in double-float; 0 = 1.4 sigma (at least 1.05 x the
+                                capping distance); >= rc: every pair in double-float */
 } mrmd_md_config;
 
 int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int64_t n,

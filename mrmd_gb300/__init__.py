@@ -714,7 +714,7 @@ class LJSystem:
     def __init__(self, pos, vel, box_min, box_max, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
                  capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
                  rebuild_interval=10, use_graph=True, sort_atoms=True, max_neighbors=0, mass=None,
-                 observe=False, ctx: Context | None = None):
+                 observe=False, split_radius=0.0, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -732,6 +732,7 @@ class LJSystem:
         cfg.sortAtoms = int(bool(sort_atoms))
         cfg.maxNeighbors = int(max_neighbors)
         cfg.observe = int(bool(observe))
+        cfg.splitRadius = float(split_radius)
         self.cfg = cfg
         h = C.c_void_p()
         m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())

@@ -91,7 +91,7 @@ class MDConfigS(C.Structure):
                 ("cappingDistance", C.c_double), ("shifted", C.c_int32),
                 ("precision", C.c_int32), ("dt", C.c_double), ("rebuildInterval", C.c_int64),
                 ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64),
-                ("observe", C.c_int32), ("reserved0", C.c_int32)]
+                ("observe", C.c_int32), ("reserved0", C.c_int32), ("splitRadius", C.c_double)]
 
 
 class AdResSConfigS(C.Structure):

@@ -353,6 +353,7 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     if (!ctx || !out || !cfg || !pos3 || !vel3 || n <= 0) return MRMD_ERR_ARG;
     MRMD_CHECK_ARG(cfg->rc > 0 && cfg->skin >= 0 && cfg->dt > 0 && cfg->rebuildInterval >= 1, ctx, "bad config");
     MRMD_CHECK_ARG(cfg->precision == MRMD_PREC_FP64 || cfg->precision == MRMD_PREC_MIXED, ctx, "bad precision");
+    MRMD_CHECK_ARG(cfg->splitRadius >= 0.0, ctx, "splitRadius must be >= 0");
     MRMD_CHECK_ARG(n < INT32_MAX / 2, ctx, "too many atoms");
     *out = nullptr;
     mrmd_md* md = new mrmd_md();
@@ -383,7 +384,8 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     if (rc == MRMD_OK) rc = mrmd_ghost_layer_alloc(ctx, &md->ghosts, cap);
     if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->list);
     if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->farList);
-    md->rsplit = lj_split_radius(cfg->sigma, cfg->cappingDistance);
+    md->rsplit = cfg->splitRadius > 0.0 ? cfg->splitRadius : lj_split_radius(cfg->sigma, cfg->cappingDistance);
+    if (md->rsplit < 1.05 * cfg->cappingDistance) md->rsplit = 1.05 * cfg->cappingDistance;
     if (rc == MRMD_OK)
     {
         const double c = cfg->cappingDistance, r = cfg->rc, s = cfg->sigma, e = cfg->epsilon;

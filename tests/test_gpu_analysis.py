@@ -92,13 +92,16 @@ def test_fused_step_observables_match_oracle(M, orc, graph):
 
 def test_fused_step_energy_conservation(M):
     """Total energy from the device records stays within the velocity-Verlet
-    fluctuation (1e-3 per atom) over 400 steps in both forms, and the FP64
-    form keeps the velocity sum at rounding level."""
+    fluctuation (1e-3 per atom) over 400 steps in both forms.  The velocity
+    sum stays at rounding level: in the FP64 form (half list, F_ji = -F_ij
+    exactly) near 1e-12; in the mixed form each side of a pair is rounded on
+    its own (full list, FP32 far pairs), a random walk of about
+    sqrt(N) * 1e-7 * F_rms * dt per step."""
     pos, L = fcc(8)
     rng = np.random.default_rng(9)
     pos = pos + rng.normal(0, 0.01, pos.shape)
     vel = mb_velocities(len(pos), 0.728, 3)
-    for prec, mom_tol in ((M.PREC_FP64, 1e-9), (M.PREC_MIXED, 1e-6)):
+    for prec, mom_tol in ((M.PREC_FP64, 1e-9), (M.PREC_MIXED, 2e-5)):
         s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, observe=True)
         rec = s.run_observed(400)
         etot = rec[:, 0] + rec[:, 2]

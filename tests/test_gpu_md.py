@@ -151,3 +151,27 @@ def test_mixed_vs_fp64_forces_and_drift(M):
     n = len(pos)
     # total energy at the end vs start (potential from the run, kinetic at end)
     assert np.all(np.isfinite(e))
+
+
+@pytest.mark.parametrize("split_radius,bound", [(0.0, 1e-6), (1.8, 5e-7), (2.8, 1e-8)])
+def test_mixed_split_radius_error(M, split_radius, bound):
+    """The mixed form evaluates pairs beyond the split radius in FP32 (default
+    1.4 sigma) and closer pairs in double-float; a split radius at the list
+    radius keeps every pair in double-float.  Force error against FP64 on the
+    same positions, normalised by the RMS force."""
+    pos, L = fcc(8)
+    vel = mb_velocities(len(pos), 0.728, 4)
+    ref = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64)
+    ref.run(150)
+    p, v, _ = ref.state()
+    mix = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED, split_radius=split_radius)
+    ref.set_state(p, v)
+    em, wm = mix.eval_forces()
+    er, wr = ref.eval_forces()
+    _, _, fm = mix.state()
+    _, _, fr = ref.state()
+    rms = np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean())
+    err = np.linalg.norm(fm - fr, axis=1).max() / rms
+    assert err < bound, err
+    assert abs(em - er) <= 1e-6 * abs(er) and abs(wm - wr) <= 1e-6 * abs(wr)
+    assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
