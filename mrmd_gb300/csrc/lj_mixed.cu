@@ -37,7 +37,7 @@ SplitParams split_params(const double* origin, double extent)
 }
 
 __global__ void k_split_coords(const double4* __restrict__ pos, int64_t n, SplitParams sp,
-                               float4* __restrict__ hi, float4* __restrict__ lo)
+                               float4* __restrict__ hi, float4* __restrict__ lo, int stride)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -49,16 +49,17 @@ __global__ void k_split_coords(const double4* __restrict__ pos, int64_t n, Split
         split_one(p.z - sp.origin.z, sp, h.z, l.z);
         h.w = 0.0f;
         l.w = 0.0f;
-        hi[i] = h;
-        lo[i] = l;
+        hi[i * stride] = h;
+        lo[i * stride] = l;
     }
 }
 
-int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo)
+int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo,
+                 int stride)
 {
     if (n == 0) return MRMD_OK;
     k_split_coords<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n, sp,
-                                                                   hi, lo);
+                                                                   hi, lo, stride);
     return after_launch(ctx, "split_coords");
 }
 
@@ -183,8 +184,8 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
 // has come closer.  Per-lane decisions keep every pair on the right path;
 // the split only keeps the warps' lanes on the same path.
 template <bool ACCUM>
-__global__ void __launch_bounds__(MX_TB) k_lj_mixed_split(
-    const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
+__global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
+    const float4* __restrict__ x2, double4* __restrict__ force, const LJDev p,
     RcSq rc2, float rsplitSq, const int32_t* __restrict__ countsN, const int32_t* __restrict__ nbrsN, int64_t capN,
     const int32_t* __restrict__ countsF, const int32_t* __restrict__ nbrsF, int64_t capF, int64_t n,
     double* __restrict__ ev)
@@ -195,51 +196,47 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_split(
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n)
     {
-        const float4 hi_i = hi[i], lo_i = lo[i];
+        const float4 hi_i = x2[2 * i], lo_i = x2[2 * i + 1];
+        auto one = [&](const float4& h, const float4& l) {
+            if (pair_far(hi_i, lo_i, h, l, p, rc2, rsplitSq, fa) == 2)
+            {
+                PairMixed q;
+                if (pair_mixed(hi_i, lo_i, h, l, p, rc2, q)) acc.add(q);
+            }
+        };
         {
             const int32_t cnt = countsN[i];
             const int32_t* __restrict__ col = nbrsN + mrmd_dev::nbr_row(i, capN);
             for (int32_t k = 0; k < cnt; ++k)
             {
                 const int32_t j = __ldg(col + 32 * (int64_t)k);
-                const float4 h = __ldg(hi + j), l = __ldg(lo + j);
-                if (pair_far(hi_i, lo_i, h, l, p, rc2, rsplitSq, fa) == 2)
-                {
-                    PairMixed q;
-                    if (pair_mixed(hi_i, lo_i, h, l, p, rc2, q)) acc.add(q);
-                }
+                one(__ldg(x2 + 2 * j), __ldg(x2 + 2 * j + 1));
             }
         }
         {
+            // far rows: two gathers in flight before the (short) FP32 pairs
             const int32_t cnt = countsF[i];
             const int32_t* __restrict__ col = nbrsF + mrmd_dev::nbr_row(i, capF);
             int32_t k = 0;
             for (; k + 1 < cnt; k += 2)
             {
-                const int32_t j0 = __ldg(col + 32 * (int64_t)k);
-                const int32_t j1 = __ldg(col + 32 * (int64_t)(k + 1));
-                const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
-                const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
-                if (pair_far(hi_i, lo_i, h0, l0, p, rc2, rsplitSq, fa) == 2)
+                int32_t j[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) j[u] = __ldg(col + 32 * (int64_t)(k + u));
+                float4 h[2], l[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
                 {
-                    PairMixed q;
-                    if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
+                    h[u] = __ldg(x2 + 2 * j[u]);
+                    l[u] = __ldg(x2 + 2 * j[u] + 1);
                 }
-                if (pair_far(hi_i, lo_i, h1, l1, p, rc2, rsplitSq, fa) == 2)
-                {
-                    PairMixed q;
-                    if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, q)) acc.add(q);
-                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u) one(h[u], l[u]);
             }
-            if (k < cnt)
+            for (; k < cnt; ++k)
             {
                 const int32_t j0 = __ldg(col + 32 * (int64_t)k);
-                const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
-                if (pair_far(hi_i, lo_i, h0, l0, p, rc2, rsplitSq, fa) == 2)
-                {
-                    PairMixed q;
-                    if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
-                }
+                one(__ldg(x2 + 2 * j0), __ldg(x2 + 2 * j0 + 1));
             }
         }
         df_acc(acc.fx, fa.fx);
@@ -268,8 +265,8 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_split(
 }
 }  // namespace
 
-int lj_mixed_split(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
-                   double rsplit, const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate)
+int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
+                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate)
 {
     const int64_t n = nearList->rows;
     if (n == 0) return MRMD_OK;
@@ -277,7 +274,7 @@ int lj_mixed_split(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* fo
     const RcSq rc2 = make_rcsq(rcSqr);
     const float rsplitSq = (float)(rsplit * rsplit);
 #define SPLIT_LAUNCH(A)                                                                                              \
-    k_lj_mixed_split<A><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,         \
+    k_lj_mixed_split<A><<<grid, MX_TB, 0, ctx->stream>>>(x2, reinterpret_cast<double4*>(force4), p, rc2,             \
                                                          rsplitSq, nearList->counts, nearList->nbrs,                 \
                                                          nearList->maxNeighbors, farList->counts, farList->nbrs,     \
                                                          farList->maxNeighbors, n, ev)

@@ -22,7 +22,10 @@ __device__ __forceinline__ void split_one(double c, const SplitParams& sp, float
     l = (float)(c - hd);
 }
 
-int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo);
+// hi[i * stride], lo[i * stride] (stride 2 with lo = hi + 1: one 32-byte
+// record per particle).
+int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo,
+                 int stride = 1);
 
 // Full-list mixed pair force on split coordinates; writes (or adds to) the
 // FP64 force of rows [0, nl->rows), energy/virial added to ev[0..1].
@@ -30,9 +33,10 @@ int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* for
                   const mrmd_nlist* nl, double* ev, bool accumulate);
 
 // Full-list mixed pair force over a near/far split list (build_split_list):
-// pairs at r >= sqrt(rsplitSq) in FP32 (pair_far), the others double-float.
-int lj_mixed_split(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
-                   double rsplit, const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate);
+// pairs at r >= rsplit in FP32 (pair_far), the others double-float.  x2 holds
+// the split coordinates interleaved, hi of particle j at x2[2j], lo at x2[2j+1].
+int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
+                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate);
 
 // The r_split of lj_mixed_split for LJ parameters sigma and capping distance:
 // 1.4 sigma, and beyond the capping distance (the FP32 path has no cap).

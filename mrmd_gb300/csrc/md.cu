@@ -155,7 +155,7 @@ struct mrmd_md
     CellGrid grid{};
     int32_t* orig = nullptr;     // original index of each local atom
     int32_t* origTmp = nullptr;
-    float4* split = nullptr;     // [2][capacity] hi, lo
+    float4* split = nullptr;     // [capacity][2] hi, lo interleaved
     int64_t splitCap = 0;
     SplitParams sp{};
     double* dEnergy = nullptr;   // [energyCap][REC] per-step records
@@ -235,9 +235,9 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
     if (md->cfg.precision == MRMD_PREC_MIXED)
     {
         const int64_t nAll = a->numLocal + a->numGhost;
-        MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + md->splitCap));
-        return lj_mixed_split(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
-                              md->rsplit, &md->list, &md->farList, ev, false);
+        MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + 1, 2));
+        return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
+                              &md->farList, ev, false);
     }
     MRMD_TRY(lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev));
     return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
@@ -367,7 +367,10 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
         if (!(md->sd.diameter[d] > rlist)) rc = set_error(ctx, MRMD_ERR_ARG, "box must exceed the list radius");
     if (rc == MRMD_OK)
     {
-        md->grid = make_grid(md->sd.minGhostCorner, md->sd.maxGhostCorner, rlist);
+        // mixed form: cells of half the list radius (5^3 cells searched: 42%
+        // fewer candidates than 3^3 cells of the full radius)
+        md->grid = make_grid(md->sd.minGhostCorner, md->sd.maxGhostCorner, rlist,
+                             cfg->precision == MRMD_PREC_MIXED ? 2 : 1);
         md->sp = split_params(md->sd.minGhostCorner, md->grid.extent * 1.25 + 8.0);
     }
     std::vector<double> m((size_t)n, 1.0);
@@ -633,8 +636,8 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
     {
         if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
         if (md->cfg.precision == MRMD_PREC_MIXED)
-            return lj_mixed_split(ctx, md->split, md->split + md->splitCap, a->force, md->lj->p0, md->lj->rcSqr,
-                                  md->rsplit, &md->list, &md->farList, ev, false);
+            return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
+                                  &md->farList, ev, false);
         return lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev);
     }
     const int oldSync = ctx->sync;

@@ -19,10 +19,12 @@ using namespace mrmd_impl;
 
 namespace mrmd_impl
 {
-CellGrid make_grid(const double* gridMin, const double* gridMax, double delta)
+CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, int reach)
 {
-    // n = max(1, floor(L / delta)) cells per axis, edge L / n >= delta
+    // n = max(1, floor(L reach / delta)) cells per axis, edge L / n >= delta / reach
     CellGrid g{};
+    g.reach = reach < 1 ? 1 : reach;
+    delta /= g.reach;
     double mn[3], rdx[3];
     int n[3];
     double extent = 0.0;
@@ -128,11 +130,12 @@ __global__ void __launch_bounds__(128) k_build_list(
         const int cx = ci / (g.n.z * g.n.y);
         int32_t cnt = 0, cntFar = 0;
         const int64_t row = i - begin;
-        const int axEnd = min(cx + 1, g.n.x - 1);
-        const int az0 = max(cz - 1, 0), az1 = min(cz + 1, g.n.z - 1);
-        for (int ax = FULL ? max(cx - 1, 0) : cx; ax <= axEnd; ++ax)
+        const int R = g.reach;
+        const int axEnd = min(cx + R, g.n.x - 1);
+        const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
+        for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
         {
-            for (int ay = max(cy - 1, 0); ay <= min(cy + 1, g.n.y - 1); ++ay)
+            for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
             {
                 // cells (ax, ay, az0..az1) are adjacent in the cell order, so
                 // their particles form one contiguous span of `spos`

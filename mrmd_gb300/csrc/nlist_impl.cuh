@@ -15,10 +15,12 @@ struct CellGrid
     int3 n;       // cells per axis
     int64_t ncell;
     double extent;  // max |coordinate| relative bound used for FP32 error bands
+    int reach;      // list builds search cells within +-reach per axis
 };
 
-// n = max(1, floor(L / delta)) cells per axis, edge L/n >= delta.
-CellGrid make_grid(const double* gridMin, const double* gridMax, double delta);
+// n = max(1, floor(L * reach / delta)) cells per axis, edge L/n >= delta / reach,
+// so that every pair within delta is within `reach` cells per axis.
+CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, int reach = 1);
 
 // cell = clamp(floor((x - min) * rdx), 0, n - 1) per axis, id (ix*ny + iy)*nz + iz
 __device__ __forceinline__ int32_t cell_coord(double x, double mn, double rdx, int n)
