@@ -184,9 +184,7 @@ __device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int
     {
         const float h = (float)m;
         B.lamtf[s] = make_float2(h, (float)(m - (double)h));
-        SplitParams sp;
-        sp.scale = R.splitScale;
-        sp.invScale = R.splitInv;
+        const SplitParams sp = make_split(R.splitScale, R.splitInv);
         float4 hv, lv;
         split_one(x.x - R.gmn[0], sp, hv.x, lv.x);
         split_one(x.y - R.gmn[1], sp, hv.y, lv.y);

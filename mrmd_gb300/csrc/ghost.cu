@@ -7,6 +7,7 @@
 // order".  A stable exclusive scan gives the same order as the reference's
 // parallel_scan, so ghost indices are identical to the reference's.
 #include "common.cuh"
+#include "ghost_impl.cuh"
 
 using namespace mrmd_impl;
 
@@ -175,18 +176,7 @@ __global__ void k_ghost_update(double4* __restrict__ pos, const int32_t* __restr
          g += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t idx = nLocal + g;
-        const double4 old = pos[idx];
-        const double4 r = pos[corr[idx]];
-        const double dx = __dsub_rn(old.x, r.x), dy = __dsub_rn(old.y, r.y), dz = __dsub_rn(old.z, r.z);
-        double4 p = r;
-        if (dx > +delta.x) p.x = __dadd_rn(p.x, L.x);
-        if (dy > +delta.y) p.y = __dadd_rn(p.y, L.y);
-        if (dz > +delta.z) p.z = __dadd_rn(p.z, L.z);
-        if (dx < -delta.x) p.x = __dsub_rn(p.x, L.x);
-        if (dy < -delta.y) p.y = __dsub_rn(p.y, L.y);
-        if (dz < -delta.z) p.z = __dsub_rn(p.z, L.z);
-        p.w = 0.0;
-        pos[idx] = p;
+        pos[idx] = ghost_position(pos[idx], pos[corr[idx]], L, delta);
     }
 }
 

@@ -10,16 +10,35 @@ struct SplitParams
     double3 origin;
     double scale;     // 2^q
     double invScale;  // 2^-q
+    double magic;     // 1.5 * 2^(52 - q)
+    float invScaleF;  // 2^-q
 };
 
 // origin = grid corner; extent bounds |x - origin| for every coordinate.
 SplitParams split_params(const double* origin, double extent);
 
+// hi = c rounded to the nearest multiple of 2^-q (ties to even) and
+// lo = c - hi rounded to FP32.  The rounding is the magic-number addition
+// t = c + 1.5 * 2^(52 - q): t has ulp 2^-q, so t - magic is hi exactly and the
+// low word of t's bits is the integer k = hi * 2^q (|k| < 2^24), converted
+// to FP32 without the FP64 pipe; four FP64 operations per coordinate.
 __device__ __forceinline__ void split_one(double c, const SplitParams& sp, float& h, float& l)
 {
-    const double hd = rint(c * sp.scale) * sp.invScale;  // exact multiple of 2^-q
-    h = (float)hd;                                        // exact: < 2^24 steps
-    l = (float)(c - hd);
+    const double t = __dadd_rn(c, sp.magic);
+    const int k = __double2loint(t);
+    h = __int2float_rn(k) * sp.invScaleF;  // exact: |k| < 2^24, power-of-two scale
+    l = __double2float_rn(__dsub_rn(c, __dsub_rn(t, sp.magic)));
+}
+
+// The split parameters for quantum 2^-q given by `invScale`.
+__host__ __device__ inline SplitParams make_split(double scale, double invScale)
+{
+    SplitParams s{};
+    s.scale = scale;
+    s.invScale = invScale;
+    s.magic = 6755399441055744.0 * invScale;  // 1.5 * 2^52 * 2^-q
+    s.invScaleF = (float)invScale;
+    return s;
 }
 
 // hi[i * stride], lo[i * stride] (stride 2 with lo = hi + 1: one 32-byte

@@ -19,6 +19,7 @@
 #include "integrate_impl.cuh"
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
+#include "ghost_impl.cuh"
 #include "nlist_impl.cuh"
 #include "reduce_impl.cuh"
 
@@ -40,13 +41,29 @@ __device__ __forceinline__ void observe_add(double (&o)[4], const double4& v, do
     o[3] += v.z;
 }
 
+// Split coordinates (hi, lo) of one position into the interleaved record.
+__device__ __forceinline__ void split_store(const double4& x, const SplitParams& sp, float4* __restrict__ x2,
+                                            int64_t i)
+{
+    float4 h, l;
+    split_one(x.x - sp.origin.x, sp, h.x, l.x);
+    split_one(x.y - sp.origin.y, sp, h.y, l.y);
+    split_one(x.z - sp.origin.z, sp, h.z, l.z);
+    h.w = 0.0f;
+    l.w = 0.0f;
+    x2[2 * i] = h;
+    x2[2 * i + 1] = l;
+}
+
 // OBS: the velocities after the post-kick are the full-step velocities of
 // the previous step; their kinetic energy and momentum go to rec[2..5] of
-// that step's record (deterministic grid sum).
-template <bool OBS>
+// that step's record (deterministic grid sum).  SPLIT: the new positions'
+// split coordinates are written too (the mixed form between rebuilds).
+template <bool OBS, bool SPLIT>
 __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
                                    const double* __restrict__ mass, int64_t n, double dtHalf, double dt, int postKick,
-                                   double* partial, unsigned* ticket, double* rec)
+                                   double* partial, unsigned* ticket, double* rec, SplitParams sp,
+                                   float4* __restrict__ x2)
 {
     double o[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -63,8 +80,25 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
         pos[i] = x;
         vel[i] = v;
         force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+        if (SPLIT) split_store(x, sp, x2, i);
     }
     if (OBS) grid_sum<4>(o, partial, ticket, rec + 2);
+}
+
+// Ghost position update (the ghost layer's) fused with the ghosts' split
+// coordinates.
+__global__ void k_ghost_update_split(double4* __restrict__ pos, const int32_t* __restrict__ corr, int64_t nLocal,
+                                     int64_t nGhost, double3 L, double3 delta, SplitParams sp,
+                                     float4* __restrict__ x2)
+{
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nGhost;
+         g += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t idx = nLocal + g;
+        const double4 p = ghost_position(pos[idx], pos[corr[idx]], L, delta);
+        pos[idx] = p;
+        split_store(p, sp, x2, idx);
+    }
 }
 
 // The record of the last step of a run: full-step velocities formed on the
@@ -201,11 +235,12 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
     const double rlist = md->cfg.rc + md->cfg.skin;
     if (full)
     {
-        // near rows: closer than r_split + skin, so that no far pair can come
-        // within r_split before the next rebuild (displacement < skin / 2)
+        // near rows: closer than r_split + skin / 2 at the rebuild.  A far pair
+        // that comes within r_split later is still evaluated in double-float
+        // (the pair kernel decides per pair); the margin only keeps that rare.
         if (md->farList.maxNeighbors == 0) md->farList.maxNeighbors = md->cfg.maxNeighbors;
         MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
-                                  md->rsplit + md->cfg.skin, md->grid));
+                                  md->rsplit + 0.5 * md->cfg.skin, md->grid));
         MRMD_TRY(list_total_pairs(ctx, &md->farList));
     }
     else
@@ -229,13 +264,13 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
 
 // Force evaluation of the current positions into atoms.force (zeroed by the
 // caller), energy/virial added into ev.
-int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
+int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool splitDone = false)
 {
     mrmd_atoms* a = &md->atoms;
     if (md->cfg.precision == MRMD_PREC_MIXED)
     {
         const int64_t nAll = a->numLocal + a->numGhost;
-        MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + 1, 2));
+        if (!splitDone) MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + 1, 2));
         return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
                               &md->farList, ev, false);
     }
@@ -245,31 +280,52 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev)
 
 // Kick / drift / force reset of one step; prevRec (may be null) receives the
 // observables of the previous step when the stepper records them.
-int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec)
+// split: also write the split coordinates of the new local positions.
+int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec, bool split = false)
 {
     mrmd_atoms* a = &md->atoms;
     const unsigned grid = grid_for(ctx, md->n, TB);
-    if (md->cfg.observe && postKick && prevRec)
-        k_fused_kick_drift<true><<<grid, TB, 0, ctx->stream>>>(
-            reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
-            reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, 1, md->dPartial,
-            md->dTicket, prevRec);
-    else
-        k_fused_kick_drift<false><<<grid, TB, 0, ctx->stream>>>(
-            reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),
-            reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0,
-            nullptr, nullptr, nullptr);
+    const bool obs = md->cfg.observe && postKick && prevRec;
+#define KD_LAUNCH(O, S)                                                                                         \
+    k_fused_kick_drift<O, S><<<grid, TB, 0, ctx->stream>>>(                                                     \
+        reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),                                 \
+        reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0, \
+        md->dPartial, md->dTicket, prevRec, md->sp, md->split)
+    if (obs && split) KD_LAUNCH(true, true);
+    else if (obs) KD_LAUNCH(true, false);
+    else if (split) KD_LAUNCH(false, true);
+    else KD_LAUNCH(false, false);
+#undef KD_LAUNCH
     return after_launch(ctx, "fused_kick_drift");
 }
 
 // One step without rebuild, for capture: kick/drift, ghost update, forces
 // into this step's record rec; prevRec (may be null) is the previous step's.
+// The mixed form writes the split coordinates inside the kick/drift and
+// ghost-update kernels instead of a separate pass over all positions.
 int md_plain_step(mrmd_ctx* ctx, mrmd_md* md, double* rec, double* prevRec, bool postKick)
 {
     mrmd_atoms* a = &md->atoms;
-    MRMD_TRY(md_kick_drift(ctx, md, postKick, prevRec));
-    MRMD_TRY(mrmd_ghost_update(ctx, &md->ghosts, a, &md->sd));
-    return md_forces(ctx, md, rec);
+    const bool mixed = md->cfg.precision == MRMD_PREC_MIXED;
+    MRMD_TRY(md_kick_drift(ctx, md, postKick, prevRec, mixed));
+    if (!mixed)
+    {
+        MRMD_TRY(mrmd_ghost_update(ctx, &md->ghosts, a, &md->sd));
+        return md_forces(ctx, md, rec);
+    }
+    const mrmd_ghost_layer* g = &md->ghosts;
+    if (g->numLocal != a->numLocal || g->numGhost != a->numGhost)
+        return set_error(ctx, MRMD_ERR_STATE, "ghost layer does not match atoms");
+    if (a->numGhost > 0)
+    {
+        const mrmd_subdomain& sd = md->sd;
+        k_ghost_update_split<<<grid_for(ctx, a->numGhost, TB), TB, 0, ctx->stream>>>(
+            reinterpret_cast<double4*>(a->pos), g->correspondingRealAtom, a->numLocal, a->numGhost,
+            make_double3(sd.diameter[0], sd.diameter[1], sd.diameter[2]),
+            make_double3(0.1 * sd.diameter[0], 0.1 * sd.diameter[1], 0.1 * sd.diameter[2]), md->sp, md->split);
+        MRMD_TRY(after_launch(ctx, "ghost_update_split"));
+    }
+    return md_forces(ctx, md, rec, true);
 }
 
 int ensure_energy(mrmd_ctx* ctx, mrmd_md* md, int64_t nsteps)

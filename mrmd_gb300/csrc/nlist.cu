@@ -10,6 +10,7 @@
 //
 // Because x_j >= x_i implies cell_x(j) >= cell_x(i) (floor is monotone),
 // only the 9 + 9 cells with cell_x >= cell_x(i) can hold neighbours.
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -47,13 +48,37 @@ CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, i
     return g;
 }
 
+// Bits of v spread to every third position (v < 2^10).
+__device__ __forceinline__ uint32_t spread3(uint32_t v)
+{
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// morton != 0: the key is the Morton (Z-order) code of the cell coordinates,
+// so that particles sorted by it form compact blocks in space.
 __global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGrid g,
-                             int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount)
+                             int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount, int morton)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
-        const int32_t c = cell_of(pos[i], g);
+        int32_t c;
+        const double4 p = pos[i];
+        if (morton)
+        {
+            const uint32_t cx = (uint32_t)cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x);
+            const uint32_t cy = (uint32_t)cell_coord(p.y, g.mn.y, g.rdx.y, g.n.y);
+            const uint32_t cz = (uint32_t)cell_coord(p.z, g.mn.z, g.rdx.z, g.n.z);
+            c = (int32_t)((spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz));
+        }
+        else
+        {
+            c = cell_of(p, g);
+        }
         cellOf[i] = c;
         atomicAdd(&cellCount[c], 1);
     }
@@ -133,6 +158,37 @@ __global__ void __launch_bounds__(128) k_build_list(
         const int R = g.reach;
         const int axEnd = min(cx + R, g.n.x - 1);
         const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
+        auto candidate = [&](const float4& q) {
+            const int32_t j = __float_as_int(q.w);
+            if (j == (int32_t)i) return;
+            // lexicographic (x, y, z): float order is exact unless equal
+            if (!FULL && q.x < xi) return;
+            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+            const float d2f = dx * dx + dy * dy + dz * dz;
+            if (d2f > rsqHi) return;
+            bool keep;
+            if ((FULL || q.x > xi) && d2f < rsqLo)
+            {
+                keep = true;
+            }
+            else
+            {
+                const double4 pj = pos[j];
+                const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+                const double d2 =
+                    __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+                keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
+            }
+            if (!keep) return;
+            if (SPLIT && d2f >= nearSqF)
+            {
+                if (cntFar < capFar) nbrsFar[mrmd_dev::nbr_row(row, capFar) + 32 * (int64_t)cntFar] = j;
+                ++cntFar;
+                return;
+            }
+            if (cnt < cap) nbrs[mrmd_dev::nbr_row(row, cap) + 32 * (int64_t)cnt] = j;
+            ++cnt;
+        };
         for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
         {
             for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
@@ -142,39 +198,18 @@ __global__ void __launch_bounds__(128) k_build_list(
                 {
                     const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
                     const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
-                    for (int32_t s = s0; s < s1; ++s)
+                    // four candidates loaded per iteration: the loop is bound by
+                    // the latency of these loads, not by the arithmetic
+                    int32_t s = s0;
+                    for (; s + 3 < s1; s += 4)
                     {
-                        const float4 q = spos[s];
-                        const int32_t j = __float_as_int(q.w);
-                        if (j == (int32_t)i) continue;
-                        // lexicographic (x, y, z): float order is exact unless equal
-                        if (!FULL && q.x < xi) continue;
-                        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-                        const float d2f = dx * dx + dy * dy + dz * dz;
-                        if (d2f > rsqHi) continue;
-                        bool keep;
-                        if ((FULL || q.x > xi) && d2f < rsqLo)
-                        {
-                            keep = true;
-                        }
-                        else
-                        {
-                            const double4 pj = pos[j];
-                            const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-                            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
-                                                        __dmul_rn(ddz, ddz));
-                            keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
-                        }
-                        if (!keep) continue;
-                        if (SPLIT && d2f >= nearSqF)
-                        {
-                            if (cntFar < capFar) nbrsFar[mrmd_dev::nbr_row(row, capFar) + 32 * (int64_t)cntFar] = j;
-                            ++cntFar;
-                            continue;
-                        }
-                        if (cnt < cap) nbrs[mrmd_dev::nbr_row(row, cap) + 32 * (int64_t)cnt] = j;
-                        ++cnt;
+                        const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
+                        candidate(q0);
+                        candidate(q1);
+                        candidate(q2);
+                        candidate(q3);
                     }
+                    for (; s < s1; ++s) candidate(spos[s]);
                 }
             }
         }
@@ -188,9 +223,15 @@ __global__ void __launch_bounds__(128) k_build_list(
     }
 }
 
-int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid)
+int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton)
 {
     g = grid;
+    // Morton keys need at most 10 bits per axis; the key range is then a
+    // power-of-two cube covering the grid
+    int bits = 0;
+    while ((1 << bits) < std::max(g.n.x, std::max(g.n.y, g.n.z))) ++bits;
+    if (bits > 10) morton = false;
+    const int64_t nkeys = morton ? (int64_t)1 << (3 * bits) : g.ncell;
     if (n > INT32_MAX || g.ncell > INT32_MAX) return set_error(ctx, MRMD_ERR_CAPACITY, "too many particles or cells");
     if (n + 1 > capN)
     {
@@ -205,27 +246,27 @@ int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&spos), sizeof(float4) * (size_t)c));
         capN = c;
     }
-    if (g.ncell + 1 > capCells)
+    if (nkeys + 1 > capCells)
     {
         dfree(cellStart);
         dfree(cursor);
         cellStart = cursor = nullptr;
-        const int64_t c = g.ncell + 1;
+        const int64_t c = nkeys + 1;
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&cellStart), sizeof(int32_t) * (size_t)c));
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&cursor), sizeof(int32_t) * (size_t)c));
         capCells = c;
     }
     numParticles = n;
     constexpr int TB = 256;
-    MRMD_CUDA(ctx, cudaMemsetAsync(cellStart, 0, sizeof(int32_t) * (size_t)(g.ncell + 1), ctx->stream));
-    MRMD_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)(g.ncell + 1), ctx->stream));
+    MRMD_CUDA(ctx, cudaMemsetAsync(cellStart, 0, sizeof(int32_t) * (size_t)(nkeys + 1), ctx->stream));
+    MRMD_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)(nkeys + 1), ctx->stream));
     if (n > 0)
     {
         k_cell_count<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n,
-                                                                   g, cellOf, cellStart);
+                                                                   g, cellOf, cellStart, morton ? 1 : 0);
         MRMD_TRY(after_launch(ctx, "cell_count"));
     }
-    MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, g.ncell + 1, nullptr));
+    MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, nkeys + 1, nullptr));
     if (n > 0)
     {
         // unordered scatter into `spos` storage (reused as int32 scratch), then

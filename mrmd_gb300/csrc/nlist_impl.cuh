@@ -51,7 +51,9 @@ struct CellList
     float4* spos = nullptr;
     int64_t capN = 0, capCells = 0, numParticles = 0;
 
-    int build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid);
+    // morton: order the cells along a Z-order curve instead of row-major (for
+    // sorting particles; list builds need the row-major order)
+    int build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton = false);
     void release();
 };
 
