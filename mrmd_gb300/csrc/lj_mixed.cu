@@ -222,7 +222,16 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
         {
             const int32_t cnt = countsN[i];
             const int32_t* __restrict__ col = nbrsN + mrmd_dev::nbr_row(i, capN);
-            for (int32_t k = 0; k < cnt; ++k)
+            int32_t k = 0;
+            for (; k + 1 < cnt; k += 2)
+            {
+                const int32_t j0 = __ldg(col + 32 * (int64_t)k), j1 = __ldg(col + 32 * (int64_t)(k + 1));
+                const float4 h0 = __ldg(x2 + 2 * j0), l0 = __ldg(x2 + 2 * j0 + 1);
+                const float4 h1 = __ldg(x2 + 2 * j1), l1 = __ldg(x2 + 2 * j1 + 1);
+                one(h0, l0);
+                one(h1, l1);
+            }
+            if (k < cnt)
             {
                 const int32_t j = __ldg(col + 32 * (int64_t)k);
                 one(__ldg(x2 + 2 * j), __ldg(x2 + 2 * j + 1));

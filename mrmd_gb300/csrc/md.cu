@@ -59,11 +59,13 @@ __device__ __forceinline__ void split_store(const double4& x, const SplitParams&
 // the previous step; their kinetic energy and momentum go to rec[2..5] of
 // that step's record (deterministic grid sum).  SPLIT: the new positions'
 // split coordinates are written too (the mixed form between rebuilds).
+// dtfm[i] = (dt / 2) / mass[i], divided once per sort (kick_factors), the
+// same FP64 quotient VelocityVerlet forms per atom and step.
 template <bool OBS, bool SPLIT>
 __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
-                                   const double* __restrict__ mass, int64_t n, double dtHalf, double dt, int postKick,
-                                   double* partial, unsigned* ticket, double* rec, SplitParams sp,
-                                   float4* __restrict__ x2)
+                                   const double* __restrict__ mass, const double* __restrict__ dtfmOf, int64_t n,
+                                   double dt, int postKick, double* partial, unsigned* ticket, double* rec,
+                                   SplitParams sp, float4* __restrict__ x2)
 {
     double o[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -71,10 +73,9 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
     {
         double4 v = vel[i], x = pos[i];
         const double4 f = force[i];
-        const double m = mass[i];
-        const double dtfm = __ddiv_rn(dtHalf, m);
+        const double dtfm = dtfmOf[i];
         if (postKick) kick(v, f, dtfm);  // VelocityVerlet::postForceIntegrate of the previous step
-        if (OBS) observe_add(o, v, m);
+        if (OBS) observe_add(o, v, mass[i]);
         kick(v, f, dtfm);                // preForceIntegrate
         drift(x, v, dt);
         pos[i] = x;
@@ -83,6 +84,13 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
         if (SPLIT) split_store(x, sp, x2, i);
     }
     if (OBS) grid_sum<4>(o, partial, ticket, rec + 2);
+}
+
+__global__ void k_kick_factors(const double* __restrict__ mass, int64_t n, double dtHalf, double* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __ddiv_rn(dtHalf, mass[i]);  // action/VelocityVerlet.cpp:35
 }
 
 // Ghost position update (the ghost layer's) fused with the ghosts' split
@@ -195,6 +203,7 @@ struct mrmd_md
     double* dEnergy = nullptr;   // [energyCap][REC] per-step records
     int64_t energyCap = 0;
     double* hEnergy = nullptr;   // pinned
+    double* dtfm = nullptr;      // (dt / 2) / mass per local atom, in the current atom order
     double* dPartial = nullptr;  // per-block partial sums of the step observables
     unsigned* dTicket = nullptr;
     int64_t n = 0;
@@ -210,13 +219,22 @@ struct mrmd_md
 
 namespace
 {
+int kick_factors(mrmd_ctx* ctx, mrmd_md* md)
+{
+    k_kick_factors<<<grid_for(ctx, md->n, TB), TB, 0, ctx->stream>>>(md->atoms.mass, md->n, 0.5 * md->cfg.dt,
+                                                                      md->dtfm);
+    return after_launch(ctx, "kick_factors");
+}
+
 int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
 {
     mrmd_atoms* a = &md->atoms;
     MRMD_TRY(mrmd_ghost_exchange_real_atoms(ctx, a, &md->sd));
     if (md->cfg.sortAtoms > 0 && md->rebuilds % md->cfg.sortAtoms == 0)
     {
-        MRMD_TRY(md->sortCells.build(ctx, a->pos, md->n, md->grid));
+        // Z-order of the cells: a warp's 32 atoms form a compact block, so
+        // their neighbours overlap and the pair kernel's gathers hit in L1
+        MRMD_TRY(md->sortCells.build(ctx, a->pos, md->n, md->grid, true));
         if (md->shadow.capacity < a->capacity)
         {
             mrmd_atoms_free(ctx, &md->shadow);
@@ -228,6 +246,7 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
                                                                         md->n);
         MRMD_TRY(after_launch(ctx, "gather_orig"));
         std::swap(md->orig, md->origTmp);
+        MRMD_TRY(kick_factors(ctx, md));
     }
     MRMD_TRY(mrmd_ghost_create(ctx, &md->ghosts, a, &md->sd));
     const int64_t nAll = a->numLocal + a->numGhost;
@@ -289,7 +308,7 @@ int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec, bo
 #define KD_LAUNCH(O, S)                                                                                         \
     k_fused_kick_drift<O, S><<<grid, TB, 0, ctx->stream>>>(                                                     \
         reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),                                 \
-        reinterpret_cast<double4*>(a->force), a->mass, md->n, 0.5 * md->cfg.dt, md->cfg.dt, postKick ? 1 : 0, \
+        reinterpret_cast<double4*>(a->force), a->mass, md->dtfm, md->n, md->cfg.dt, postKick ? 1 : 0,         \
         md->dPartial, md->dTicket, prevRec, md->sp, md->split)
     if (obs && split) KD_LAUNCH(true, true);
     else if (obs) KD_LAUNCH(true, false);
@@ -452,6 +471,8 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     }
     if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->orig), sizeof(int32_t) * (size_t)n);
     if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->origTmp), sizeof(int32_t) * (size_t)n);
+    if (rc == MRMD_OK) rc = dmalloc(ctx, reinterpret_cast<void**>(&md->dtfm), sizeof(double) * (size_t)n);
+    if (rc == MRMD_OK) rc = kick_factors(ctx, md);
     if (rc == MRMD_OK)
     {
         // one partial per block of the fused kernel, then the ticket
@@ -496,6 +517,7 @@ int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md)
     dfree(md->split);
     dfree(md->dEnergy);
     dfree(md->dPartial);
+    dfree(md->dtfm);
     if (md->hEnergy) cudaFreeHost(md->hEnergy);
     delete md;
     return MRMD_OK;
