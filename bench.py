@@ -743,9 +743,13 @@ def main():
     line = {
         "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 state, f32 double-float pair arithmetic" if head == "mixed" else "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("f64 state; pair arithmetic f32 beyond 1.4 sigma, f32 double-float closer" if head == "mixed"
+                  else "f64"),
         "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
-        "config": {"workload": WORKLOAD, "atoms": n, "form": head, "l2": "inputs larger than L2 (no flush needed)",
+        "config": {"workload": WORKLOAD if args.cells == 100 else WORKLOAD.replace(
+                       "4,000,000 atoms (fcc 100^3", f"{n:,} atoms (fcc {args.cells}^3"),
+                   "atoms": n, "form": head, "l2": "inputs larger than L2 (no flush needed)",
                    "list_pairs": st["pairs"], "ghosts": st["ghosts"],
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "nve_drift_per_atom_per_1000tau": res[f]["drift"],

@@ -131,59 +131,6 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     }
 }
 
-// Full-list form: every pair is evaluated from both sides, each thread owns
-// its atom's force (no atomics, deterministic) and ghosts receive nothing,
-// so no ghost force fold-back is needed.  Energy and virial are halved.
-template <bool ACCUM>
-__global__ void __launch_bounds__(MX_TB) k_lj_mixed_full(
-    const float4* __restrict__ hi, const float4* __restrict__ lo, double4* __restrict__ force, const LJDev p,
-    RcSq rc2, const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
-    double* __restrict__ ev)
-{
-    __shared__ double red[64];
-    Acc acc;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n)
-    {
-        const float4 hi_i = hi[i], lo_i = lo[i];
-        const int32_t cnt = counts[i];
-        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
-        int32_t k = 0;
-        for (; k + 1 < cnt; k += 2)
-        {
-            const int32_t j0 = __ldg(col + 32 * (int64_t)k);
-            const int32_t j1 = __ldg(col + 32 * (int64_t)(k + 1));
-            const float4 h0 = __ldg(hi + j0), l0 = __ldg(lo + j0);
-            const float4 h1 = __ldg(hi + j1), l1 = __ldg(lo + j1);
-            PairMixed q;
-            if (pair_mixed(hi_i, lo_i, h0, l0, p, rc2, q)) acc.add(q);
-            if (pair_mixed(hi_i, lo_i, h1, l1, p, rc2, q)) acc.add(q);
-        }
-        if (k < cnt)
-        {
-            const int32_t j0 = __ldg(col + 32 * (int64_t)k);
-            PairMixed q;
-            if (pair_mixed(hi_i, lo_i, __ldg(hi + j0), __ldg(lo + j0), p, rc2, q)) acc.add(q);
-        }
-        double4 f = make_double4((double)acc.fx.h + (double)acc.fx.l, (double)acc.fy.h + (double)acc.fy.l,
-                                 (double)acc.fz.h + (double)acc.fz.l, 0.0);
-        if (ACCUM)
-        {
-            const double4 o = force[i];
-            f.x += o.x;
-            f.y += o.y;
-            f.z += o.z;
-        }
-        force[i] = f;
-    }
-    double e = 0.5 * ((double)acc.e.h + (double)acc.e.l), w = 0.5 * ((double)acc.w.h + (double)acc.w.l);
-    mrmd_dev::block_sum2(e, w, red);
-    if (threadIdx.x == 0)
-    {
-        atomicAdd(ev + 0, e);
-        atomicAdd(ev + 1, w);
-    }
-}
 // Full list split into near and far rows: the near rows (pairs closer than
 // r_split + skin at the rebuild) take the double-float path unless the pair
 // has since moved beyond r_split; the far rows take the FP32 path unless it
@@ -308,22 +255,6 @@ int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev&
         SPLIT_LAUNCH(false);
 #undef SPLIT_LAUNCH
     return after_launch(ctx, "lj_mixed_split");
-}
-
-int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
-                  const mrmd_nlist* nl, double* ev, bool accumulate)
-{
-    const int64_t n = nl->rows;
-    if (n == 0) return MRMD_OK;
-    const unsigned grid = (unsigned)div_up(n, MX_TB);
-    const RcSq rc2 = make_rcsq(rcSqr);
-    if (accumulate)
-        k_lj_mixed_full<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
-                                                              nl->counts, nl->nbrs, nl->maxNeighbors, n, ev);
-    else
-        k_lj_mixed_full<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, reinterpret_cast<double4*>(force4), p, rc2,
-                                                               nl->counts, nl->nbrs, nl->maxNeighbors, n, ev);
-    return after_launch(ctx, "lj_mixed_full");
 }
 
 int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_lj* lj, mrmd_atoms* a,

@@ -46,11 +46,6 @@ __host__ __device__ inline SplitParams make_split(double scale, double invScale)
 int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo,
                  int stride = 1);
 
-// Full-list mixed pair force on split coordinates; writes (or adds to) the
-// FP64 force of rows [0, nl->rows), energy/virial added to ev[0..1].
-int lj_mixed_full(mrmd_ctx* ctx, const float4* hi, const float4* lo, double* force4, const LJDev& p, double rcSqr,
-                  const mrmd_nlist* nl, double* ev, bool accumulate);
-
 // Full-list mixed pair force over a near/far split list (build_split_list):
 // pairs at r >= rsplit in FP32 (pair_far), the others double-float.  x2 holds
 // the split coordinates interleaved, hi of particle j at x2[2j], lo at x2[2j+1].
