@@ -130,10 +130,6 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def kinetic(v, m=1.0):
-    return 0.5 * m * float((v * v).sum())
-
-
 def run_cpu(pos, vel, L, steps, warmup, budget_s, threads):
     """The oracle (CPU restatement of the reference loop, OpenMP) on the same
     workload: examples/02_LennardJones_NVE.cpp:135-216 with rebuild every 10."""
@@ -259,6 +255,33 @@ def time_run(torch, M, sysm, steps, stream):
     ev1.synchronize()
     wall = time.perf_counter() - t0
     return ev0.elapsed_time(ev1), wall, e, sysm.ctx.launches - l0
+
+
+DRIFT_SETUP = ("32,000 atoms (fcc 20^3, same density, T 0.728 start), 2,000 FP64 steps to equilibrate, then "
+               "200,000 steps (1000 tau) per form from that state; drift = slope of a least-squares line "
+               "through (E_pot + E_kin)/N of every step, both summed on the device inside the step")
+
+
+def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005):
+    """Energy drift per atom per 1000 tau of each form, from the per-step
+    records of the observing stepper (no host transfer inside the run)."""
+    pos, L = fcc(cells)
+    vel = mb_velocities(len(pos), 0.728, 7)
+    eq = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64, ctx=ctx)
+    eq.run(equil, energies=False)
+    p, v, _ = eq.state()
+    eq.close()
+    out = {}
+    for form in forms:
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        s = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=prec, observe=True, ctx=ctx)
+        rec = s.run_observed(steps)
+        s.close()
+        et = (rec[:, 0] + rec[:, 2]) / len(p)
+        t = np.arange(steps) * dt
+        slope = float(np.polyfit(t, et, 1)[0])
+        out[form] = dict(drift=slope * 1000.0, fluct=float(et.std()))
+    return out
 
 
 def time_pair_kernel(torch, sysm, stream, reps=20):
@@ -659,21 +682,13 @@ def main():
     for form in forms:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
         sysm = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, ctx=ctx)
-        ew = sysm.run(args.warmup)
+        sysm.run(args.warmup, energies=False)
         barrier()
-        _, v0, _ = sysm.state()
         with ClockSampler(local_rank) as clk:
             ms, wall, e, launches = time_run(torch, M, sysm, args.steps, stream)
-        _, v1, _ = sysm.state()
         ms = max_over_ranks(ms, dist, "cuda")
-        # NVE drift over the timed steps: potential energy of the last step of
-        # each run with the full-step velocities of the same positions
-        e_start = ew[-1, 0] + kinetic(v0)
-        e_end = e[-1, 0] + kinetic(v1)
-        tau = args.steps * 0.005
         res[form] = dict(ms=ms, wall=wall, launches=launches,
                          value=replica_throughput(n, args.steps, world, ms * 1e-3),
-                         drift=(e_end - e_start) / n / tau * 1000.0,
                          clocks=clk.summary(), stats=sysm.stats())
         systems[form] = sysm
 
@@ -696,6 +711,11 @@ def main():
         ferr = {"max_abs_over_rms": float(d.max() / rms), "rms_over_rms": float(np.sqrt((d ** 2).mean()) / rms),
                 "max_per_atom_relative": float((d / np.maximum(mag, 1e-300)).max()),
                 "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
+
+    # NVE energy drift of each form on a separate equilibrated system
+    drift = nve_drift(M, ctx, list(res)) if rank == 0 else {}
+    for f in res:
+        res[f]["drift"] = drift.get(f, {}).get("drift")
 
     # the pair kernel alone (dominant kernel) for the roofline
     kern_ms = time_pair_kernel(torch, sysm, stream)
@@ -753,9 +773,11 @@ def main():
                    "list_pairs": st["pairs"], "ghosts": st["ghosts"],
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "nve_drift_per_atom_per_1000tau": res[f]["drift"],
+                                 "nve_energy_fluctuation_per_atom": drift.get(f, {}).get("fluct"),
                                  "kernel_launches": res[f]["launches"]} for f in res},
                    "mixed_over_fp64": (res["mixed"]["value"] / res["fp64"]["value"]) if {"mixed", "fp64"} <= res.keys() else None,
-                   "force_error_mixed_vs_fp64": ferr},
+                   "force_error_mixed_vs_fp64": ferr,
+                   "nve_drift_measurement": DRIFT_SETUP},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(48 * n / args.steps),
