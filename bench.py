@@ -623,13 +623,75 @@ def diff_main(args, rank, world, local_rank):
     print(json.dumps(out), flush=True)
 
 
+PRECISION_WORKLOAD = ("LJ fluid 4,000,000 atoms (fcc 100^3, rho 0.8442, T 0.728, rc 2.5 shifted, skin 0.3, "
+                      "rebuild/10, dt 0.005), 10,000 NVE steps per form")
+
+
+def precision_main(args, rank, world, local_rank):
+    """The precision study: both forms run the same 4 M-atom fluid for
+    `--steps` NVE steps (default 10,000) recording LJ energy and kinetic energy
+    of every step on the device; energy drift per atom per 1000 tau from a
+    linear fit, force error of the mixed form against FP64 at the end state."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    import mrmd_gb300 as M
+
+    if rank != 0:
+        return
+    ctx = M.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    pos, L = fcc(args.cells)
+    n = len(pos)
+    vel = mb_velocities(n, 0.728, 1000)
+    out = {}
+    systems = {}
+    for form in ("fp64", "mixed"):
+        prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+        s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, observe=True, ctx=ctx)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        rec = s.run_observed(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        et = (rec[:, 0] + rec[:, 2]) / n
+        t = np.arange(args.steps) * 0.005
+        half = args.steps // 2
+        out[form] = {"atom_steps_per_s": n * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "nve_drift_per_atom_per_1000tau": float(np.polyfit(t, et, 1)[0]) * 1000.0,
+                     "drift_second_half": float(np.polyfit(t[half:], et[half:], 1)[0]) * 1000.0,
+                     "energy_per_atom_start_end": [float(et[0]), float(et[-1])],
+                     "max_abs_momentum": float(np.abs(rec[:, 3:]).max())}
+        systems[form] = s
+    p, v, _ = systems["fp64"].state()
+    for f in systems.values():
+        f.set_state(p, v)
+        f.eval_forces()
+    _, _, fm = systems["mixed"].state()
+    _, _, fr = systems["fp64"].state()
+    d = np.linalg.norm(fm - fr, axis=1)
+    rms = float(np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean()))
+    line = {"metric": METRIC, "value": out["mixed"]["atom_steps_per_s"], "unit": METRIC, "n_gpus": 1,
+            "steps": args.steps, "warmup": 0, "ms_per_step": out["mixed"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 state; pair arithmetic f32 beyond 1.4 sigma, f32 double-float closer",
+            "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
+            "config": {"workload": PRECISION_WORKLOAD, "atoms": n, "forms": out,
+                       "mixed_over_fp64": out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"],
+                       "force_error_mixed_vs_fp64_end_state": {"max_abs_over_rms": float(d.max() / rms),
+                                                               "rms_over_rms": float(np.sqrt((d ** 2).mean()) / rms)}}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff"], default="lj")
+    ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff", "precision"], default="lj")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
     ap.add_argument("--replicas", type=int, default=None, help="batch workload: replica count (default 512)")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
@@ -654,6 +716,9 @@ def main():
         return
     if args.workload == "diff":
         diff_main(args, rank, world, local_rank)
+        return
+    if args.workload == "precision":
+        precision_main(args, rank, world, local_rank)
         return
 
     import torch
