@@ -31,7 +31,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "atom-steps/s"
-WORKLOAD = "LJ fluid 4,000,000 atoms (fcc 100^3, rho 0.8442, T 0.728, rc 2.5 shifted, skin 0.3, rebuild/10, dt 0.005)"
+WORKLOAD = ("LJ fluid 4,000,000 atoms (fcc 100^3, rho 0.8442, T 0.728, rc 2.5 shifted, skin 0.3, rebuild/10, "
+            "dt 0.005; atoms re-sorted every 4th rebuild)")
 
 
 def fcc(cells, rho=0.8442):

@@ -709,11 +709,15 @@ def getPressure(atoms: Atoms, subdomain: Subdomain) -> float:
 
 
 class LJSystem:
-    """Fused device-resident LJ NVE stepper (mrmd_md_*), the examples/02 loop."""
+    """Fused device-resident LJ NVE stepper (mrmd_md_*), the examples/02 loop.
+
+    sort_atoms: permute the atoms into Z-order of their cells at every k-th
+    list rebuild (True = every rebuild, 0 = never; the order decays slowly,
+    so every 4th rebuild is the default)."""
 
     def __init__(self, pos, vel, box_min, box_max, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
                  capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
-                 rebuild_interval=10, use_graph=True, sort_atoms=True, max_neighbors=0, mass=None,
+                 rebuild_interval=10, use_graph=True, sort_atoms=4, max_neighbors=0, mass=None,
                  observe=False, split_radius=0.0, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
@@ -729,7 +733,7 @@ class LJSystem:
         cfg.dt = dt
         cfg.rebuildInterval = int(rebuild_interval)
         cfg.useGraph = int(bool(use_graph))
-        cfg.sortAtoms = int(bool(sort_atoms))
+        cfg.sortAtoms = int(sort_atoms)  # True: every rebuild; k: every k-th rebuild
         cfg.maxNeighbors = int(max_neighbors)
         cfg.observe = int(bool(observe))
         cfg.splitRadius = float(split_radius)
