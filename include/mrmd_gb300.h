@@ -564,6 +564,10 @@ typedef struct {
     int64_t sortEvery;        /* cell-sort the molecules at every k-th rebuild; 0 = never */
     int64_t graphSteps;       /* steps per CUDA graph (0 = no graphs); a multiple of
                                  rebuildInterval * max(sortEvery, 1) */
+    int32_t listLayout;       /* mixed form: 0 = one full row per molecule, all pairs in
+                                 double-float; 1 = near and far rows, pairs beyond 1.4 sigma
+                                 in FP32 (the FP64 form ignores it) */
+    int32_t reserved0;
 } mrmd_batch_tuning;
 
 typedef struct {

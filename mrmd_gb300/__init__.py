@@ -902,7 +902,7 @@ class Replica:
 def _tuning_dict(t):
     return dict(threads_per_row=int(t.threadsPerRow), block_size=int(t.blockSize),
                 rebuild_interval=int(t.rebuildInterval), sort_every=int(t.sortEvery),
-                graph_steps=int(t.graphSteps))
+                graph_steps=int(t.graphSteps), list_layout=int(t.listLayout))
 
 
 def _tuning_struct(d):
@@ -912,6 +912,7 @@ def _tuning_struct(d):
     t.rebuildInterval = int(d["rebuild_interval"])
     t.sortEvery = int(d["sort_every"])
     t.graphSteps = int(d["graph_steps"])
+    t.listLayout = int(d.get("list_layout", 0))
     return t
 
 
@@ -921,7 +922,7 @@ class BatchSystem:
     `replicas` is a list of Replica; pos/vel are the replicas' molecules
     concatenated in that order.  Physics parameters are shared, as in
     AdResSSystem; the tuning (lanes per row, block size, rebuild interval,
-    sort interval, graph length) can be set or picked by autotune()."""
+    sort interval, graph length, list layout) can be set or picked by autotune()."""
 
     def __init__(self, replicas, pos, vel, hybrid_diameter, nu=1, rc=2.5, skin=0.3, sigma=1.0,
                  epsilon=1.0, capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
@@ -929,7 +930,7 @@ class BatchSystem:
                  tf_modulation=1.0, tf_sigma=2.4, tf_range=3.0, tf_sample_interval=1,
                  tf_update_interval=1000, comp_sampling_interval=0, comp_update_interval=0, comp_frozen=False,
                  threads_per_row=1, block_size=128, rebuild_interval=10, sort_every=5, graph_steps=50,
-                 initial_max_neighbors=0, initial_ghost_capacity=0, ctx: Context | None = None):
+                 list_layout=0, initial_max_neighbors=0, initial_ghost_capacity=0, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -956,7 +957,7 @@ class BatchSystem:
         c.initialMaxNeighbors, c.initialGhostCapacity = int(initial_max_neighbors), int(initial_ghost_capacity)
         c.tuning = _tuning_struct(dict(threads_per_row=threads_per_row, block_size=block_size,
                                        rebuild_interval=rebuild_interval, sort_every=sort_every,
-                                       graph_steps=graph_steps))
+                                       graph_steps=graph_steps, list_layout=list_layout))
         self.cfg = c
         reps = (_abi.ReplicaS * len(self.replicas))(*[r._struct() for r in self.replicas])
         h = C.c_void_p()

@@ -115,7 +115,8 @@ class ReplicaS(C.Structure):
 
 class BatchTuningS(C.Structure):
     _fields_ = [("threadsPerRow", C.c_int32), ("blockSize", C.c_int32), ("rebuildInterval", C.c_int64),
-                ("sortEvery", C.c_int64), ("graphSteps", C.c_int64)]
+                ("sortEvery", C.c_int64), ("graphSteps", C.c_int64), ("listLayout", C.c_int32),
+                ("reserved0", C.c_int32)]
 
 
 class BatchConfigS(C.Structure):

@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
         const int cz = ci % R.gn[2];
         const int cy = (ci / R.gn[2]) % R.gn[1];
         const int cx = ci / (R.gn[2] * R.gn[1]);
-        int32_t cnt = 0;
+        int32_t cnt = 0, cntF = 0;
         const int az0 = max(cz - 1, 0), az1 = min(cz + 1, R.gn[2] - 1);
         for (int ax = max(cx - 1, 0); ax <= min(cx + 1, R.gn[0] - 1); ++ax)
         {
@@ -380,6 +380,12 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
                         if (!has) continue;
                         entry = j | REVERSED;
                     }
+                    if (B.split && d2f >= B.nearSqF)
+                    {
+                        if (cntF < B.listCapF) B.nbrsF[mrmd_dev::nbr_row(i, B.listCapF) + 32 * (int64_t)cntF] = entry;
+                        ++cntF;
+                        continue;
+                    }
                     if (cnt < B.listCap) B.nbrs[mrmd_dev::nbr_row(i, B.listCap) + 32 * (int64_t)cnt] = entry;
                     ++cnt;
                 }
@@ -390,6 +396,15 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
         {
             atomicMax(&B.sc->maxCount, cnt);
             atomicOr(&B.sc->overflow, FLAG_LIST_OVERFLOW);
+        }
+        if (B.split)
+        {
+            B.countsF[i] = cntF < B.listCapF ? cntF : B.listCapF;
+            if (cntF > B.listCapF)
+            {
+                atomicMax(&B.sc->maxCountF, cntF);
+                atomicOr(&B.sc->overflow, FLAG_FAR_LIST_OVERFLOW);
+            }
         }
     }
 }
@@ -495,9 +510,8 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
     const int cnt = B.counts[i];
     const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
     const int binAlpha = is_hy(la.y) ? comp_bin(la.x) : -1;
-    for (int k = sub; k < cnt; k += TPR)
-    {
-        const int32_t entry = B.nbrs[rowBase + 32 * (int64_t)k];
+    float ffx = 0.0f, ffy = 0.0f, ffz = 0.0f, vsF = 0.0f, csF = 0.0f;  // FP32 sums of the far pairs
+    auto pair_entry = [&](const int32_t entry) {
         const bool rev = entry < 0;
         const int32_t j = entry & 0x7fffffff;
         // own slot (the molecule or one of its images) and partner slot weights
@@ -559,10 +573,42 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
         if (MIXED)
         {
             const float2 ownF = ownImgF;
-            if (ownF.x <= 0.0f && partModF.x <= 0.0f) continue;  // both coarse grained: ideal gas
+            if (ownF.x <= 0.0f && partModF.x <= 0.0f) return;  // both coarse grained: ideal gas
             const float4 hj = B.hi[j], lj = B.lo[j];
+            if (B.split && ownIsSelf)
+            {
+                // beyond r_split: plain FP32 (the pair force is small there,
+                // see pair_far); the weights enter with their FP32 heads
+                const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
+                const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
+                const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
+                const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
+                if (r2 > B.rc2.h * 1.0000005f) return;
+                if (r2 >= B.rsplitSq && r2 < B.rc2.h * 0.9999995f)
+                {
+                    const float u = __fdividef(1.0f, r2);
+                    const float u3 = u * u * u;
+                    const float ff = u3 * u * __fmaf_rn(B.lj.ff1h, u3, -B.lj.ff2h);
+                    const float e = __fmaf_rn(u3, __fmaf_rn(B.lj.ef1f, u3, -B.lj.ef2f), -B.lj.shiftf);
+                    const bool bothAT =
+                        ownF.x == 1.0f && ownF.y == 0.0f && partModF.x == 1.0f && partModF.y == 0.0f;
+                    const float w = bothAT ? 1.0f : 0.5f * (ownF.x + partModF.x);
+                    const float ffw = ff * w;
+                    ffx = __fmaf_rn(dx, ffw, ffx);
+                    ffy = __fmaf_rn(dy, ffw, ffy);
+                    ffz = __fmaf_rn(dz, ffw, ffz);
+                    if (is_hy_df(ownF) || is_hy_df(partModF))
+                    {
+                        const float V = 0.5f * e;  // V_ij = e/2 drives the drift force
+                        vsF += V;
+                        if (sampling && binAlpha != -1) csF += V;
+                    }
+                    fenergy = __fmaf_rn(e, w, fenergy);
+                    return;
+                }
+            }
             PairMixed q;
-            if (!pair_mixed(hi_i, lo_i, hj, lj, B.lj, B.rc2, q)) continue;
+            if (!pair_mixed(hi_i, lo_i, hj, lj, B.lj, B.rc2, q)) return;
             const bool hyPair = is_hy_df(ownF) || is_hy_df(partModF);
             // weighting = (lambda~_own + lambda~_partner) / 2 as a double-float
             const bool bothAT = ownF.x == 1.0f && ownF.y == 0.0f && partModF.x == 1.0f && partModF.y == 0.0f;
@@ -600,11 +646,11 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
         }
         else
         {
-            if (ownMod <= 0.0 && partMod <= 0.0) continue;  // both coarse grained: ideal gas
+            if (ownMod <= 0.0 && partMod <= 0.0) return;  // both coarse grained: ideal gas
             const double4 pj = B.pos[j];
             const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const double distSqr = dx * dx + dy * dy + dz * dz;
-            if (distSqr > B.rcSqr) continue;
+            if (distSqr > B.rcSqr) return;
             const bool hyPair = is_hy(ownMod) || is_hy(partMod);
             double ff, e;
             lj_eval_fp64(B.lj, distSqr, ff, e);
@@ -635,6 +681,21 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
                 }
             }
         }
+        };
+    for (int k = sub; k < cnt; k += TPR) pair_entry(B.nbrs[rowBase + 32 * (int64_t)k]);
+    if (MIXED && B.split)
+    {
+        const int cntF = B.countsF[i];
+        const int64_t rowBaseF = mrmd_dev::nbr_row(i, B.listCapF);
+        for (int k = sub; k < cntF; k += TPR) pair_entry(B.nbrsF[rowBaseF + 32 * (int64_t)k]);
+    }
+    if (MIXED)
+    {
+        df_acc(fx, ffx);
+        df_acc(fy, ffy);
+        df_acc(fz, ffz);
+        df_acc(vs, vsF);
+        df_acc(cs, csF);
     }
     // reduce the TPR lanes of the row (fixed butterfly: identical sums on every lane)
     RowOut o;
@@ -910,7 +971,7 @@ void drop_graph(mrmd_batch* b)
 }
 
 // (Re)size the ghost-dependent and list buffers.
-int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap)
+int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF)
 {
     BDev& B = b->B;
     const int64_t N = b->N;
@@ -940,7 +1001,20 @@ int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap)
         B.listCap = listCap;
         drop_graph(b);
     }
+    if (listCapF >= 0 && listCapF != B.listCapF)
+    {
+        const int64_t tiles = div_up(N, 32);
+        MRMD_TRY(grow(ctx, B.nbrsF, 0, tiles * 32 * (int64_t)std::max(listCapF, 1)));
+        B.listCapF = listCapF;
+        drop_graph(b);
+    }
     return MRMD_OK;
+}
+
+// the list layout of the tuning: near/far rows for the mixed form only
+void apply_layout(mrmd_batch* b)
+{
+    b->B.split = (b->cfg.precision == MRMD_PREC_MIXED && b->cfg.tuning.listLayout == 1) ? 1 : 0;
 }
 
 // Cell binning of the locals (withGhosts = 0) or of every slot.
@@ -1057,10 +1131,11 @@ int rebuild_checked(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
         const uint32_t f = b->hSc->overflow;
         if (!f) return MRMD_OK;
         if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
-        int32_t gCap = B.gCap, lCap = B.listCap;
+        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF;
         if (f & FLAG_GHOST_OVERFLOW) gCap = b->hSc->numGhost + b->hSc->numGhost / 4 + 1024;
         if (f & FLAG_LIST_OVERFLOW) lCap = b->hSc->maxCount + b->hSc->maxCount / 5 + 8;
-        MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
+        if (f & FLAG_FAR_LIST_OVERFLOW) fCap = b->hSc->maxCountF + b->hSc->maxCountF / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap));
         b->recoveries++;
         sort = false;  // the locals are already in cell order
     }
@@ -1209,12 +1284,13 @@ int run_graph(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
         }
         if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
         // roll back, grow, re-capture
-        const int32_t needG = b->hSc->numGhost, needL = b->hSc->maxCount;
+        const int32_t needG = b->hSc->numGhost, needL = b->hSc->maxCount, needF = b->hSc->maxCountF;
         MRMD_TRY(snapshot(ctx, b, b->sn, false));
-        int32_t gCap = B.gCap, lCap = B.listCap;
+        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF;
         if (f & FLAG_GHOST_OVERFLOW) gCap = needG + needG / 4 + 1024;
         if (f & FLAG_LIST_OVERFLOW) lCap = needL + needL / 5 + 8;
-        MRMD_TRY(set_capacity(ctx, b, gCap, lCap));
+        if (f & FLAG_FAR_LIST_OVERFLOW) fCap = needF + needF / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap));
         drop_graph(b);
         b->recoveries++;
     }
@@ -1236,6 +1312,7 @@ int validate_tuning(mrmd_ctx* ctx, const mrmd_batch_tuning& t)
                    "threadsPerRow must be 1, 2, 4 or 8");
     MRMD_CHECK_ARG(t.blockSize >= 64 && t.blockSize <= 1024 && t.blockSize % 32 == 0, ctx, "bad blockSize");
     MRMD_CHECK_ARG(t.rebuildInterval >= 1 && t.sortEvery >= 0 && t.graphSteps >= 0, ctx, "bad tuning intervals");
+    MRMD_CHECK_ARG(t.listLayout == 0 || t.listLayout == 1, ctx, "listLayout must be 0 or 1");
     const int64_t period = t.rebuildInterval * (t.sortEvery > 0 ? t.sortEvery : 1);
     MRMD_CHECK_ARG(t.graphSteps == 0 || t.graphSteps % period == 0, ctx,
                    "graphSteps must be a multiple of rebuildInterval * sortEvery");
@@ -1266,8 +1343,9 @@ void free_all(mrmd_batch* b)
     BDev& B = b->B;
     void* ptrs[] = {B.pos, B.vel, B.force, B.mass, B.orig, B.slotRep, B.gSrc, B.gShift, B.imgFlags, B.ref, B.xImg, B.gCount,
                     B.lam, B.lamt, B.lamtf, B.hi, B.lo, B.cellOf, B.cellStart, B.cursor, B.unordered, B.sorted,
-                    B.spos, B.counts, B.nbrs, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce, B.tfDensity, B.tfWork,
-                    B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc, b->dReps, b->dTfFF};
+                    B.spos, B.counts, B.nbrs, B.countsF, B.nbrsF, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce,
+                    B.tfDensity, B.tfWork, B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc,
+                    b->dReps, b->dTfFF};
     for (void* p : ptrs) dfree(p);
     snap_free(b->sn);
     if (b->hSc) cudaFreeHost(b->hSc);
@@ -1402,6 +1480,12 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     B.temperature = cfg->temperature;
     B.rlist = rlist;
     B.halfSkin = 0.5 * cfg->skin;
+    {
+        const double rs = lj_split_radius(cfg->sigma, cfg->cappingDistance);
+        B.rsplitSq = (float)(rs * rs);
+        B.nearSqF = (float)((rs + 0.5 * cfg->skin) * (rs + 0.5 * cfg->skin));
+    }
+    apply_layout(b);
     B.cgMargin = cfg->skin + 1e-3;  // twice the skin/2 a molecule may move between rebuilds
     B.K = cfg->tuning.rebuildInterval;
     B.tfEnabled = cfg->tfEnabled;
@@ -1434,6 +1518,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     alloc(B.xImg, N);
     alloc(B.gCount, N + 1);
     alloc(B.counts, N);
+    alloc(B.countsF, N);
     alloc(B.sPos, N);
     alloc(B.sVel, N);
     alloc(B.sMass, N);
@@ -1455,7 +1540,8 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     // initial guesses for the ghost and list capacity: measured below
     const int32_t g0 = cfg->initialGhostCapacity > 0 ? (int32_t)cfg->initialGhostCapacity : (int32_t)std::min<int64_t>(2 * N + 1024, INT32_MAX / 2);
     const int32_t l0 = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : 64;
-    if (rc == MRMD_OK) rc = set_capacity(ctx, b, g0, l0);
+    const int32_t f0 = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : 96;
+    if (rc == MRMD_OK) rc = set_capacity(ctx, b, g0, l0, f0);
     B.reps = b->dReps;
     B.tfFF = b->dTfFF;
     if (rc == MRMD_OK)
@@ -1509,11 +1595,20 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
                 mc = 0;
                 for (int32_t c : counts) mc = std::max(mc, c);
             }
+            int32_t mcF = b->hSc->maxCountF;
+            if (rc == MRMD_OK && B.split && !(b->hSc->overflow & FLAG_FAR_LIST_OVERFLOW))
+            {
+                std::vector<int32_t> counts((size_t)N);
+                rc = d2h(ctx, counts.data(), B.countsF, sizeof(int32_t) * (size_t)N);
+                mcF = 0;
+                for (int32_t c : counts) mcF = std::max(mcF, c);
+            }
             const int32_t gCap = cfg->initialGhostCapacity > 0 ? (int32_t)cfg->initialGhostCapacity : ng + ng / 3 + 1024;
             const int32_t lCap = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : mc + mc / 3 + 8;
+            const int32_t fCap = B.split ? mcF + mcF / 3 + 8 : B.listCapF;
             Scalars z{};
             if (rc == MRMD_OK) rc = h2d(ctx, B.sc, &z, sizeof(Scalars));
-            if (rc == MRMD_OK) rc = set_capacity(ctx, b, gCap, lCap);
+            if (rc == MRMD_OK) rc = set_capacity(ctx, b, gCap, lCap, fCap);
         }
     }
     if (rc == MRMD_OK) rc = check_cuda(ctx, cudaDeviceSynchronize(), "batch create");
@@ -1648,6 +1743,7 @@ int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning*
     MRMD_TRY(validate_tuning(ctx, *t));
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     b->cfg.tuning = *t;
+    apply_layout(b);
     b->B.K = t->rebuildInterval;
     b->needRebuild = true;
     drop_graph(b);
@@ -1663,6 +1759,11 @@ int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
     MRMD_TRY(d2h(ctx, counts.data(), b->B.counts, sizeof(int32_t) * counts.size()));
     int64_t pairs = 0;
     for (int32_t c : counts) pairs += c;
+    if (b->B.split)
+    {
+        MRMD_TRY(d2h(ctx, counts.data(), b->B.countsF, sizeof(int32_t) * counts.size()));
+        for (int32_t c : counts) pairs += c;
+    }
     out10[0] = b->steps;
     out10[1] = b->rebuilds;
     out10[2] = pairs;
@@ -1670,7 +1771,7 @@ int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
     out10[4] = b->graphLaunches;
     out10[5] = ctx->launches;
     out10[6] = b->recoveries;
-    out10[7] = b->B.listCap;
+    out10[7] = b->B.listCap + (b->B.split ? b->B.listCapF : 0);
     out10[8] = b->B.gCap;
     out10[9] = b->hSc->flags | b->hSc->overflow;
     return MRMD_OK;
@@ -1713,23 +1814,26 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
 {
     if (!ctx || !b || trialSteps < 1) return MRMD_ERR_ARG;
     const mrmd_batch_tuning t0 = b->cfg.tuning;
-    // candidates: lanes per row x block size x rebuild interval
+    // candidates: list layout (mixed form) x lanes per row x block size x rebuild interval
     std::vector<mrmd_batch_tuning> cand;
     const int tprs[4] = {1, 2, 4, 8};
     const int blocks[3] = {64, 128, 256};
     const int64_t Ks[2] = {t0.rebuildInterval, 2 * t0.rebuildInterval};
-    for (int64_t K : Ks)
-        for (int tpr : tprs)
-            for (int bs : blocks)
-            {
-                mrmd_batch_tuning t = t0;
-                t.threadsPerRow = tpr;
-                t.blockSize = bs;
-                t.rebuildInterval = K;
-                const int64_t period = K * (t.sortEvery > 0 ? t.sortEvery : 1);
-                if (t.graphSteps > 0) t.graphSteps = ((t0.graphSteps + period - 1) / period) * period;
-                cand.push_back(t);
-            }
+    const int layouts = b->cfg.precision == MRMD_PREC_MIXED ? 2 : 1;
+    for (int layout = 0; layout < layouts; ++layout)
+        for (int64_t K : Ks)
+            for (int tpr : tprs)
+                for (int bs : blocks)
+                {
+                    mrmd_batch_tuning t = t0;
+                    t.threadsPerRow = tpr;
+                    t.blockSize = bs;
+                    t.rebuildInterval = K;
+                    t.listLayout = layouts > 1 ? layout : t0.listLayout;
+                    const int64_t period = K * (t.sortEvery > 0 ? t.sortEvery : 1);
+                    if (t.graphSteps > 0) t.graphSteps = ((t0.graphSteps + period - 1) / period) * period;
+                    cand.push_back(t);
+                }
     const int oldSync = ctx->sync;
     ctx->sync = 0;
     Snap keep;
@@ -1744,6 +1848,7 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
     for (size_t c = 0; c < cand.size() && rc == MRMD_OK; ++c)
     {
         b->cfg.tuning = cand[c];
+        apply_layout(b);
         b->B.K = cand[c].rebuildInterval;
         b->needRebuild = true;
         drop_graph(b);
@@ -1777,6 +1882,7 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
     b->graphLaunches = gl0;
     b->recoveries = rec0;
     b->cfg.tuning = bestIdx >= 0 ? cand[(size_t)bestIdx] : t0;
+    apply_layout(b);
     b->B.K = b->cfg.tuning.rebuildInterval;
     b->needRebuild = true;
     drop_graph(b);

@@ -371,6 +371,7 @@ int mrmd_diff_create(mrmd_ctx* ctx, mrmd_diff** out, const mrmd_batch_config* cf
     c.tfUpdateInterval = dc->steps + 1;      // the table is a parameter, not updated inside
     c.tuning.graphSteps = 0;
     c.tuning.sortEvery = 0;
+    c.tuning.listLayout = 0;                 // the adjoint walks one full row per molecule
     *out = nullptr;
     mrmd_diff* d = new mrmd_diff();
     d->dc = *dc;

@@ -28,6 +28,7 @@ enum : uint32_t
     FLAG_GHOST_OVERFLOW = 1u,
     FLAG_LIST_OVERFLOW = 2u,
     FLAG_UNSAFE_INTERVAL = 4u,
+    FLAG_FAR_LIST_OVERFLOW = 8u,
 };
 
 // Per-replica constants.
@@ -56,6 +57,7 @@ struct Scalars
     double dispStep;            // max |x - x_rebuild|^2 of the current step
     int32_t numGhost;           // total ghosts written at the last rebuild (true count on overflow)
     int32_t maxCount;           // largest list row seen (true count on overflow)
+    int32_t maxCountF;          // the same for the far rows of the split layout
     uint32_t overflow;          // ghost / list overflow of the rebuilds since the host cleared it
     uint32_t flags;             // sticky: a molecule moved skin/2 between rebuilds
     uint32_t done;              // tail-kernel block ticket
@@ -107,9 +109,16 @@ struct BDev
     int32_t* unordered;
     int32_t* sorted;
     float4* spos;
-    // list (32-row tiles)
+    // list (32-row tiles); with the split layout the near rows (pairs closer
+    // than r_split + skin/2 at the rebuild) and the far rows
     int32_t* counts;
     int32_t* nbrs;
+    int32_t* countsF;
+    int32_t* nbrsF;
+    int32_t listCapF;
+    int32_t split;      // 1: near/far rows, far pairs in FP32 (mixed form only)
+    float rsplitSq;     // r_split^2: FP32 pair arithmetic at and beyond it
+    float nearSqF;      // (r_split + skin/2)^2: near rows at the rebuild
     // shadow for the cell sort of locals
     double4* sPos;
     double4* sVel;
@@ -257,7 +266,7 @@ int grow(mrmd_ctx* ctx, T*& p, int64_t oldCount, int64_t newCount)
 }
 
 void drop_graph(mrmd_batch* b);
-int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap);
+int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF = -1);
 // ghosts, cells and the list of the current local positions (no wrap), with
 // the overflow check and buffer growth of an eager step
 int rebuild_checked(mrmd_ctx* ctx, mrmd_batch* b, bool sort);

@@ -69,8 +69,10 @@ def test_slab_reaching_into_the_ghost_layer_matches_oracle(M, orc):
     pos, vel = random_system(n, box, 9)
     steps = 11
     po, vo, eo, fo, mo = oracle_loop(orc, pos, vel, box, steps, p)
-    for prec, tol, etol in ((M.PREC_FP64, 1e-9, 1e-9), (M.PREC_MIXED, 1e-6, 1e-5)):
-        b = batch(M, [replica(M, n, box, p["at"], p["seed"])], pos, vel, p=p, precision=prec)
+    for prec, layout, tol, etol in ((M.PREC_FP64, 0, 1e-9, 1e-9), (M.PREC_MIXED, 0, 1e-6, 1e-5),
+                                    (M.PREC_MIXED, 1, 1e-6, 1e-5)):
+        b = batch(M, [replica(M, n, box, p["at"], p["seed"])], pos, vel, p=p, precision=prec,
+                  list_layout=layout)
         eg = b.run(steps)[:, 0]
         pg, vg, _ = b.state()
         np.testing.assert_allclose(pg, po, rtol=0, atol=tol)
@@ -91,11 +93,12 @@ def replica_set(M):
     return reps, np.concatenate(P_), np.concatenate(V_)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_split"])
 def test_replicas_bitwise_equal_alone(M, prec):
     precision = M.PREC_FP64 if prec == "fp64" else M.PREC_MIXED
     reps, pos, vel = replica_set(M)
-    tune = dict(threads_per_row=2, block_size=128, rebuild_interval=5, sort_every=2, graph_steps=10)
+    tune = dict(threads_per_row=2, block_size=128, rebuild_interval=5, sort_every=2, graph_steps=10,
+                list_layout=1 if prec == "mixed_split" else 0)
     b = batch(M, reps, pos, vel, precision=precision, **tune)
     steps = 23
     eb = b.run(steps)
@@ -117,10 +120,12 @@ def test_replicas_bitwise_equal_alone(M, prec):
         assert np.array_equal(ta[0], tb[r])
 
 
-def test_mixed_close_to_fp64(M):
+@pytest.mark.parametrize("layout", [0, 1])
+def test_mixed_close_to_fp64(M, layout):
+    """Layout 1 evaluates the pairs beyond 1.4 sigma in FP32 (near/far rows)."""
     reps, pos, vel = replica_set(M)
     a = batch(M, reps, pos, vel, precision=M.PREC_FP64)
-    b = batch(M, reps, pos, vel, precision=M.PREC_MIXED)
+    b = batch(M, reps, pos, vel, precision=M.PREC_MIXED, list_layout=layout)
     # the first step's forces act on identical positions (the pre-force
     # integration is FP64 in both forms)
     a.run(1)
@@ -137,14 +142,19 @@ def test_mixed_close_to_fp64(M):
     assert np.abs(pa - pb).max() < 1e-7
 
 
-def test_capacity_overflow_recovery(M):
+@pytest.mark.parametrize("prec,layout", [("fp64", 0), ("mixed", 1)])
+def test_capacity_overflow_recovery(M, prec, layout):
+    """Ghost and list buffers that start far too small (near and far rows in
+    the split layout) grow by roll-back and re-run, bitwise like a batch that
+    never overflowed."""
+    precision = M.PREC_FP64 if prec == "fp64" else M.PREC_MIXED
     reps, pos, vel = replica_set(M)
-    tune = dict(rebuild_interval=5, sort_every=1, graph_steps=10)
-    a = batch(M, reps, pos, vel, **tune)
+    tune = dict(rebuild_interval=5, sort_every=1, graph_steps=10, list_layout=layout)
+    a = batch(M, reps, pos, vel, precision=precision, **tune)
     b = M.BatchSystem(reps, pos, vel, hybrid_diameter=P["hy"], rc=P["rc"], skin=P["skin"],
                       capping_distance=P["cap"], dt=P["dt"], tf_sample_interval=P["S"], tf_update_interval=P["U"],
-                      threads_per_row=1, block_size=128, rebuild_interval=5, sort_every=1, graph_steps=10,
-                      initial_max_neighbors=6, initial_ghost_capacity=32)
+                      precision=precision, threads_per_row=1, block_size=128, rebuild_interval=5, sort_every=1,
+                      graph_steps=10, list_layout=layout, initial_max_neighbors=6, initial_ghost_capacity=32)
     a.run(20)
     b.run(20)
     assert b.stats()["recoveries"] >= 1
