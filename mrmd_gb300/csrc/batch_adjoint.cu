@@ -133,6 +133,21 @@ __device__ __forceinline__ double slab_m2(const SlabDev& s, double x)
     return -n * k * k * (pow_int(c, s.exponent) - (n - 1.0) * sn * sn * pow_int(c, s.exponent - 2));
 }
 
+// The FP32 copies of the LJDiff factors used for pairs beyond r_split in the
+// mixed form (the pair force and its derivatives are small there: see
+// pair_far in lj_mixed.cuh).
+struct LJDiffF
+{
+    float ff1, ff2, ef1, ef2, shift, ff1s, ff2s, ef1s, ef2s, shifts, invEps, rcSq;
+};
+
+LJDiffF to_float(const LJDiff& L)
+{
+    return LJDiffF{(float)L.ff1, (float)L.ff2, (float)L.ef1, (float)L.ef2, (float)L.shift, (float)L.ff1s,
+                   (float)L.ff2s, (float)L.ef1s, (float)L.ef2s, (float)L.shifts, (float)(1.0 / L.eps),
+                   (float)L.rcSqr};
+}
+
 struct AdjArgs
 {
     const double4* a;  // [N] dL/dF of the step
@@ -140,9 +155,14 @@ struct AdjArgs
     double* grad;      // [2] epsilon, sigma
     double* tfGrad;    // [sum bins]
     LJDiff L;
+    LJDiffF Lf;
 };
 
-// dPhi/dx_i (added to xbar) and the parameter terms of one force evaluation
+// dPhi/dx_i (added to xbar) and the parameter terms of one force evaluation.
+// MIXED: pairs at r >= r_split are evaluated in FP32 on the split
+// coordinates with FP32 sums per row; closer pairs, and pairs within the
+// FP32 error band of rc, in FP64.
+template <bool MIXED>
 __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
 {
     __shared__ double red[64];
@@ -155,6 +175,14 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
         const double4 ai = A.a[i];
         const double agi = ai.x * la.z;
         double bx = 0.0, by = 0.0, bz = 0.0, esum = 0.0;
+        float fbx = 0.f, fby = 0.f, fbz = 0.f, fesum = 0.f, fge = 0.f, fgs = 0.f;
+        float4 hi_i, lo_i;
+        if (MIXED)
+        {
+            hi_i = B.hi[i];
+            lo_i = B.lo[i];
+        }
+        const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, agif = (float)agi;
         const int cnt = B.counts[i];
         const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
         for (int k = 0; k < cnt; ++k)
@@ -162,6 +190,40 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
             const int32_t j = B.nbrs[rowBase + 32 * (int64_t)k] & 0x7fffffff;
             const double4 lj = B.lam[j];
             if (la.y <= 0.0 && lj.y <= 0.0) continue;  // both coarse grained
+            if (MIXED)
+            {
+                const float4 hj = B.hi[j], loj = B.lo[j];
+                const float rx = (hi_i.x - hj.x) + (lo_i.x - loj.x);
+                const float ry = (hi_i.y - hj.y) + (lo_i.y - loj.y);
+                const float rz = (hi_i.z - hj.z) + (lo_i.z - loj.z);
+                const float s = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, rz * rz));
+                const LJDiffF& L = A.Lf;
+                if (s > L.rcSq * 1.0000005f) continue;
+                if (s >= B.rsplitSq && s < L.rcSq * 0.9999995f)
+                {
+                    const int32_t src = j < B.N ? j : B.gSrc[j - B.N];
+                    const double4 aj = A.a[src];
+                    const float u = __fdividef(1.0f, s), u3 = u * u * u, u6 = u3 * u3;
+                    const float f = u3 * u * __fmaf_rn(L.ff1, u3, -L.ff2);
+                    const float fp = u * u * __fmaf_rn(-7.0f * L.ff1, u6, 4.0f * L.ff2 * u3);
+                    const float e = __fmaf_rn(u3, __fmaf_rn(L.ef1, u3, -L.ef2), -L.shift);
+                    const float ep = u * __fmaf_rn(-6.0f * L.ef1, u6, 3.0f * L.ef2 * u3);
+                    const float fs = u3 * u * __fmaf_rn(L.ff1s, u3, -L.ff2s);
+                    const float es = __fmaf_rn(u3, __fmaf_rn(L.ef1s, u3, -L.ef2s), -L.shifts);
+                    const float w = 0.5f * (float)(la.y + lj.y);
+                    const float dax = aix - (float)aj.x, day = aiy - (float)aj.y, daz = aiz - (float)aj.z;
+                    const float q = __fmaf_rn(dax, rx, __fmaf_rn(day, ry, daz * rz));
+                    const float agsum = agif + (float)(aj.x * lj.z);
+                    const float c1 = 2.0f * w * fp * q - ep * agsum;
+                    fbx += c1 * rx + w * f * dax + 0.5f * (float)la.z * f * q;
+                    fby += c1 * ry + w * f * day;
+                    fbz += c1 * rz + w * f * daz;
+                    fesum += e;
+                    fge += 0.5f * (w * q * f - 0.5f * e * agsum) * L.invEps;
+                    fgs += 0.5f * (w * q * fs - 0.5f * es * agsum);
+                    continue;
+                }
+            }
             const double4 pj = B.pos[j];
             const double rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
             const double s = rx * rx + ry * ry + rz * rz;
@@ -180,6 +242,15 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
             esum += V.e;
             ge += 0.5 * (w * q * V.fe - 0.5 * V.ee * (agi + agj));
             gs += 0.5 * (w * q * V.fs - 0.5 * V.es * (agi + agj));
+        }
+        if (MIXED)
+        {
+            bx += (double)fbx;
+            by += (double)fby;
+            bz += (double)fbz;
+            esum += (double)fesum;
+            ge += (double)fge;
+            gs += (double)fgs;
         }
         // curvature of the own weight: drift (-e/2 m') and compensation (mu m')
         if (is_hy(la.y))
@@ -520,6 +591,8 @@ int mrmd_diff_backward(mrmd_ctx* ctx, mrmd_diff* d, double* gradTable, double* g
     A.grad = d->grad;
     A.tfGrad = d->tfGrad;
     A.L = make_ljdiff(d->eps, d->sig, d->rc, d->rcap, d->shifted);
+    A.Lf = to_float(A.L);
+    const bool mixed = b->cfg.precision == MRMD_PREC_MIXED;
     const int64_t segs = (S + C - 1) / C;
     for (int64_t sg = segs - 1; sg >= 0 && rc == MRMD_OK; --sg)
     {
@@ -564,7 +637,10 @@ int mrmd_diff_backward(mrmd_ctx* ctx, mrmd_diff* d, double* gradTable, double* g
             rc = after_launch(ctx, "adj prepare");
             if (rc == MRMD_OK)
             {
-                k_adj_force<<<g, TB, 0, ctx->stream>>>(b->B, A);
+                if (mixed)
+                    k_adj_force<true><<<g, TB, 0, ctx->stream>>>(b->B, A);
+                else
+                    k_adj_force<false><<<g, TB, 0, ctx->stream>>>(b->B, A);
                 rc = after_launch(ctx, "adj force");
             }
             if (rc == MRMD_OK && st >= S - W)
@@ -625,7 +701,11 @@ int mrmd_diff_force_vjp(mrmd_ctx* ctx, mrmd_diff* d, const double* tfTable, doub
         A.grad = d->grad;
         A.tfGrad = d->tfGrad;
         A.L = make_ljdiff(epsilon, sigma, d->rc, d->rcap, d->shifted);
-        k_adj_force<<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(b->B, A);
+        A.Lf = to_float(A.L);
+        if (b->cfg.precision == MRMD_PREC_MIXED)
+            k_adj_force<true><<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(b->B, A);
+        else
+            k_adj_force<false><<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(b->B, A);
         rc = after_launch(ctx, "adj force");
     }
     if (rc == MRMD_OK && xbar3) rc = d2h(ctx, h.data(), d->xbar, sizeof(double4) * N);

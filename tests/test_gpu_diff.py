@@ -176,3 +176,18 @@ def test_torch_function_and_gradient_descent(M):
     with torch.no_grad():
         new = table - lr * table.grad
     assert d.forward(new.numpy(), 1.0, 1.0) < float(loss)
+
+
+def test_mixed_trajectory_gradient_matches_finite_differences(M):
+    """The mixed form's adjoint (pairs beyond 1.4 sigma in FP32) against
+    central differences of the mixed form's own loss."""
+    d, pos, vel = system(M, precision=M.PREC_MIXED)
+    tab = table_of(d, seed=2, scale=0.3)
+    L0 = d.forward(tab, 1.0, 1.0)
+    gt, ge, gs = d.backward()
+    h = 1e-6
+    floor = 1e-15 * abs(L0) / h * 10
+    fe = central_fd(lambda e: d.forward(tab, e, 1.0), 1.0, h)
+    fs = central_fd(lambda s: d.forward(tab, 1.0, s), 1.0, h)
+    assert abs(fe - ge) <= 1e-5 * abs(fe) + floor, (fe, ge)
+    assert abs(fs - gs) <= 1e-5 * abs(fs) + floor, (fs, gs)
