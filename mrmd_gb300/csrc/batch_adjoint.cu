@@ -148,9 +148,12 @@ LJDiffF to_float(const LJDiff& L)
                    (float)L.rcSqr};
 }
 
+constexpr int ADJ_TPR = 4;  // lanes per row of the adjoint pair kernel
+
 struct AdjArgs
 {
     const double4* a;  // [N] dL/dF of the step
+    const float4* af;  // [N] mixed form: (a.x, a.y, a.z, a.x m') in FP32
     double4* xbar;     // [N] dL/dx, accumulated
     double* grad;      // [2] epsilon, sigma
     double* tfGrad;    // [sum bins]
@@ -162,13 +165,19 @@ struct AdjArgs
 // MIXED: pairs at r >= r_split are evaluated in FP32 on the split
 // coordinates with FP32 sums per row; closer pairs, and pairs within the
 // FP32 error band of rc, in FP64.
-template <bool MIXED>
+// TPR lanes share a row (entries k = sub, sub + TPR, ...) and reduce with a
+// fixed butterfly, so that the few long rows of the atomistic and hybrid
+// regions are spread over more warps.
+template <bool MIXED, int TPR>
 __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
 {
     __shared__ double red[64];
     double ge = 0.0, gs = 0.0;
-    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < B.N; i += gridDim.x * blockDim.x)
+    const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool valid = gtid < (int64_t)B.N * TPR;
+    const int sub = (int)(gtid % TPR);
     {
+        const int32_t i = valid ? (int32_t)(gtid / TPR) : 0;
         const RepDev& R = B.reps[B.slotRep[i]];
         const double4 la = B.lam[i];  // lambda, m, m'
         const double4 pi = B.pos[i];
@@ -176,22 +185,26 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
         const double agi = ai.x * la.z;
         double bx = 0.0, by = 0.0, bz = 0.0, esum = 0.0;
         float fbx = 0.f, fby = 0.f, fbz = 0.f, fesum = 0.f, fge = 0.f, fgs = 0.f;
-        float4 hi_i, lo_i;
+        float4 hi_i, lo_i, afi;
+        float mi = 0.f, gi = 0.f;
         if (MIXED)
         {
             hi_i = B.hi[i];
             lo_i = B.lo[i];
+            afi = A.af[i];
+            mi = B.lamtf[i].x;
+            gi = (float)la.z;
         }
-        const float aix = (float)ai.x, aiy = (float)ai.y, aiz = (float)ai.z, agif = (float)agi;
-        const int cnt = B.counts[i];
+        const int cnt = valid ? B.counts[i] : 0;
         const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
-        for (int k = 0; k < cnt; ++k)
+        for (int k = sub; k < cnt; k += TPR)
         {
             const int32_t j = B.nbrs[rowBase + 32 * (int64_t)k] & 0x7fffffff;
-            const double4 lj = B.lam[j];
-            if (la.y <= 0.0 && lj.y <= 0.0) continue;  // both coarse grained
             if (MIXED)
             {
+                // no FP64 operation on the FP32 path: weights and adjoint in FP32
+                const float mj = B.lamtf[j].x;
+                if (mi <= 0.0f && mj <= 0.0f) continue;  // both coarse grained
                 const float4 hj = B.hi[j], loj = B.lo[j];
                 const float rx = (hi_i.x - hj.x) + (lo_i.x - loj.x);
                 const float ry = (hi_i.y - hj.y) + (lo_i.y - loj.y);
@@ -201,8 +214,10 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
                 if (s > L.rcSq * 1.0000005f) continue;
                 if (s >= B.rsplitSq && s < L.rcSq * 0.9999995f)
                 {
+                    // a ghost takes its source's adjoint and (the replica is
+                    // consistent) its source's weight derivative
                     const int32_t src = j < B.N ? j : B.gSrc[j - B.N];
-                    const double4 aj = A.a[src];
+                    const float4 afj = A.af[src];
                     const float u = __fdividef(1.0f, s), u3 = u * u * u, u6 = u3 * u3;
                     const float f = u3 * u * __fmaf_rn(L.ff1, u3, -L.ff2);
                     const float fp = u * u * __fmaf_rn(-7.0f * L.ff1, u6, 4.0f * L.ff2 * u3);
@@ -210,12 +225,12 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
                     const float ep = u * __fmaf_rn(-6.0f * L.ef1, u6, 3.0f * L.ef2 * u3);
                     const float fs = u3 * u * __fmaf_rn(L.ff1s, u3, -L.ff2s);
                     const float es = __fmaf_rn(u3, __fmaf_rn(L.ef1s, u3, -L.ef2s), -L.shifts);
-                    const float w = 0.5f * (float)(la.y + lj.y);
-                    const float dax = aix - (float)aj.x, day = aiy - (float)aj.y, daz = aiz - (float)aj.z;
+                    const float w = 0.5f * (mi + mj);
+                    const float dax = afi.x - afj.x, day = afi.y - afj.y, daz = afi.z - afj.z;
                     const float q = __fmaf_rn(dax, rx, __fmaf_rn(day, ry, daz * rz));
-                    const float agsum = agif + (float)(aj.x * lj.z);
+                    const float agsum = afi.w + afj.w;
                     const float c1 = 2.0f * w * fp * q - ep * agsum;
-                    fbx += c1 * rx + w * f * dax + 0.5f * (float)la.z * f * q;
+                    fbx += c1 * rx + w * f * dax + 0.5f * gi * f * q;
                     fby += c1 * ry + w * f * day;
                     fbz += c1 * rz + w * f * daz;
                     fesum += e;
@@ -224,6 +239,8 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
                     continue;
                 }
             }
+            const double4 lj = B.lam[j];
+            if (!MIXED && la.y <= 0.0 && lj.y <= 0.0) continue;  // both coarse grained
             const double4 pj = B.pos[j];
             const double rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
             const double s = rx * rx + ry * ry + rz * rz;
@@ -252,24 +269,35 @@ __global__ void __launch_bounds__(TB) k_adj_force(BDev B, AdjArgs A)
             ge += (double)fge;
             gs += (double)fgs;
         }
-        // curvature of the own weight: drift (-e/2 m') and compensation (mu m')
-        if (is_hy(la.y))
+#pragma unroll
+        for (int off = 1; off < TPR; off <<= 1)
         {
-            const double m2 = slab_m2(R.slab, pi.x);
-            double mu = 0.0;
-            const int b = comp_bin(la.x);
-            if (b != -1) mu = B.compMean[B.slotRep[i] * COMP_BINS + b];
-            bx += (mu - 0.5 * esum) * ai.x * m2;
+            bx += __shfl_xor_sync(0xffffffffu, bx, off);
+            by += __shfl_xor_sync(0xffffffffu, by, off);
+            bz += __shfl_xor_sync(0xffffffffu, bz, off);
+            esum += __shfl_xor_sync(0xffffffffu, esum, off);
         }
-        double4 xb = A.xbar[i];
-        xb.x += bx;
-        xb.y += by;
-        xb.z += bz;
-        A.xbar[i] = xb;
-        if (B.tfEnabled)
+        if (valid && sub == 0)
         {
-            const int64_t b = (int64_t)floor((pi.x - R.tfMin) * R.tfInvBin);
-            if (b >= 0 && b < R.tfBins) atomicAdd(A.tfGrad + R.tfBase + b, ai.x);
+            // curvature of the own weight: drift (-e/2 m') and compensation (mu m')
+            if (is_hy(la.y))
+            {
+                const double m2 = slab_m2(R.slab, pi.x);
+                double mu = 0.0;
+                const int b = comp_bin(la.x);
+                if (b != -1) mu = B.compMean[B.slotRep[i] * COMP_BINS + b];
+                bx += (mu - 0.5 * esum) * ai.x * m2;
+            }
+            double4 xb = A.xbar[i];
+            xb.x += bx;
+            xb.y += by;
+            xb.z += bz;
+            A.xbar[i] = xb;
+            if (B.tfEnabled)
+            {
+                const int64_t b = (int64_t)floor((pi.x - R.tfMin) * R.tfInvBin);
+                if (b >= 0 && b < R.tfBins) atomicAdd(A.tfGrad + R.tfBase + b, ai.x);
+            }
         }
     }
     mrmd_dev::block_sum2(ge, gs, red);
@@ -289,6 +317,17 @@ __global__ void k_adj_prepare(const double4* __restrict__ Fbar, const double4* _
     {
         const double4 f = Fbar[i], v = vbar[i];
         a[i] = make_double4(f.x + h * v.x, f.y + h * v.y, f.z + h * v.z, 0.0);
+    }
+}
+
+// FP32 copy of the adjoint for the mixed form's FP32 pair path: (a, a.x m')
+__global__ void k_adj_float(const double4* __restrict__ a, const double4* __restrict__ lam, int32_t n,
+                            float4* __restrict__ af)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const double4 v = a[i];
+        af[i] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)(v.x * lam[i].z));
     }
 }
 
@@ -370,6 +409,7 @@ struct mrmd_diff
     std::vector<mrmd_batch_impl::Snap> ckpt;
     double4* x2 = nullptr;  // [checkpointInterval][N] pre-force positions of a segment
     double4 *xbar = nullptr, *vbar = nullptr, *Fbar = nullptr, *adj = nullptr;
+    float4* adjf = nullptr;  // mixed form: FP32 copy of adj
     double* grad = nullptr;    // [2]
     double* tfGrad = nullptr;  // [nBins]
     double* rho = nullptr;     // [lossBins]
@@ -472,6 +512,7 @@ int mrmd_diff_create(mrmd_ctx* ctx, mrmd_diff** out, const mrmd_batch_config* cf
     if (rc == MRMD_OK) rc = grow(ctx, d->vbar, 0, N);
     if (rc == MRMD_OK) rc = grow(ctx, d->Fbar, 0, N);
     if (rc == MRMD_OK) rc = grow(ctx, d->adj, 0, N);
+    if (rc == MRMD_OK) rc = grow(ctx, d->adjf, 0, N);
     if (rc == MRMD_OK) rc = grow(ctx, d->grad, 0, (int64_t)2);
     if (rc == MRMD_OK) rc = grow(ctx, d->tfGrad, 0, (int64_t)std::max(d->nBins, 1));
     if (rc == MRMD_OK) rc = grow(ctx, d->rho, 0, dc->lossBins);
@@ -494,7 +535,7 @@ int mrmd_diff_destroy(mrmd_ctx* ctx, mrmd_diff* d)
     if (ctx) cudaStreamSynchronize(ctx->stream);
     snap_free(d->init);
     for (auto& s : d->ckpt) snap_free(s);
-    void* ptrs[] = {d->x2, d->xbar, d->vbar, d->Fbar, d->adj, d->grad, d->tfGrad, d->rho, d->coef};
+    void* ptrs[] = {d->x2, d->xbar, d->vbar, d->Fbar, d->adj, d->adjf, d->grad, d->tfGrad, d->rho, d->coef};
     for (void* p : ptrs) dfree(p);
     if (d->b) mrmd_batch_destroy(ctx, d->b);
     delete d;
@@ -587,6 +628,7 @@ int mrmd_diff_backward(mrmd_ctx* ctx, mrmd_diff* d, double* gradTable, double* g
     const unsigned g = grid_for(ctx, N, TB);
     AdjArgs A{};
     A.a = d->adj;
+    A.af = d->adjf;
     A.xbar = d->xbar;
     A.grad = d->grad;
     A.tfGrad = d->tfGrad;
@@ -635,12 +677,18 @@ int mrmd_diff_backward(mrmd_ctx* ctx, mrmd_diff* d, double* gradTable, double* g
             if (rc != MRMD_OK) break;
             k_adj_prepare<<<g, TB, 0, ctx->stream>>>(d->Fbar, d->vbar, d->adj, N, h);
             rc = after_launch(ctx, "adj prepare");
+            if (rc == MRMD_OK && mixed)
+            {
+                k_adj_float<<<g, TB, 0, ctx->stream>>>(d->adj, b->B.lam, N, d->adjf);
+                rc = after_launch(ctx, "adj float");
+            }
             if (rc == MRMD_OK)
             {
+                const unsigned ga = (unsigned)div_up((int64_t)N * ADJ_TPR, TB);
                 if (mixed)
-                    k_adj_force<true><<<g, TB, 0, ctx->stream>>>(b->B, A);
+                    k_adj_force<true, ADJ_TPR><<<ga, TB, 0, ctx->stream>>>(b->B, A);
                 else
-                    k_adj_force<false><<<g, TB, 0, ctx->stream>>>(b->B, A);
+                    k_adj_force<false, ADJ_TPR><<<ga, TB, 0, ctx->stream>>>(b->B, A);
                 rc = after_launch(ctx, "adj force");
             }
             if (rc == MRMD_OK && st >= S - W)
@@ -697,15 +745,19 @@ int mrmd_diff_force_vjp(mrmd_ctx* ctx, mrmd_diff* d, const double* tfTable, doub
     {
         AdjArgs A{};
         A.a = d->adj;
+        A.af = d->adjf;
         A.xbar = d->xbar;
         A.grad = d->grad;
         A.tfGrad = d->tfGrad;
         A.L = make_ljdiff(epsilon, sigma, d->rc, d->rcap, d->shifted);
         A.Lf = to_float(A.L);
         if (b->cfg.precision == MRMD_PREC_MIXED)
-            k_adj_force<true><<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(b->B, A);
+        {
+            k_adj_float<<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(d->adj, b->B.lam, (int32_t)N, d->adjf);
+            k_adj_force<true, ADJ_TPR><<<(unsigned)div_up((int64_t)N * ADJ_TPR, TB), TB, 0, ctx->stream>>>(b->B, A);
+        }
         else
-            k_adj_force<false><<<grid_for(ctx, (int64_t)N, TB), TB, 0, ctx->stream>>>(b->B, A);
+            k_adj_force<false, ADJ_TPR><<<(unsigned)div_up((int64_t)N * ADJ_TPR, TB), TB, 0, ctx->stream>>>(b->B, A);
         rc = after_launch(ctx, "adj force");
     }
     if (rc == MRMD_OK && xbar3) rc = d2h(ctx, h.data(), d->xbar, sizeof(double4) * N);
