@@ -798,12 +798,18 @@ def main():
     kern_ms = time_pair_kernel(torch, sysm, stream)
     st = sysm.stats()
     nbar = st["pairs"] / n
+    # Algorithmic bytes of the pair force per atom: the half-list FP64 layout,
+    # positions (24 B) read and forces (24 B) written once, one int32 count and
+    # one int32 per half-list entry.  The mixed kernel moves more by design
+    # (kernel_bytes_per_atom): 32-byte split records and the full list (every
+    # pair from both ends, so that no force is scattered with atomics).
+    nhalf = nbar / 2 if head == "mixed" else nbar
+    bytes_per_atom = 24 + 24 + 4 * (1 + nhalf)
     if head == "mixed":
-        # split coords read, F written, full list in near and far rows (two counts)
-        bytes_per_atom = 32 + 24 + 4 * (2 + nbar)
+        kernel_bytes = 32 + 24 + 4 * (2 + nbar)  # split records, F, near/far counts, full list
         kname = "lj_mixed_split"
     else:
-        bytes_per_atom = 24 + 24 + 4 * (1 + nbar)  # positions read, F written, half list
+        kernel_bytes = bytes_per_atom
         kname = "lj_fp64"
     peak, peak_kind = load_peaks()
     achieved = bytes_per_atom * n / (kern_ms * 1e-3) / 1e9
@@ -861,7 +867,8 @@ def main():
                 "d2h_bytes_per_step": int(16 + 72 * n / args.steps)},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "kernel_ms": kern_ms,
-                     "algorithmic_bytes_per_atom": bytes_per_atom,
+                     "algorithmic_bytes_per_atom": bytes_per_atom, "kernel_bytes_per_atom": kernel_bytes,
+                     "kernel_bytes_gbs": kernel_bytes * n / (kern_ms * 1e-3) / 1e9,
                      "traffic": (tpa * n) if tpa is not None else None},
         "cpu_baseline": cpu,
     }
