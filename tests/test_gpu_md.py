@@ -175,3 +175,27 @@ def test_mixed_split_radius_error(M, split_radius, bound):
     assert err < bound, err
     assert abs(em - er) <= 1e-6 * abs(er) and abs(wm - wr) <= 1e-6 * abs(wr)
     assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
+
+
+def test_elongated_box_linear_sort_fallback(M):
+    """A box of more than 1024 cells along x: the Z-order key needs more than
+    10 bits per axis, so the stepper sorts by row-major cells instead; forces
+    still match the FP64 form, and a short run stays finite."""
+    rng = np.random.default_rng(17)
+    box = np.array([1500.0, 6.0, 6.0])
+    # a dilute gas on a jittered lattice (no close contacts)
+    g = np.stack(np.meshgrid(np.arange(0.75, 1500.0, 1.5), np.arange(0.75, 6.0, 1.5),
+                             np.arange(0.75, 6.0, 1.5), indexing="ij"), -1).reshape(-1, 3)
+    pos = g + rng.uniform(-0.2, 0.2, g.shape)
+    vel = rng.normal(0, 0.5, pos.shape)
+    ref = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_FP64)
+    mix = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_MIXED)
+    er, _ = ref.eval_forces()
+    em, _ = mix.eval_forces()
+    _, _, fr = ref.state()
+    _, _, fm = mix.state()
+    rms = np.sqrt((fr * fr).sum(1).mean())
+    assert np.abs(fm - fr).max() / rms < 1e-6
+    assert abs(em - er) <= 1e-7 * abs(er)
+    e = mix.run(30)
+    assert np.all(np.isfinite(e))
