@@ -189,13 +189,21 @@ def test_elongated_box_linear_sort_fallback(M):
     pos = g + rng.uniform(-0.2, 0.2, g.shape)
     vel = rng.normal(0, 0.5, pos.shape)
     ref = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_FP64)
-    mix = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_MIXED)
     er, _ = ref.eval_forces()
-    em, _ = mix.eval_forces()
     _, _, fr = ref.state()
-    _, _, fm = mix.state()
     rms = np.sqrt((fr * fr).sum(1).mean())
-    assert np.abs(fm - fr).max() / rms < 1e-6
+    # every pair in double-float: the sort fallback alone
+    dfl = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_MIXED, split_radius=2.8)
+    em, _ = dfl.eval_forces()
+    _, _, fm = dfl.state()
+    assert np.abs(fm - fr).max() / rms < 1e-8
     assert abs(em - er) <= 1e-7 * abs(er)
+    # the default split: this near-lattice gas has a small RMS force (about 1.6
+    # against 13.7 in the dense fluid), so the FP32 rounding of the pairs beyond
+    # 1.4 sigma is a larger share of it
+    mix = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_MIXED)
+    mix.eval_forces()
+    _, _, fm = mix.state()
+    assert np.abs(fm - fr).max() / rms < 3e-6
     e = mix.run(30)
     assert np.all(np.isfinite(e))
