@@ -54,7 +54,7 @@ __global__ void k_b_pre(BDev B, int rebuild)
     const unsigned long long st = B.sc->step;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (tid < B.R) B.energyRing[(int64_t)B.sc->ringSlot * B.R + tid] = 0.0;
-    double m2 = 0.0;
+    float m2 = 0.0f;
     const double dtHalf = 0.5 * B.dt;
     for (int64_t i = tid; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
     {
@@ -71,12 +71,24 @@ __global__ void k_b_pre(BDev B, int rebuild)
         v.y = fma(B.ouSigma, g[1], v.y * B.ouDamping);
         v.z = fma(B.ouSigma, g[2], v.z * B.ouDamping);
         drift_fma(x, v, dtHalf);
+        // Verlet criterion: displacement since the list was built (FP32; the
+        // bound it is compared with, skin/2, is far above the rounding)
+        const float4 r0 = B.ref[i];
+        if (MIXED && !rebuild)
         {
-            // Verlet criterion: displacement since the list was built
-            const float4 r0 = B.ref[i];
+            // the split coordinates are relative to the same origin as r0
+            B.pos[i] = x;
+            B.vel[i] = v;
+            float4 h, l;
+            slot_derived<MIXED>(B, R, i, x, &h, &l);
+            const float dx = (h.x - r0.x) + l.x, dy = (h.y - r0.y) + l.y, dz = (h.z - r0.z) + l.z;
+            m2 = fmaxf(m2, dx * dx + dy * dy + dz * dz);
+            continue;
+        }
+        {
             const float dx = (float)(x.x - R.gmn[0]) - r0.x, dy = (float)(x.y - R.gmn[1]) - r0.y,
                         dz = (float)(x.z - R.gmn[2]) - r0.z;
-            m2 = fmax(m2, (double)(dx * dx + dy * dy + dz * dz));
+            m2 = fmaxf(m2, dx * dx + dy * dy + dz * dz);
         }
         if (rebuild)
         {
@@ -93,8 +105,8 @@ __global__ void k_b_pre(BDev B, int rebuild)
         B.vel[i] = v;
         slot_derived<MIXED>(B, R, i, x);
     }
-    m2 = mrmd_dev::warp_max(m2);
-    if ((threadIdx.x & 31) == 0) mrmd_dev::atomic_max_nonneg(&B.sc->dispStep, m2);
+    for (int o = 16; o > 0; o >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    if ((threadIdx.x & 31) == 0) mrmd_dev::atomic_max_nonneg(&B.sc->dispStep, (double)m2);
 }
 
 // weights and split coordinates of the locals at their current positions

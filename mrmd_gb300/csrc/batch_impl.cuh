@@ -183,7 +183,8 @@ __device__ __forceinline__ void drift_fma(double4& x, const double4& v, double d
 // lambda, modulated lambda and grad lambda (x) of one slot, plus the mixed
 // form's split coordinates (UpdateMolecules.hpp:39-69 for a single site).
 template <bool MIXED>
-__device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int64_t s, const double4& x)
+__device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int64_t s, const double4& x,
+                                             float4* hiOut = nullptr, float4* loOut = nullptr)
 {
     double l, m, g;
     slab_eval(R.slab, x.x, l, m, g);
@@ -202,6 +203,8 @@ __device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int
         lv.w = 0.0f;
         B.hi[s] = hv;
         B.lo[s] = lv;
+        if (hiOut) *hiOut = hv;
+        if (loOut) *loOut = lv;
     }
 }
 
