@@ -498,7 +498,7 @@ def batch_main(args, rank, world, local_rank):
         with ClockSampler(local_rank) as clk:
             ms, wall, e, launches = time_run(torch, M, s, args.steps, stream)
         res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
-                         stats=s.stats(), tuning=tuned,
+                         stats=s.stats(), lstats=s.list_stats(), tuning=tuned,
                          trials=[dict(t, ms_per_step=m) for t, m in trials])
         s.close()
     ferr = None
@@ -533,6 +533,8 @@ def batch_main(args, rank, world, local_rank):
         "config": {"workload": BATCH_WORKLOAD, "replicas": len(reps), "molecules": n, "form": head,
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "kernel_launches": res[f]["launches"], "list_pairs": res[f]["stats"]["pairs"],
+                                 "list_entries": res[f]["lstats"]["entries"],
+                                 "list_lane_efficiency": res[f]["lstats"]["lane_efficiency"],
                                  "ghost_molecules": res[f]["stats"]["ghost_molecules"],
                                  "graph_launches": res[f]["stats"]["graph_launches"],
                                  "tuning": res[f]["tuning"], "autotune_trials": res[f]["trials"]}

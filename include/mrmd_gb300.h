@@ -564,9 +564,13 @@ typedef struct {
     int64_t sortEvery;        /* cell-sort the molecules at every k-th rebuild; 0 = never */
     int64_t graphSteps;       /* steps per CUDA graph (0 = no graphs); a multiple of
                                  rebuildInterval * max(sortEvery, 1) */
-    int32_t listLayout;       /* mixed form: 0 = one full row per molecule, all pairs in
-                                 double-float; 1 = near and far rows, pairs beyond 1.4 sigma
-                                 in FP32 (the FP64 form ignores it) */
+    int32_t listLayout;       /* 0 = one full row per molecule (mixed form: all pairs in
+                                 double-float); 1 = near and far rows, pairs beyond
+                                 1.4 sigma in FP32 (mixed form; the FP64 form treats it
+                                 as 0); 2 = 8 x 4 cluster pairs: one warp per 8 molecules,
+                                 a row of (4-slot j-cluster, 32-bit pair mask) entries,
+                                 threadsPerRow 4 (mixed form: pairs beyond 1.4 sigma in
+                                 FP32) */
     int32_t reserved0;
 } mrmd_batch_tuning;
 
@@ -607,8 +611,8 @@ int mrmd_batch_get_compensation(mrmd_ctx* ctx, mrmd_batch* b, double* mean);
 int mrmd_batch_set_compensation(mrmd_ctx* ctx, mrmd_batch* b, const double* mean);
 int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t);
 int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning* t);
-/* Time each candidate tuning (lanes per row, block size, rebuild interval)
- * on trialSteps steps from the current state (restored after every trial)
+/* Time each candidate tuning (list layout, lanes per row, block size, rebuild
+ * interval) on trialSteps steps from the current state (restored after every trial)
  * and set the fastest.  A rebuild interval longer than the configured one is
  * accepted only if no molecule moved skin/2 away from its position at the
  * last rebuild during the trial.  msPerStep (may be NULL) receives
@@ -621,6 +625,11 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
  * [8] ghost capacity, [9] flags (1 ghost overflow, 2 list overflow,
  * 4 a molecule moved skin/2 from its position at the last rebuild) */
 int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10);
+/* The list of the last rebuild: [0] pairs, [1] entries (one per pair in the
+ * per-molecule layouts, one per cluster pair in the cluster layout), [2] pair
+ * slots per entry (1 or 32); pairs / (entries * slots) is the fraction of
+ * the pair kernel's lanes that evaluate a listed pair. */
+int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3);
 
 /* ------------------------------------------------- differentiation -- */
 /* Gradient of a trajectory loss of one AdResS system (the batched engine with

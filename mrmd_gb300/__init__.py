@@ -922,7 +922,9 @@ class BatchSystem:
     `replicas` is a list of Replica; pos/vel are the replicas' molecules
     concatenated in that order.  Physics parameters are shared, as in
     AdResSSystem; the tuning (lanes per row, block size, rebuild interval,
-    sort interval, graph length, list layout) can be set or picked by autotune()."""
+    sort interval, graph length, list layout) can be set or picked by autotune().
+    List layouts: 0 one row per molecule, 1 near and far rows (mixed form),
+    2 8 x 4 cluster pairs (threads_per_row 4)."""
 
     def __init__(self, replicas, pos, vel, hybrid_diameter, nu=1, rc=2.5, skin=0.3, sigma=1.0,
                  epsilon=1.0, capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
@@ -1034,6 +1036,15 @@ class BatchSystem:
         keys = ["steps", "rebuilds", "pairs", "ghost_molecules", "graph_launches", "kernel_launches",
                 "recoveries", "list_capacity", "ghost_capacity", "flags"]
         return {k: int(v) for k, v in zip(keys, out)}
+
+    def list_stats(self):
+        """The list of the last rebuild: pairs, entries, pair slots per entry and
+        the fraction of the pair kernel's lanes that evaluate a listed pair."""
+        out = np.zeros(3, dtype=np.int64)
+        self.ctx.check(self.ctx.lib.mrmd_batch_list_stats(self.ctx.h, self.h, _ip(out)), "list_stats")
+        pairs, entries, slots = (int(v) for v in out)
+        return dict(pairs=pairs, entries=entries, slots_per_entry=slots,
+                    lane_efficiency=pairs / (entries * slots) if entries else 0.0)
 
     def close(self):
         if getattr(self, "h", None):

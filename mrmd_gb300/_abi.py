@@ -258,6 +258,7 @@ SIGNATURES = {
     "mrmd_batch_set_tuning": (_i, [_v, _v, P(BatchTuningS)]),
     "mrmd_batch_autotune": (_i, [_v, _v, _i64, P(BatchTuningS), c_double_p, P(BatchTuningS), c_int64_p]),
     "mrmd_batch_stats": (_i, [_v, _v, c_int64_p]),
+    "mrmd_batch_list_stats": (_i, [_v, _v, c_int64_p]),
     "mrmd_diff_create": (_i, [_v, P(_v), P(BatchConfigS), P(ReplicaS), c_double_p, c_double_p,
                               P(DiffConfigS)]),
     "mrmd_diff_destroy": (_i, [_v, _v]),

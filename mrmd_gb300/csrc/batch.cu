@@ -421,6 +421,111 @@ __global__ void __launch_bounds__(128) k_b_build_list(BDev B)
     }
 }
 
+// Cluster-pair list (8 x 4 layout) of each i-cluster, one warp per cluster:
+// the warp walks the union of its rows' 27-cell stencils as z-column spans of
+// the replica's cell-sorted slots, in j-clusters of CLUSTER_J slots aligned to
+// the replica's first sorted position.  Lane 4a + b tests row a against slot
+// b of the j-cluster with the tests of k_b_build_list (same pairs, same
+// reversed instances); a cluster pair with any pair kept is stored with the
+// ballots of the kept and the reversed pairs.  Spans come in ascending sorted
+// order, so a j-cluster shared by two spans is visited once.
+__global__ void __launch_bounds__(128) k_b_build_clusters(BDev B)
+{
+    const int lane = threadIdx.x & 31;
+    const int a = lane >> 2, sb = lane & (CLUSTER_J - 1);
+    const int32_t nw = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    for (int32_t c = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < B.numClusters; c += nw)
+    {
+        const int2 cl = B.clusters[c];
+        const bool rowValid = a < cl.y;
+        const int32_t i = cl.x + (rowValid ? a : 0);  // rows past the cluster's end repeat row 0
+        const RepDev& R = B.reps[B.slotRep[cl.x]];
+        const double4 pi = B.pos[i];
+        const float xi = (float)(pi.x - R.gmn[0]), yi = (float)(pi.y - R.gmn[1]), zi = (float)(pi.z - R.gmn[2]);
+        const uint32_t myImg = B.imgFlags[i];
+        const float deepCG = (float)(R.slab.atHalf + R.slab.hy + B.cgMargin);
+        const float cxRel = (float)(R.slab.cx - R.gmn[0]);
+        const bool rowCG = R.consistent != 0 && fabsf(xi - cxRel) > deepCG;
+        const int32_t ci = B.cellOf[i] - R.cellBase;
+        const int cz = ci % R.gn[2];
+        const int cy = (ci / R.gn[2]) % R.gn[1];
+        const int cx = ci / (R.gn[2] * R.gn[1]);
+        const int x0 = __reduce_min_sync(0xffffffffu, cx), x1 = __reduce_max_sync(0xffffffffu, cx);
+        const int y0 = __reduce_min_sync(0xffffffffu, cy), y1 = __reduce_max_sync(0xffffffffu, cy);
+        const int z0 = __reduce_min_sync(0xffffffffu, cz), z1 = __reduce_max_sync(0xffffffffu, cz);
+        const int32_t sBase = B.cellStart[R.cellBase];
+        const int32_t sEnd = B.cellStart[R.cellBase + R.gn[0] * R.gn[1] * R.gn[2]];
+        const int az0 = max(z0 - 1, 0), az1 = min(z1 + 1, R.gn[2] - 1);
+        int32_t cnt = 0, next = 0;  // first j-cluster not visited yet
+        for (int ax = max(x0 - 1, 0); ax <= min(x1 + 1, R.gn[0] - 1); ++ax)
+        {
+            for (int ay = max(y0 - 1, 0); ay <= min(y1 + 1, R.gn[1] - 1); ++ay)
+            {
+                const int32_t c0 = R.cellBase + (ax * R.gn[1] + ay) * R.gn[2];
+                const int32_t s0 = B.cellStart[c0 + az0], s1 = B.cellStart[c0 + az1 + 1];
+                if (s1 <= s0) continue;
+                const int32_t k1 = (s1 - 1 - sBase) / CLUSTER_J;
+                for (int32_t k = max((s0 - sBase) / CLUSTER_J, next); k <= k1; ++k)
+                {
+                    const int32_t s = sBase + CLUSTER_J * k + sb;
+                    bool keep = false, rev = false;
+                    if (rowValid && s < sEnd)
+                    {
+                        const float4 q = B.spos[s];
+                        const int32_t j = __float_as_int(q.w);
+                        keep = j != i && !(rowCG && fabsf(q.x - cxRel) > deepCG);
+                        if (keep)
+                        {
+                            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                            const float d2f = dx * dx + dy * dy + dz * dz;
+                            keep = !(d2f > B.listRsqHi);
+                            if (keep && !(d2f < B.listRsqLo))
+                            {
+                                const double4 pj = B.pos[j];
+                                const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+                                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
+                                                            __dmul_rn(ddz, ddz));
+                                keep = d2 <= B.listRsq;
+                            }
+                        }
+                        if (keep && j >= B.N && !lex_above(pi, B.pos[j]))
+                        {
+                            const uint32_t code = B.gShift[j - B.N];
+#pragma unroll
+                            for (int d = 0; d < 3; ++d)
+                            {
+                                const uint32_t cd = (code >> (2 * d)) & 3u;
+                                if (cd == 1) keep = keep && (myImg & (2u << (2 * d)));
+                                if (cd == 2) keep = keep && (myImg & (1u << (2 * d)));
+                            }
+                            rev = true;
+                        }
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    const uint32_t rm = __ballot_sync(0xffffffffu, keep && rev);
+                    if (m)
+                    {
+                        if (lane == 0 && cnt < B.listCapC)
+                            B.clist[(int64_t)c * B.listCapC + cnt] =
+                                make_int4(sBase + CLUSTER_J * k, (int32_t)m, (int32_t)rm, 0);
+                        ++cnt;
+                    }
+                }
+                next = k1 + 1;
+            }
+        }
+        if (lane == 0)
+        {
+            B.countsC[c] = cnt < B.listCapC ? cnt : B.listCapC;
+            if (cnt > B.listCapC)
+            {
+                atomicMax(&B.sc->maxCountC, cnt);
+                atomicOr(&B.sc->overflow, FLAG_CLUSTER_LIST_OVERFLOW);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------ pair force --
 __device__ __forceinline__ df df_shfl_xor(df v, int o)
 {
@@ -488,9 +593,11 @@ struct RowOut
 };
 
 // One row (local molecule i), lanes `sub` of TPR.  Returns this lane's
-// partial sums.
-template <bool MIXED, int TPR>
-__device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, bool sampling)
+// partial sums.  CL: the row is row `lane >> 2` of i-cluster c (-1: none) and
+// the lane takes slot `sub` of each j-cluster whose mask has bit `lane`.
+template <bool MIXED, int TPR, bool CL = false>
+__device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, bool sampling, int32_t c = -1,
+                                            int lane = 0)
 {
     const RepDev& R = B.reps[B.slotRep[i]];
     const double4 la = B.lam[i];  // lambda, modulated, grad x
@@ -519,8 +626,6 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
     double dfx = 0.0, dfy = 0.0, dfz = 0.0, dvs = 0.0, dcs = 0.0;
     double imgFx = 0.0, energy = 0.0;
     float fenergy = 0.0f;
-    const int cnt = B.counts[i];
-    const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
     const int binAlpha = is_hy(la.y) ? comp_bin(la.x) : -1;
     float ffx = 0.0f, ffy = 0.0f, ffz = 0.0f, vsF = 0.0f, csF = 0.0f;  // FP32 sums of the far pairs
     auto pair_entry = [&](const int32_t entry) {
@@ -587,7 +692,7 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             const float2 ownF = ownImgF;
             if (ownF.x <= 0.0f && partModF.x <= 0.0f) return;  // both coarse grained: ideal gas
             const float4 hj = B.hi[j], lj = B.lo[j];
-            if (B.split && ownIsSelf)
+            if (B.farF32 && ownIsSelf)
             {
                 // beyond r_split: plain FP32 (the pair force is small there,
                 // see pair_far); the weights enter with their FP32 heads
@@ -694,7 +799,27 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             }
         }
         };
-    for (int k = sub; k < cnt; k += TPR) pair_entry(B.nbrs[rowBase + 32 * (int64_t)k]);
+    if (CL)
+    {
+        // every lane walks the cluster's row (uniform loop, broadcast loads)
+        const int cntC = c >= 0 ? B.countsC[c] : 0;
+        const int4* row = B.clist + (int64_t)(c >= 0 ? c : 0) * B.listCapC;
+        for (int k = 0; k < cntC; ++k)
+        {
+            const int4 e = row[k];
+            if (((uint32_t)e.y >> lane) & 1u)
+            {
+                const int32_t j = B.sorted[e.x + sub];
+                pair_entry((((uint32_t)e.z >> lane) & 1u) ? (j | REVERSED) : j);
+            }
+        }
+    }
+    else
+    {
+        const int cnt = B.counts[i];
+        const int64_t rowBase = mrmd_dev::nbr_row(i, B.listCap);
+        for (int k = sub; k < cnt; k += TPR) pair_entry(B.nbrs[rowBase + 32 * (int64_t)k]);
+    }
     if (MIXED && B.split)
     {
         const int cntF = B.countsF[i];
@@ -770,16 +895,28 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
 // list), then per molecule: drift-compensation force and sampling, TF apply
 // (ThermodynamicForce.hpp:98-122), density sample (AxialDensityProfile.cpp:
 // 36-47) and the velocity-Verlet post kick (VelocityVerlet.cpp:69-90).
-template <bool MIXED, int TPR>
+// CL: one warp per i-cluster, 4 lanes per row (TPR = 4).
+template <bool MIXED, int TPR, bool CL>
 __global__ void k_b_force(BDev B)
 {
+    static_assert(!CL || TPR == CLUSTER_J, "the cluster layout has CLUSTER_J lanes per row");
     const bool sampling = B.sc->sampleComp != 0;
     const bool tfSample = B.sc->sampleTf != 0;
     const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int32_t i = (int32_t)(gtid / TPR);
+    int32_t i = (int32_t)(gtid / TPR);
     const int sub = (int)(gtid % TPR);
-    const bool valid = i < B.N;
-    RowOut o = row_force<MIXED, TPR>(B, valid ? i : 0, sub, sampling && valid);
+    bool valid = i < B.N;
+    int32_t c = -1;
+    if (CL)
+    {
+        const int32_t w = (int32_t)(gtid >> 5);
+        const int a = (threadIdx.x & 31) / CLUSTER_J;
+        c = w < B.numClusters ? w : -1;
+        const int2 cl = c >= 0 ? B.clusters[c] : make_int2(0, 0);
+        valid = c >= 0 && a < cl.y;
+        i = valid ? cl.x + a : cl.x;
+    }
+    RowOut o = row_force<MIXED, TPR, CL>(B, valid ? i : 0, sub, sampling && valid, c, threadIdx.x & 31);
     int32_t r = valid ? B.slotRep[i] : -1;
     if (valid && sub == 0)
     {
@@ -870,6 +1007,19 @@ __global__ void k_b_force(BDev B)
         {
             atomicAdd(ring + r, e);
         }
+    }
+}
+
+// pairs (mask bits) and cluster pairs of the cluster layout's rows
+__global__ void k_b_cluster_stats(BDev B, unsigned long long* out)
+{
+    for (int32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < B.numClusters; c += gridDim.x * blockDim.x)
+    {
+        const int n = B.countsC[c];
+        unsigned long long bits = 0;
+        for (int k = 0; k < n; ++k) bits += (unsigned long long)__popc((uint32_t)B.clist[(int64_t)c * B.listCapC + k].y);
+        atomicAdd(out, bits);
+        atomicAdd(out + 1, (unsigned long long)n);
     }
 }
 
@@ -983,7 +1133,7 @@ void drop_graph(mrmd_batch* b)
 }
 
 // (Re)size the ghost-dependent and list buffers.
-int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF)
+int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF, int32_t listCapC)
 {
     BDev& B = b->B;
     const int64_t N = b->N;
@@ -1020,13 +1170,31 @@ int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, in
         B.listCapF = listCapF;
         drop_graph(b);
     }
+    if (listCapC >= 0 && listCapC != B.listCapC)
+    {
+        MRMD_TRY(grow(ctx, B.clist, 0, (int64_t)B.numClusters * std::max(listCapC, 1)));
+        B.listCapC = listCapC;
+        drop_graph(b);
+    }
     return MRMD_OK;
 }
 
-// the list layout of the tuning: near/far rows for the mixed form only
-void apply_layout(mrmd_batch* b)
+// the list layout of the tuning: near/far rows for the mixed form only, FP32
+// far pairs in the mixed form's near/far and cluster layouts; the cluster
+// rows are allocated when the layout is first used (a guess that the
+// overflow recovery grows)
+int apply_layout(mrmd_ctx* ctx, mrmd_batch* b)
 {
-    b->B.split = (b->cfg.precision == MRMD_PREC_MIXED && b->cfg.tuning.listLayout == 1) ? 1 : 0;
+    const int32_t layout = b->cfg.tuning.listLayout;
+    const bool mixed = b->cfg.precision == MRMD_PREC_MIXED;
+    b->B.split = (mixed && layout == LAYOUT_NEAR_FAR) ? 1 : 0;
+    b->B.farF32 = (mixed && (layout == LAYOUT_NEAR_FAR || layout == LAYOUT_CLUSTER)) ? 1 : 0;
+    if (layout == LAYOUT_CLUSTER && b->B.listCapC == 0)
+    {
+        const int32_t c0 = b->cfg.initialMaxNeighbors > 0 ? (int32_t)b->cfg.initialMaxNeighbors : 96;
+        return set_capacity(ctx, b, b->B.gCap, b->B.listCap, -1, c0);
+    }
+    return MRMD_OK;
 }
 
 // Cell binning of the locals (withGhosts = 0) or of every slot.
@@ -1065,6 +1233,11 @@ int rebuild_t(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
     k_b_ghost_write<M><<<gN, TB, 0, ctx->stream>>>(B);
     MRMD_TRY(after_launch(ctx, "batch ghost_write"));
     MRMD_TRY(cell_pass(ctx, b, 1));
+    if (b->cfg.tuning.listLayout == LAYOUT_CLUSTER)
+    {
+        k_b_build_clusters<<<grid_for(ctx, (int64_t)B.numClusters * 32, 128, 16), 128, 0, ctx->stream>>>(B);
+        return after_launch(ctx, "batch build_clusters");
+    }
     k_b_build_list<<<grid_for(ctx, b->N, 128, 16), 128, 0, ctx->stream>>>(B);
     return after_launch(ctx, "batch build_list");
 }
@@ -1074,18 +1247,19 @@ int rebuild(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
     return b->cfg.precision == MRMD_PREC_MIXED ? rebuild_t<true>(ctx, b, sort) : rebuild_t<false>(ctx, b, sort);
 }
 
-template <bool M, int TPR>
+template <bool M, int TPR, bool CL = false>
 int force_t(mrmd_ctx* ctx, mrmd_batch* b)
 {
     const int bs = b->cfg.tuning.blockSize;
-    const int64_t threads = (int64_t)b->N * TPR;
-    k_b_force<M, TPR><<<(unsigned)div_up(threads, bs), bs, 0, ctx->stream>>>(b->B);
+    const int64_t threads = CL ? (int64_t)b->B.numClusters * 32 : (int64_t)b->N * TPR;
+    k_b_force<M, TPR, CL><<<(unsigned)div_up(threads, bs), bs, 0, ctx->stream>>>(b->B);
     return after_launch(ctx, "batch force");
 }
 
 template <bool M>
 int force_m(mrmd_ctx* ctx, mrmd_batch* b)
 {
+    if (b->cfg.tuning.listLayout == LAYOUT_CLUSTER) return force_t<M, CLUSTER_J, true>(ctx, b);
     switch (b->cfg.tuning.threadsPerRow)
     {
         case 1: return force_t<M, 1>(ctx, b);
@@ -1143,11 +1317,12 @@ int rebuild_checked(mrmd_ctx* ctx, mrmd_batch* b, bool sort)
         const uint32_t f = b->hSc->overflow;
         if (!f) return MRMD_OK;
         if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
-        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF;
+        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF, cCap = B.listCapC;
         if (f & FLAG_GHOST_OVERFLOW) gCap = b->hSc->numGhost + b->hSc->numGhost / 4 + 1024;
         if (f & FLAG_LIST_OVERFLOW) lCap = b->hSc->maxCount + b->hSc->maxCount / 5 + 8;
         if (f & FLAG_FAR_LIST_OVERFLOW) fCap = b->hSc->maxCountF + b->hSc->maxCountF / 5 + 8;
-        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap));
+        if (f & FLAG_CLUSTER_LIST_OVERFLOW) cCap = b->hSc->maxCountC + b->hSc->maxCountC / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap, cCap));
         b->recoveries++;
         sort = false;  // the locals are already in cell order
     }
@@ -1297,12 +1472,14 @@ int run_graph(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
         if (attempt >= 4) return set_error(ctx, MRMD_ERR_NLIST_OVERFLOW, "batch buffers kept overflowing");
         // roll back, grow, re-capture
         const int32_t needG = b->hSc->numGhost, needL = b->hSc->maxCount, needF = b->hSc->maxCountF;
+        const int32_t needC = b->hSc->maxCountC;
         MRMD_TRY(snapshot(ctx, b, b->sn, false));
-        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF;
+        int32_t gCap = B.gCap, lCap = B.listCap, fCap = B.listCapF, cCap = B.listCapC;
         if (f & FLAG_GHOST_OVERFLOW) gCap = needG + needG / 4 + 1024;
         if (f & FLAG_LIST_OVERFLOW) lCap = needL + needL / 5 + 8;
         if (f & FLAG_FAR_LIST_OVERFLOW) fCap = needF + needF / 5 + 8;
-        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap));
+        if (f & FLAG_CLUSTER_LIST_OVERFLOW) cCap = needC + needC / 5 + 8;
+        MRMD_TRY(set_capacity(ctx, b, gCap, lCap, fCap, cCap));
         drop_graph(b);
         b->recoveries++;
     }
@@ -1324,7 +1501,9 @@ int validate_tuning(mrmd_ctx* ctx, const mrmd_batch_tuning& t)
                    "threadsPerRow must be 1, 2, 4 or 8");
     MRMD_CHECK_ARG(t.blockSize >= 64 && t.blockSize <= 1024 && t.blockSize % 32 == 0, ctx, "bad blockSize");
     MRMD_CHECK_ARG(t.rebuildInterval >= 1 && t.sortEvery >= 0 && t.graphSteps >= 0, ctx, "bad tuning intervals");
-    MRMD_CHECK_ARG(t.listLayout == 0 || t.listLayout == 1, ctx, "listLayout must be 0 or 1");
+    MRMD_CHECK_ARG(t.listLayout >= LAYOUT_ROWS && t.listLayout <= LAYOUT_CLUSTER, ctx, "listLayout must be 0, 1 or 2");
+    MRMD_CHECK_ARG(t.listLayout != LAYOUT_CLUSTER || t.threadsPerRow == CLUSTER_J, ctx,
+                   "the cluster layout (listLayout 2) takes threadsPerRow 4");
     const int64_t period = t.rebuildInterval * (t.sortEvery > 0 ? t.sortEvery : 1);
     MRMD_CHECK_ARG(t.graphSteps == 0 || t.graphSteps % period == 0, ctx,
                    "graphSteps must be a multiple of rebuildInterval * sortEvery");
@@ -1355,7 +1534,7 @@ void free_all(mrmd_batch* b)
     BDev& B = b->B;
     void* ptrs[] = {B.pos, B.vel, B.force, B.mass, B.orig, B.slotRep, B.gSrc, B.gShift, B.imgFlags, B.ref, B.xImg, B.gCount,
                     B.lam, B.lamt, B.lamtf, B.hi, B.lo, B.cellOf, B.cellStart, B.cursor, B.unordered, B.sorted,
-                    B.spos, B.counts, B.nbrs, B.countsF, B.nbrsF, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce,
+                    B.spos, B.counts, B.nbrs, B.countsF, B.nbrsF, B.clusters, B.countsC, B.clist, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce,
                     B.tfDensity, B.tfWork, B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc,
                     b->dReps, b->dTfFF};
     for (void* p : ptrs) dfree(p);
@@ -1497,7 +1676,6 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
         B.rsplitSq = (float)(rs * rs);
         B.nearSqF = (float)((rs + 0.5 * cfg->skin) * (rs + 0.5 * cfg->skin));
     }
-    apply_layout(b);
     B.cgMargin = cfg->skin + 1e-3;  // twice the skin/2 a molecule may move between rebuilds
     B.K = cfg->tuning.rebuildInterval;
     B.tfEnabled = cfg->tfEnabled;
@@ -1546,6 +1724,18 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     alloc(B.sc, 1);
     alloc(b->dReps, b->R);
     alloc(b->dTfFF, 1);
+    {
+        // i-clusters of the cluster layout: CLUSTER_I molecules of one
+        // replica, aligned to the replica's first molecule
+        std::vector<int2> cls;
+        for (int32_t r = 0; r < b->R; ++r)
+            for (int64_t i = b->offsets[(size_t)r]; i < b->offsets[(size_t)r + 1]; i += CLUSTER_I)
+                cls.push_back(make_int2((int32_t)i, (int32_t)std::min<int64_t>(CLUSTER_I, b->offsets[(size_t)r + 1] - i)));
+        B.numClusters = (int32_t)cls.size();
+        alloc(B.clusters, B.numClusters);
+        alloc(B.countsC, B.numClusters);
+        if (rc == MRMD_OK) rc = h2d(ctx, B.clusters, cls.data(), sizeof(int2) * cls.size());
+    }
     if (rc == MRMD_OK) rc = snap_alloc(ctx, b, b->sn);
     if (rc == MRMD_OK) rc = check_cuda(ctx, cudaMallocHost(reinterpret_cast<void**>(&b->hSc), sizeof(Scalars)), "batch pinned");
     if (rc == MRMD_OK) rc = ensure_ring(ctx, b);
@@ -1554,6 +1744,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     const int32_t l0 = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : 64;
     const int32_t f0 = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : 96;
     if (rc == MRMD_OK) rc = set_capacity(ctx, b, g0, l0, f0);
+    if (rc == MRMD_OK) rc = apply_layout(ctx, b);
     B.reps = b->dReps;
     B.tfFF = b->dTfFF;
     if (rc == MRMD_OK)
@@ -1615,12 +1806,24 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
                 mcF = 0;
                 for (int32_t c : counts) mcF = std::max(mcF, c);
             }
+            const bool cluster = cfg->tuning.listLayout == LAYOUT_CLUSTER;
+            int32_t mcC = b->hSc->maxCountC;
+            if (rc == MRMD_OK && cluster && !(b->hSc->overflow & FLAG_CLUSTER_LIST_OVERFLOW))
+            {
+                std::vector<int32_t> counts((size_t)B.numClusters);
+                rc = d2h(ctx, counts.data(), B.countsC, sizeof(int32_t) * counts.size());
+                mcC = 0;
+                for (int32_t c : counts) mcC = std::max(mcC, c);
+            }
             const int32_t gCap = cfg->initialGhostCapacity > 0 ? (int32_t)cfg->initialGhostCapacity : ng + ng / 3 + 1024;
             const int32_t lCap = cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors : mc + mc / 3 + 8;
             const int32_t fCap = B.split ? mcF + mcF / 3 + 8 : B.listCapF;
+            const int32_t cCap = !cluster ? B.listCapC
+                                 : cfg->initialMaxNeighbors > 0 ? (int32_t)cfg->initialMaxNeighbors
+                                                                : mcC + mcC / 3 + 8;
             Scalars z{};
             if (rc == MRMD_OK) rc = h2d(ctx, B.sc, &z, sizeof(Scalars));
-            if (rc == MRMD_OK) rc = set_capacity(ctx, b, gCap, lCap, fCap);
+            if (rc == MRMD_OK) rc = set_capacity(ctx, b, gCap, lCap, fCap, cCap);
         }
     }
     if (rc == MRMD_OK) rc = check_cuda(ctx, cudaDeviceSynchronize(), "batch create");
@@ -1755,18 +1958,36 @@ int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning*
     MRMD_TRY(validate_tuning(ctx, *t));
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     b->cfg.tuning = *t;
-    apply_layout(b);
+    MRMD_TRY(apply_layout(ctx, b));
     b->B.K = t->rebuildInterval;
     b->needRebuild = true;
     drop_graph(b);
     return ensure_ring(ctx, b);
 }
 
-int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
+int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3)
 {
-    if (!ctx || !b || !out10) return MRMD_ERR_ARG;
+    if (!ctx || !b || !out3) return MRMD_ERR_ARG;
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    MRMD_TRY(d2h(ctx, b->hSc, b->B.sc, sizeof(Scalars)));
+    if (b->cfg.tuning.listLayout == LAYOUT_CLUSTER)
+    {
+        unsigned long long* d = nullptr;
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&d), 2 * sizeof(unsigned long long)));
+        unsigned long long h[2] = {0, 0};
+        int rc = check_cuda(ctx, cudaMemsetAsync(d, 0, sizeof(h), ctx->stream), "memset");
+        if (rc == MRMD_OK)
+        {
+            k_b_cluster_stats<<<grid_for(ctx, b->B.numClusters, TB), TB, 0, ctx->stream>>>(b->B, d);
+            rc = after_launch(ctx, "batch cluster_stats");
+        }
+        if (rc == MRMD_OK) rc = d2h(ctx, h, d, sizeof(h));
+        dfree(d);
+        MRMD_TRY(rc);
+        out3[0] = (int64_t)h[0];
+        out3[1] = (int64_t)h[1];
+        out3[2] = 32;
+        return MRMD_OK;
+    }
     std::vector<int32_t> counts((size_t)b->N);
     MRMD_TRY(d2h(ctx, counts.data(), b->B.counts, sizeof(int32_t) * counts.size()));
     int64_t pairs = 0;
@@ -1776,6 +1997,19 @@ int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
         MRMD_TRY(d2h(ctx, counts.data(), b->B.countsF, sizeof(int32_t) * counts.size()));
         for (int32_t c : counts) pairs += c;
     }
+    out3[0] = pairs;
+    out3[1] = pairs;
+    out3[2] = 1;
+    return MRMD_OK;
+}
+
+int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
+{
+    if (!ctx || !b || !out10) return MRMD_ERR_ARG;
+    int64_t ls[3];
+    MRMD_TRY(mrmd_batch_list_stats(ctx, b, ls));
+    MRMD_TRY(d2h(ctx, b->hSc, b->B.sc, sizeof(Scalars)));
+    const int64_t pairs = ls[0];
     out10[0] = b->steps;
     out10[1] = b->rebuilds;
     out10[2] = pairs;
@@ -1783,7 +2017,8 @@ int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10)
     out10[4] = b->graphLaunches;
     out10[5] = ctx->launches;
     out10[6] = b->recoveries;
-    out10[7] = b->B.listCap + (b->B.split ? b->B.listCapF : 0);
+    out10[7] = b->cfg.tuning.listLayout == LAYOUT_CLUSTER ? b->B.listCapC
+                                                          : b->B.listCap + (b->B.split ? b->B.listCapF : 0);
     out10[8] = b->B.gCap;
     out10[9] = b->hSc->flags | b->hSc->overflow;
     return MRMD_OK;
@@ -1826,22 +2061,27 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
 {
     if (!ctx || !b || trialSteps < 1) return MRMD_ERR_ARG;
     const mrmd_batch_tuning t0 = b->cfg.tuning;
-    // candidates: list layout (mixed form) x lanes per row x block size x rebuild interval
+    // candidates: list layout x lanes per row x block size x rebuild interval;
+    // the near/far rows exist in the mixed form only, the cluster layout has
+    // CLUSTER_J lanes per row
     std::vector<mrmd_batch_tuning> cand;
     const int tprs[4] = {1, 2, 4, 8};
     const int blocks[3] = {64, 128, 256};
     const int64_t Ks[2] = {t0.rebuildInterval, 2 * t0.rebuildInterval};
-    const int layouts = b->cfg.precision == MRMD_PREC_MIXED ? 2 : 1;
-    for (int layout = 0; layout < layouts; ++layout)
+    std::vector<int32_t> layouts{LAYOUT_ROWS};
+    if (b->cfg.precision == MRMD_PREC_MIXED) layouts.push_back(LAYOUT_NEAR_FAR);
+    layouts.push_back(LAYOUT_CLUSTER);
+    for (int32_t layout : layouts)
         for (int64_t K : Ks)
             for (int tpr : tprs)
                 for (int bs : blocks)
                 {
+                    if (layout == LAYOUT_CLUSTER && tpr != CLUSTER_J) continue;
                     mrmd_batch_tuning t = t0;
                     t.threadsPerRow = tpr;
                     t.blockSize = bs;
                     t.rebuildInterval = K;
-                    t.listLayout = layouts > 1 ? layout : t0.listLayout;
+                    t.listLayout = layout;
                     const int64_t period = K * (t.sortEvery > 0 ? t.sortEvery : 1);
                     if (t.graphSteps > 0) t.graphSteps = ((t0.graphSteps + period - 1) / period) * period;
                     cand.push_back(t);
@@ -1860,7 +2100,8 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
     for (size_t c = 0; c < cand.size() && rc == MRMD_OK; ++c)
     {
         b->cfg.tuning = cand[c];
-        apply_layout(b);
+        rc = apply_layout(ctx, b);
+        if (rc != MRMD_OK) break;
         b->B.K = cand[c].rebuildInterval;
         b->needRebuild = true;
         drop_graph(b);
@@ -1894,7 +2135,7 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
     b->graphLaunches = gl0;
     b->recoveries = rec0;
     b->cfg.tuning = bestIdx >= 0 ? cand[(size_t)bestIdx] : t0;
-    apply_layout(b);
+    if (rc == MRMD_OK) rc = apply_layout(ctx, b);
     b->B.K = b->cfg.tuning.rebuildInterval;
     b->needRebuild = true;
     drop_graph(b);

@@ -29,7 +29,18 @@ enum : uint32_t
     FLAG_LIST_OVERFLOW = 2u,
     FLAG_UNSAFE_INTERVAL = 4u,
     FLAG_FAR_LIST_OVERFLOW = 8u,
+    FLAG_CLUSTER_LIST_OVERFLOW = 16u,
 };
+
+// list layouts (mrmd_batch_tuning::listLayout)
+enum : int32_t
+{
+    LAYOUT_ROWS = 0,      // one full row per molecule
+    LAYOUT_NEAR_FAR = 1,  // near and far rows per molecule (mixed form)
+    LAYOUT_CLUSTER = 2,   // 8 x 4 cluster pairs with a pair mask
+};
+constexpr int CLUSTER_I = 8;  // molecules of an i-cluster (rows of one warp)
+constexpr int CLUSTER_J = 4;  // cell-sorted slots of a j-cluster (lanes of one row)
 
 // Per-replica constants.
 struct RepDev
@@ -58,6 +69,7 @@ struct Scalars
     int32_t numGhost;           // total ghosts written at the last rebuild (true count on overflow)
     int32_t maxCount;           // largest list row seen (true count on overflow)
     int32_t maxCountF;          // the same for the far rows of the split layout
+    int32_t maxCountC;          // the same for the cluster-pair rows of the cluster layout
     uint32_t overflow;          // ghost / list overflow of the rebuilds since the host cleared it
     uint32_t flags;             // sticky: a molecule moved skin/2 between rebuilds
     uint32_t done;              // tail-kernel block ticket
@@ -116,7 +128,19 @@ struct BDev
     int32_t* countsF;
     int32_t* nbrsF;
     int32_t listCapF;
-    int32_t split;      // 1: near/far rows, far pairs in FP32 (mixed form only)
+    int32_t split;      // 1: near/far rows (mixed form only)
+    int32_t farF32;     // mixed form: pairs at and beyond r_split in FP32 (near/far and cluster layouts)
+    // cluster layout: i-cluster c holds the locals [clusters[c].x, clusters[c].x
+    // + clusters[c].y), at most CLUSTER_I of one replica, aligned to the
+    // replica's first molecule; its row lists cluster pairs (first sorted
+    // position of the j-cluster, pair mask, reversed mask, 0), the j-cluster
+    // being CLUSTER_J consecutive cell-sorted slots aligned to the replica's
+    // first cell; mask bit 4a + b: row a with slot b
+    int2* clusters;
+    int32_t numClusters;
+    int32_t listCapC;
+    int32_t* countsC;
+    int4* clist;
     float rsplitSq;     // r_split^2: FP32 pair arithmetic at and beyond it
     float nearSqF;      // (r_split + skin/2)^2: near rows at the rebuild
     // shadow for the cell sort of locals
@@ -269,7 +293,8 @@ int grow(mrmd_ctx* ctx, T*& p, int64_t oldCount, int64_t newCount)
 }
 
 void drop_graph(mrmd_batch* b);
-int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF = -1);
+int set_capacity(mrmd_ctx* ctx, mrmd_batch* b, int32_t gCap, int32_t listCap, int32_t listCapF = -1,
+                 int32_t listCapC = -1);
 // ghosts, cells and the list of the current local positions (no wrap), with
 // the overflow check and buffer growth of an eager step
 int rebuild_checked(mrmd_ctx* ctx, mrmd_batch* b, bool sort);

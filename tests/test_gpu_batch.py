@@ -1,6 +1,7 @@
 """Batched AdResS replicas (mrmd_batch_*): one replica against the
 oracle-driven AdResS loop, every replica of a batch bitwise against the same
-replica run alone, capacity overflow recovery, and the autotuner."""
+replica run alone, the three list layouts (rows, near/far rows, 8 x 4
+cluster pairs), capacity overflow recovery, and the autotuner."""
 import numpy as np
 import pytest
 
@@ -24,6 +25,8 @@ P = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=5, ga
 def batch(M, replicas, pos, vel, p=P, precision=None, **tuning):
     kw = dict(threads_per_row=1, block_size=128, rebuild_interval=p["K"], sort_every=0, graph_steps=p["K"])
     kw.update(tuning)
+    if kw.get("list_layout") == 2:
+        kw["threads_per_row"] = 4  # the cluster layout's 4 lanes per row
     return M.BatchSystem(replicas, pos, vel, hybrid_diameter=p["hy"], nu=p["nu"], rc=p["rc"], skin=p["skin"],
                          sigma=p["sigma"], epsilon=p["epsilon"], capping_distance=p["cap"],
                          precision=M.PREC_FP64 if precision is None else precision, dt=p["dt"],
@@ -37,13 +40,13 @@ def replica(M, n, box, at, seed, center=None):
     return M.Replica(n, [0, 0, 0], box, c, at, seed)
 
 
-@pytest.mark.parametrize("graph", [0, 5])
-def test_single_replica_matches_oracle(M, orc, graph):
+@pytest.mark.parametrize("graph,layout", [(0, 0), (5, 0), (5, 2)])
+def test_single_replica_matches_oracle(M, orc, graph, layout):
     box = [36.0, 10.0, 10.0]
     pos, vel = random_system(1800, box, 5)
     steps = 13
     po, vo, eo, fo, mo = oracle_loop(orc, pos, vel, box, steps, P)
-    b = batch(M, [replica(M, 1800, box, P["at"], P["seed"])], pos, vel, graph_steps=graph)
+    b = batch(M, [replica(M, 1800, box, P["at"], P["seed"])], pos, vel, graph_steps=graph, list_layout=layout)
     eg = b.run(steps)[:, 0]
     pg, vg, _ = b.state()
     # the compensation histogram is accumulated in 2^-32 fixed point and the
@@ -69,8 +72,9 @@ def test_slab_reaching_into_the_ghost_layer_matches_oracle(M, orc):
     pos, vel = random_system(n, box, 9)
     steps = 11
     po, vo, eo, fo, mo = oracle_loop(orc, pos, vel, box, steps, p)
-    for prec, layout, tol, etol in ((M.PREC_FP64, 0, 1e-9, 1e-9), (M.PREC_MIXED, 0, 1e-6, 1e-5),
-                                    (M.PREC_MIXED, 1, 1e-6, 1e-5)):
+    for prec, layout, tol, etol in ((M.PREC_FP64, 0, 1e-9, 1e-9), (M.PREC_FP64, 2, 1e-9, 1e-9),
+                                    (M.PREC_MIXED, 0, 1e-6, 1e-5), (M.PREC_MIXED, 1, 1e-6, 1e-5),
+                                    (M.PREC_MIXED, 2, 1e-6, 1e-5)):
         b = batch(M, [replica(M, n, box, p["at"], p["seed"])], pos, vel, p=p, precision=prec,
                   list_layout=layout)
         eg = b.run(steps)[:, 0]
@@ -93,12 +97,15 @@ def replica_set(M):
     return reps, np.concatenate(P_), np.concatenate(V_)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_split"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_split", "fp64_cluster", "mixed_cluster"])
 def test_replicas_bitwise_equal_alone(M, prec):
-    precision = M.PREC_FP64 if prec == "fp64" else M.PREC_MIXED
+    """Clusters are aligned to each replica's first molecule and first cell,
+    so the cluster layout keeps every replica's pair order too."""
+    precision = M.PREC_FP64 if prec.startswith("fp64") else M.PREC_MIXED
     reps, pos, vel = replica_set(M)
-    tune = dict(threads_per_row=2, block_size=128, rebuild_interval=5, sort_every=2, graph_steps=10,
-                list_layout=1 if prec == "mixed_split" else 0)
+    layout = 1 if prec == "mixed_split" else (2 if prec.endswith("cluster") else 0)
+    tune = dict(threads_per_row=4 if layout == 2 else 2, block_size=128, rebuild_interval=5, sort_every=2,
+                graph_steps=10, list_layout=layout)
     b = batch(M, reps, pos, vel, precision=precision, **tune)
     steps = 23
     eb = b.run(steps)
@@ -114,15 +121,15 @@ def test_replicas_bitwise_equal_alone(M, prec):
         assert np.array_equal(fa, fb[sl]), f"replica {r} forces"
         # energies are diagnostics summed with atomics (FP32 warp sums in the
         # mixed form), so they agree to rounding, not bitwise
-        np.testing.assert_allclose(eb[:, r], ea, rtol=1e-11 if prec == "fp64" else 1e-5, atol=1e-9)
+        np.testing.assert_allclose(eb[:, r], ea, rtol=1e-11 if precision == M.PREC_FP64 else 1e-5, atol=1e-9)
         ta, _ = a.thermodynamic_force()
         tb, _ = b.thermodynamic_force()
         assert np.array_equal(ta[0], tb[r])
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_mixed_close_to_fp64(M, layout):
-    """Layout 1 evaluates the pairs beyond 1.4 sigma in FP32 (near/far rows)."""
+    """Layouts 1 and 2 evaluate the pairs beyond 1.4 sigma in FP32."""
     reps, pos, vel = replica_set(M)
     a = batch(M, reps, pos, vel, precision=M.PREC_FP64)
     b = batch(M, reps, pos, vel, precision=M.PREC_MIXED, list_layout=layout)
@@ -142,18 +149,19 @@ def test_mixed_close_to_fp64(M, layout):
     assert np.abs(pa - pb).max() < 1e-7
 
 
-@pytest.mark.parametrize("prec,layout", [("fp64", 0), ("mixed", 1)])
+@pytest.mark.parametrize("prec,layout", [("fp64", 0), ("mixed", 1), ("fp64", 2), ("mixed", 2)])
 def test_capacity_overflow_recovery(M, prec, layout):
     """Ghost and list buffers that start far too small (near and far rows in
-    the split layout) grow by roll-back and re-run, bitwise like a batch that
-    never overflowed."""
+    the split layout, cluster-pair rows in the cluster layout) grow by
+    roll-back and re-run, bitwise like a batch that never overflowed."""
     precision = M.PREC_FP64 if prec == "fp64" else M.PREC_MIXED
     reps, pos, vel = replica_set(M)
     tune = dict(rebuild_interval=5, sort_every=1, graph_steps=10, list_layout=layout)
     a = batch(M, reps, pos, vel, precision=precision, **tune)
     b = M.BatchSystem(reps, pos, vel, hybrid_diameter=P["hy"], rc=P["rc"], skin=P["skin"],
                       capping_distance=P["cap"], dt=P["dt"], tf_sample_interval=P["S"], tf_update_interval=P["U"],
-                      precision=precision, threads_per_row=1, block_size=128, rebuild_interval=5, sort_every=1,
+                      precision=precision, threads_per_row=4 if layout == 2 else 1, block_size=128,
+                      rebuild_interval=5, sort_every=1,
                       graph_steps=10, list_layout=layout, initial_max_neighbors=6, initial_ghost_capacity=32)
     a.run(20)
     b.run(20)
@@ -176,3 +184,45 @@ def test_autotune_picks_a_candidate_and_keeps_the_state(M):
     assert b.stats()["steps"] == 10
     b.run(20)
     assert b.stats()["steps"] == 30
+
+
+def test_cluster_layout_lists_the_same_pairs(M):
+    """The 8 x 4 cluster rows hold exactly the pairs of the per-molecule rows
+    (the same tests per pair), and the FP64 forces of the two layouts differ
+    only by the order of the pair sums."""
+    reps, pos, vel = replica_set(M)
+    a = batch(M, reps, pos, vel, sort_every=1)
+    b = batch(M, reps, pos, vel, sort_every=1, list_layout=2)
+    a.run(1)
+    b.run(1)
+    la, lb = a.list_stats(), b.list_stats()
+    assert la["pairs"] == lb["pairs"] > 0
+    assert la["slots_per_entry"] == 1 and lb["slots_per_entry"] == 32
+    assert 0.0 < lb["lane_efficiency"] <= 1.0
+    _, _, fa = a.state()
+    _, _, fb = b.state()
+    rms = np.sqrt((fa ** 2).sum(axis=1).mean())
+    assert np.abs(fa - fb).max() / rms < 1e-12
+    a.run(9)
+    b.run(9)
+    assert a.list_stats()["pairs"] == b.list_stats()["pairs"]
+
+
+def test_layout_switch_and_bad_cluster_tuning(M):
+    """Switching layouts between runs keeps the trajectory on the FP64 path
+    (to rounding), and the cluster layout takes 4 lanes per row only."""
+    reps, pos, vel = replica_set(M)
+    a = batch(M, reps, pos, vel)
+    b = batch(M, reps, pos, vel)
+    a.run(10)
+    b.run(5)
+    b.tuning = dict(list_layout=2, threads_per_row=4)
+    b.run(5)
+    assert b.tuning["list_layout"] == 2
+    pa, _, _ = a.state()
+    pb, _, _ = b.state()
+    assert np.abs(pa - pb).max() < 1e-10
+    with pytest.raises(M.MrmdError):
+        b.tuning = dict(list_layout=2, threads_per_row=2)
+    with pytest.raises(M.MrmdError):
+        b.tuning = dict(list_layout=3, threads_per_row=4)
