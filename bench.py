@@ -308,8 +308,20 @@ ADRESS_WORKLOAD = ("AdResS LJ<->ideal gas, 34,560 single-site molecules in 120x2
                    "100 bins sampled every step / updated every 1000, rebuild/10, dt 0.005")
 
 
-def adress_initial(seed=0):
-    c = ADRESS
+def adress_config(molecules=None):
+    """The AdResS workload, or the same physics at `molecules` molecules: the
+    box, slab centre and atomistic width scaled by the same factor (density
+    0.5 kept), hybrid width and bin width unchanged."""
+    c = dict(ADRESS)
+    if molecules and molecules != c["n"]:
+        f = (molecules / c["n"]) ** (1.0 / 3.0)
+        c.update(n=int(molecules), box=tuple(x * f for x in c["box"]), center=tuple(x * f for x in c["center"]),
+                 at=c["at"] * f)
+    return c
+
+
+def adress_initial(seed=0, c=None):
+    c = c or ADRESS
     rng = np.random.default_rng(seed)
     pos = rng.uniform(0.0, 1.0, (c["n"], 3)) * np.asarray(c["box"])
     vel = mb_velocities(c["n"], c["T"], seed + 1)
@@ -387,9 +399,12 @@ def adress_main(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     ctx = M.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    c = ADRESS
-    pos, vel = adress_initial(100 + rank)
+    c = adress_config(args.molecules)
+    pos, vel = adress_initial(100 + rank, c)
     n = len(pos)
+    workload = ADRESS_WORKLOAD if n == ADRESS["n"] else (
+        f"{ADRESS_WORKLOAD}; scaled to {n:,} molecules in {c['box'][0]:.1f}x{c['box'][1]:.1f}x{c['box'][2]:.1f}, "
+        f"atomistic slab {c['at']:.1f}")
     res = {}
     for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
@@ -423,7 +438,8 @@ def adress_main(args, rank, world, local_rank):
     cpu = None
     if not args.no_cpu:
         ncores, model = cpu_info()
-        cv, done, ctime = run_adress_cpu(pos, vel, 10 ** 6, 3, args.cpu_budget, ncores)
+        geom = {k: c[k] for k in ("box", "center", "at")}
+        cv, done, ctime = run_adress_cpu(pos, vel, 10 ** 6, 3, args.cpu_budget, ncores, geom)
         cpu = {"value": cv, "unit": METRIC, "cores": ncores, "kind": "port",
                "sample": f"{done} steps of the {n}-molecule system, {ncores} OpenMP threads ({model})"}
     head = max(res, key=lambda f: res[f]["value"])
@@ -433,7 +449,7 @@ def adress_main(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if head.startswith("fp64") else "f64 state, f32 double-float pair arithmetic",
         "data": "synthetic (seeded uniform positions, Maxwell-Boltzmann velocities)",
-        "config": {"workload": ADRESS_WORKLOAD, "molecules": n, "form": head,
+        "config": {"workload": workload, "molecules": n, "form": head,
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "kernel_launches": res[f]["launches"], "list_pairs": res[f]["stats"]["pairs"],
                                  "ghost_molecules": res[f]["stats"]["ghost_molecules"]} for f in res}},
@@ -708,6 +724,8 @@ def main():
     ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff", "precision"], default="lj")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
     ap.add_argument("--replicas", type=int, default=None, help="batch workload: replica count (default 512)")
+    ap.add_argument("--molecules", type=int, default=None,
+                    help="adress workload: molecules (default 34,560; the box is scaled at density 0.5)")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")

@@ -65,6 +65,15 @@ int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams
 namespace
 {
 constexpr int MX_TB = 128;
+constexpr int LIST_PREFETCH = 4;  // list entries ahead of the pair loop
+
+// The warp's list entries k of a 32-row tile are one 128-byte line, read
+// once from DRAM: fetch the line LIST_PREFETCH entries ahead into L1.
+__device__ __forceinline__ void prefetch_list(const int32_t* col, int32_t k, int32_t cnt)
+{
+    if (k + LIST_PREFETCH < cnt)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(col + 32 * (int64_t)(k + LIST_PREFETCH)));
+}
 
 struct Acc
 {
@@ -172,6 +181,7 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
             int32_t k = 0;
             for (; k + 1 < cnt; k += 2)
             {
+                prefetch_list(col, k, cnt);
                 const int32_t j0 = __ldg(col + 32 * (int64_t)k), j1 = __ldg(col + 32 * (int64_t)(k + 1));
                 const float4 h0 = __ldg(x2 + 2 * j0), l0 = __ldg(x2 + 2 * j0 + 1);
                 const float4 h1 = __ldg(x2 + 2 * j1), l1 = __ldg(x2 + 2 * j1 + 1);
@@ -191,6 +201,7 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
             int32_t k = 0;
             for (; k + 1 < cnt; k += 2)
             {
+                prefetch_list(col, k, cnt);
                 int32_t j[2];
 #pragma unroll
                 for (int u = 0; u < 2; ++u) j[u] = __ldg(col + 32 * (int64_t)(k + u));
