@@ -624,6 +624,39 @@ def diff_main(args, rank, world, local_rank):
         res[form] = dict(loss=loss, fwd=t1 - t0, bwd=t2 - t1, launches=ctx.launches - l0, clocks=clk.summary(),
                          grad_eps=ge, grad_sigma=gs, grad_table_norm=float(np.linalg.norm(gt)))
         d.close()
+    # the table fitted by gradient descent next to the reference's iterative
+    # update, both scored with the trajectory loss (the last form)
+    fit = None
+    if args.fit_iterations > 0:
+        from mrmd_gb300.tf_fit import ThermoForceFit
+
+        tf = ThermoForceFit(rep, pos, vel, g["hy"], steps=g["steps"], window=g["window"],
+                            checkpoint_interval=g["ckpt"], loss_bins=g["loss_bins"], loss_sigma=g["loss_sigma"],
+                            tf_bin_width=g["box"][0] / g["tf_bins"], tf_target_density=c["rho"],
+                            tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], capping_distance=c["cap"],
+                            precision=prec, dt=c["dt"], gamma=c["gamma"], temperature=c["T"],
+                            rebuild_interval=g["K"], ctx=ctx)
+        t0 = time.perf_counter()
+        tg, lg = tf.gradient_descent(table, args.fit_iterations)
+        t1 = time.perf_counter()
+        tu, lu = tf.iterative_update(table, args.fit_iterations)
+        t2 = time.perf_counter()
+        tf.close()
+        # both tables scored on a held-out trajectory: same start, other noise
+        held = M.DiffSystem(M.Replica(n, [0, 0, 0], list(g["box"]), list(g["center"]), g["at"], 4321), pos, vel,
+                            hybrid_diameter=g["hy"], steps=g["steps"], window=g["window"],
+                            checkpoint_interval=g["ckpt"], loss_bins=g["loss_bins"], loss_sigma=g["loss_sigma"],
+                            capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
+                            temperature=c["T"], tf_bin_width=g["box"][0] / g["tf_bins"], rebuild_interval=g["K"],
+                            ctx=ctx)
+        heldout = {k: held.forward(t, 1.0, 1.0) for k, t in
+                   (("initial", table), ("gradient_descent", tg), ("iterative_update", tu))}
+        held.close()
+        fit = {"form": form, "iterations": args.fit_iterations, "gradient_descent_loss": lg,
+               "iterative_update_loss": lu, "gradient_descent_s": t1 - t0, "iterative_update_s": t2 - t1,
+               "held_out_loss": heldout,
+               "note": "loss[k] before iteration k; the iterative update is ThermodynamicForce::update "
+                       f"(smoothing sigma {c['tfs']}, range {c['tfr']}) after each {g['steps']}-step trajectory"}
     cpu = None
     if not args.no_cpu:
         ncores, model = cpu_info()
@@ -648,7 +681,8 @@ def diff_main(args, rank, world, local_rank):
                                  "atom_steps_per_s_gradient": n * steps / (res[f]["fwd"] + res[f]["bwd"]),
                                  "dL_depsilon": res[f]["grad_eps"], "dL_dsigma": res[f]["grad_sigma"],
                                  "norm_dL_dtable": res[f]["grad_table_norm"], "kernel_launches": res[f]["launches"]}
-                             for f in res}},
+                             for f in res},
+                   "tf_fit": fit},
         "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}
     print(json.dumps(out), flush=True)
 
@@ -730,6 +764,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")
     ap.add_argument("--forms", default="fp64,mixed")
+    ap.add_argument("--fit-iterations", type=int, default=5,
+                    help="diff workload: iterations of each table fit (0 = no fit)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -1,8 +1,9 @@
 """Adjoint of the AdResS trajectory (mrmd_diff_*): one force evaluation's
 vector-Jacobian product against central finite differences, the trajectory
 gradient against central finite differences of the GPU loss and of the
-oracle's (CPU FP64) loss, the torch.autograd shim, and a gradient-descent
-step on the thermodynamic-force table."""
+oracle's (CPU FP64) loss, the torch.autograd shim, a gradient-descent step on
+the thermodynamic-force table, and the table fit by gradient descent next to
+the reference's iterative update."""
 import numpy as np
 import pytest
 
@@ -191,3 +192,33 @@ def test_mixed_trajectory_gradient_matches_finite_differences(M):
     fs = central_fd(lambda s: d.forward(tab, 1.0, s), 1.0, h)
     assert abs(fe - ge) <= 1e-5 * abs(fe) + floor, (fe, ge)
     assert abs(fs - gs) <= 1e-5 * abs(fs) + floor, (fs, gs)
+
+
+def test_tf_fit_gradient_descent_next_to_iterative_update(M):
+    """Fitting the thermodynamic-force table (mrmd_gb300.tf_fit): the
+    reference's iterative update runs on exactly the trajectory the loss
+    scores (the batched engine reproduces the DiffSystem forward bitwise) and
+    changes the table; gradient descent on the adjoint's gradient lowers the
+    loss in every iteration it takes."""
+    from mrmd_gb300.tf_fit import ThermoForceFit
+
+    n = 2000
+    pos, vel = random_system(n, BOX, 3)
+    rep = M.Replica(n, [0, 0, 0], BOX, [BOX[0] / 2, BOX[1] / 2, BOX[2] / 2], AT, P["seed"])
+    fit = ThermoForceFit(rep, pos, vel, HY, steps=20, window=10, checkpoint_interval=5, loss_bins=32,
+                         loss_sigma=1.0, capping_distance=P["cap"], rebuild_interval=5, tf_sigma=1.0, tf_range=1.0)
+    t0 = np.zeros(fit.num_bins)
+    L0 = fit.loss(t0)
+    pd, _ = fit.diff.state()
+    t1, pb = fit.update(t0)
+    assert np.array_equal(pb, pd)
+    assert np.all(np.isfinite(t1)) and np.abs(t1).max() > 0.0
+    # the loss is summed with FP64 atomics: equal to rounding between runs
+    same = lambda a, b: abs(a - b) <= 1e-12 * abs(b)
+    tu, lu = fit.iterative_update(t0, 2)
+    assert same(lu[0], L0) and len(lu) == 3 and np.array_equal(fit.update(t0)[0], t1)
+    tg, lg = fit.gradient_descent(t0, 3)
+    assert same(lg[0], L0) and len(lg) == 4
+    assert all(b <= a * (1 + 1e-12) for a, b in zip(lg, lg[1:])) and lg[-1] < 0.999 * L0
+    assert same(fit.loss(tg), lg[-1])
+    fit.close()
