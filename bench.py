@@ -504,8 +504,9 @@ def batch_main(args, rank, world, local_rank):
                           capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
                           temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
                           tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
-                          tf_update_interval=c["U"], threads_per_row=1, block_size=128, rebuild_interval=c["K"],
-                          sort_every=5, graph_steps=BATCH["graph"], ctx=ctx)
+                          tf_update_interval=c["U"], threads_per_row=4 if args.list_layout == 2 else 1,
+                          block_size=128, rebuild_interval=c["K"], sort_every=5, graph_steps=BATCH["graph"],
+                          list_layout=args.list_layout, ctx=ctx)
         s.run(1)
         forces[form] = s.state()[2]
         s.run(BATCH["graph"] - 1)
@@ -757,6 +758,8 @@ def main():
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff", "precision"], default="lj")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: keep the default tuning")
+    ap.add_argument("--list-layout", type=int, default=0, choices=[0, 1, 2],
+                    help="batch workload: list layout before autotuning (0 rows, 1 near/far rows, 2 8x4 clusters)")
     ap.add_argument("--replicas", type=int, default=None, help="batch workload: replica count (default 512)")
     ap.add_argument("--molecules", type=int, default=None,
                     help="adress workload: molecules (default 34,560; the box is scaled at density 0.5)")
