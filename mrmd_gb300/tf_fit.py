@@ -51,6 +51,12 @@ class ThermoForceFit:
                                 tf_update_interval=self.steps, comp_frozen=True, threads_per_row=1,
                                 block_size=128, sort_every=0, graph_steps=0, list_layout=0, **physics)
 
+    def grid(self):
+        """Bin centres of the table, min + (i + 0.5) (max - min) / numBins
+        along x (MultiHistogram's createGrid), as io.write_table wants them."""
+        lo, hi = self.replica.box_min[0], self.replica.box_max[0]
+        return lo + (np.arange(self.num_bins) + 0.5) * ((hi - lo) / self.num_bins)
+
     def loss(self, table):
         """Loss of the trajectory with this table (LJ epsilon = sigma = 1)."""
         return self.diff.forward(np.asarray(table, dtype=np.float64), 1.0, 1.0)

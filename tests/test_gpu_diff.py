@@ -194,7 +194,7 @@ def test_mixed_trajectory_gradient_matches_finite_differences(M):
     assert abs(fs - gs) <= 1e-5 * abs(fs) + floor, (fs, gs)
 
 
-def test_tf_fit_gradient_descent_next_to_iterative_update(M):
+def test_tf_fit_gradient_descent_next_to_iterative_update(M, tmp_path):
     """Fitting the thermodynamic-force table (mrmd_gb300.tf_fit): the
     reference's iterative update runs on exactly the trajectory the loss
     scores (the batched engine reproduces the DiffSystem forward bitwise) and
@@ -221,4 +221,12 @@ def test_tf_fit_gradient_descent_next_to_iterative_update(M):
     assert same(lg[0], L0) and len(lg) == 4
     assert all(b <= a * (1 + 1e-12) for a, b in zip(lg, lg[1:])) and lg[-1] < 0.999 * L0
     assert same(fit.loss(tg), lg[-1])
+    # the fitted table round-trips through the reference's text format
+    from mrmd_gb300 import io
+
+    path = tmp_path / "tf.txt"
+    io.write_table(path, fit.grid(), tg, 0)
+    grid, force, bw = io.read_table(path)
+    assert force.shape == (fit.num_bins, 1) and abs(bw - BOX[0] / fit.num_bins) < 1e-5
+    np.testing.assert_allclose(force[:, 0], tg, rtol=1e-5, atol=1e-6 * np.abs(tg).max())
     fit.close()
