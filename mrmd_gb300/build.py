@@ -67,7 +67,10 @@ def build_examples() -> list[str]:
         if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
             outs.append(exe)
             continue
-        cmd = ["g++", "-O2", "-std=c++20", "-Wall", f"-I{INCLUDE}", f"-I{CPP_INCLUDE}", src, "-o", exe,
+        # mrmd/ on the include path too: drivers written against the reference
+        # include "action/LennardJones.hpp" and the like
+        cmd = ["g++", "-O2", "-std=c++20", "-Wall", f"-I{INCLUDE}", f"-I{CPP_INCLUDE}",
+               f"-I{os.path.join(CPP_INCLUDE, 'mrmd')}", src, "-o", exe,
                f"-L{PKG}", "-lmrmd_gb300", f"-Wl,-rpath,{PKG}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -1,5 +1,4 @@
-// Drop-in action::LennardJones (action/LennardJones.hpp:98-133) and
-// action::VelocityVerlet (action/VelocityVerlet.hpp:26-31).
+// Drop-in action::LennardJones (action/LennardJones.hpp:98-133).
 #pragma once
 
 #include <vector>
@@ -24,11 +23,11 @@ public:
                  const std::vector<real_t>& sigma, const std::vector<real_t>& epsilon, const idx_t& numTypes,
                  const bool isShifted)
     {
-        impl::check(mrmd_lj_create(impl::context(), &lj_, numTypes, 1, cappingDistance.data(), rc.data(),
+        gb300::check(mrmd_lj_create(gb300::context(), &lj_, numTypes, 1, cappingDistance.data(), rc.data(),
                                    sigma.data(), epsilon.data(), isShifted ? 1 : 0),
                     "LennardJones");
     }
-    ~LennardJones() { mrmd_lj_destroy(impl::context(), lj_); }
+    ~LennardJones() { mrmd_lj_destroy(gb300::context(), lj_); }
     LennardJones(const LennardJones&) = delete;
     LennardJones& operator=(const LennardJones&) = delete;
 
@@ -36,7 +35,7 @@ public:
 
     void apply_if(const data::Atoms& atoms, const HalfVerletList& verletList, const TwoPositionsPredicate& pred)
     {
-        impl::check(mrmd_lj_apply(impl::context(), lj_, const_cast<mrmd_atoms*>(atoms.raw()), verletList.raw(),
+        gb300::check(mrmd_lj_apply(gb300::context(), lj_, const_cast<mrmd_atoms*>(atoms.raw()), verletList.raw(),
                                   &pred.p, precision, &energy_, &virial_),
                     "LennardJones::apply_if");
     }
@@ -51,51 +50,9 @@ private:
     real_t energy_ = 0_r;
     real_t virial_ = 0_r;
 };
-
-class VelocityVerlet
-{
-public:
-    static real_t preForceIntegrate(data::Atoms& atoms, const real_t dt)
-    {
-        real_t maxDisp = 0_r;
-        impl::check(mrmd_vv_pre(impl::context(), atoms.raw(), dt, &maxDisp), "preForceIntegrate");
-        return maxDisp;
-    }
-    static void postForceIntegrate(data::Atoms& atoms, const real_t dt)
-    {
-        impl::check(mrmd_vv_post(impl::context(), atoms.raw(), dt), "postForceIntegrate");
-    }
-};
-
-// VelocityVerletLangevinThermostat (action/VelocityVerletLangevinThermostat.hpp:29-121)
-// with reproducible Philox noise keyed by (seed, step).
-class VelocityVerletLangevinThermostat
-{
-public:
-    VelocityVerletLangevinThermostat(const real_t& zeta, const real_t& temperature) { set(zeta, temperature); }
-    void set(const real_t& zeta, const real_t& temperature)
-    {
-        zeta_ = zeta;
-        temperature_ = temperature;
-    }
-    real_t preForceIntegrate(data::Atoms& atoms, const real_t dt)
-    {
-        return preForceIntegrate_apply_if(atoms, dt, mrmd_pred{MRMD_PRED_ALWAYS, 0, 0, 0, 0, 0});
-    }
-    real_t preForceIntegrate_apply_if(data::Atoms& atoms, const real_t dt, const mrmd_pred& pred)
-    {
-        real_t maxDisp = 0_r;
-        impl::check(mrmd_langevin_pre(impl::context(), atoms.raw(), dt, zeta_, temperature_, seed, step_++, &pred,
-                                      &maxDisp),
-                    "preForceIntegrate");
-        return maxDisp;
-    }
-    void postForceIntegrate(data::Atoms& atoms, const real_t dt) { VelocityVerlet::postForceIntegrate(atoms, dt); }
-
-    uint64_t seed = 1234;  // the reference seeds its pool with 1234 (:32)
-
-private:
-    real_t zeta_ = 0_r, temperature_ = 0_r;
-    uint64_t step_ = 0;
-};
 }  // namespace mrmd::action
+
+// The integrators have their own headers, as in the reference; they are
+// included here too for drivers that reach them through this one.
+#include "VelocityVerlet.hpp"
+#include "VelocityVerletLangevinThermostat.hpp"

@@ -10,26 +10,26 @@ namespace mrmd::communication
 class GhostLayer
 {
 public:
-    GhostLayer() { impl::check(mrmd_ghost_layer_alloc(impl::context(), &g_, 1), "GhostLayer"); }
-    ~GhostLayer() { mrmd_ghost_layer_free(impl::context(), &g_); }
+    GhostLayer() { gb300::check(mrmd_ghost_layer_alloc(gb300::context(), &g_, 1), "GhostLayer"); }
+    ~GhostLayer() { mrmd_ghost_layer_free(gb300::context(), &g_); }
     GhostLayer(const GhostLayer&) = delete;
     GhostLayer& operator=(const GhostLayer&) = delete;
 
     void exchangeRealAtoms(data::Atoms& atoms, const data::Subdomain& subdomain)
     {
-        impl::check(mrmd_ghost_exchange_real_atoms(impl::context(), atoms.raw(), &subdomain.s), "exchangeRealAtoms");
+        gb300::check(mrmd_ghost_exchange_real_atoms(gb300::context(), atoms.raw(), &subdomain.s), "exchangeRealAtoms");
     }
     void createGhostAtoms(data::Atoms& atoms, const data::Subdomain& subdomain)
     {
-        impl::check(mrmd_ghost_create(impl::context(), &g_, atoms.raw(), &subdomain.s), "createGhostAtoms");
+        gb300::check(mrmd_ghost_create(gb300::context(), &g_, atoms.raw(), &subdomain.s), "createGhostAtoms");
     }
     void updateGhostAtoms(data::Atoms& atoms, const data::Subdomain& subdomain)
     {
-        impl::check(mrmd_ghost_update(impl::context(), &g_, atoms.raw(), &subdomain.s), "updateGhostAtoms");
+        gb300::check(mrmd_ghost_update(gb300::context(), &g_, atoms.raw(), &subdomain.s), "updateGhostAtoms");
     }
     void contributeBackGhostToReal(data::Atoms& atoms)
     {
-        impl::check(mrmd_ghost_reduce_force(impl::context(), &g_, atoms.raw()), "contributeBackGhostToReal");
+        gb300::check(mrmd_ghost_reduce_force(gb300::context(), &g_, atoms.raw()), "contributeBackGhostToReal");
     }
 
 protected:
@@ -41,12 +41,12 @@ class MultiResGhostLayer : public GhostLayer
 public:
     void exchangeRealAtoms(data::Molecules& molecules, data::Atoms& atoms, const data::Subdomain& subdomain)
     {
-        impl::check(mrmd_multires_exchange_real_atoms(impl::context(), molecules.raw(), atoms.raw(), &subdomain.s),
+        gb300::check(mrmd_multires_exchange_real_atoms(gb300::context(), molecules.raw(), atoms.raw(), &subdomain.s),
                     "exchangeRealAtoms");
     }
     void createGhostAtoms(data::Molecules& molecules, data::Atoms& atoms, const data::Subdomain& subdomain)
     {
-        impl::check(mrmd_multires_ghost_create(impl::context(), &g_, molecules.raw(), atoms.raw(), &subdomain.s),
+        gb300::check(mrmd_multires_ghost_create(gb300::context(), &g_, molecules.raw(), atoms.raw(), &subdomain.s),
                     "createGhostAtoms");
     }
 };

@@ -10,7 +10,7 @@ struct Subdomain
     Subdomain() = default;
     Subdomain(const Point3D& minCornerArg, const Point3D& maxCornerArg, const Vector3D& ghostLayerThicknessArg)
     {
-        impl::check(mrmd_subdomain_init(&s, minCornerArg.data(), maxCornerArg.data(), ghostLayerThicknessArg.data()),
+        gb300::check(mrmd_subdomain_init(&s, minCornerArg.data(), maxCornerArg.data(), ghostLayerThicknessArg.data()),
                     "Subdomain");
         for (int d = 0; d < 3; ++d)
         {

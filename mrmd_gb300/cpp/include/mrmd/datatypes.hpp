@@ -37,7 +37,10 @@ public:
     int code;
 };
 
-namespace impl
+// The drop-in's own helpers live in mrmd::gb300, a namespace the reference
+// does not use (its mrmd::*::impl namespaces hold its own internals, such as
+// action::impl::CoulombDSF).
+namespace gb300
 {
 inline mrmd_ctx* context();  // process-wide context on device 0 (initialization.cpp:23-44)
 
@@ -56,7 +59,7 @@ inline mrmd_ctx* context()
     }();
     return ctx;
 }
-}  // namespace impl
+}  // namespace gb300
 
 // Two-position predicates for LennardJones::apply_if: the in-tree callers use
 // util::IsInSymmetricSlab combined with || or && (examples/04:206-227).
@@ -69,8 +72,8 @@ struct TwoPositionsPredicate
 class HalfVerletList
 {
 public:
-    HalfVerletList() { impl::check(mrmd_nlist_init(impl::context(), &list_), "HalfVerletList"); }
-    ~HalfVerletList() { mrmd_nlist_free(impl::context(), &list_); }
+    HalfVerletList() { gb300::check(mrmd_nlist_init(gb300::context(), &list_), "HalfVerletList"); }
+    ~HalfVerletList() { mrmd_nlist_free(gb300::context(), &list_); }
     HalfVerletList(const HalfVerletList&) = delete;
     HalfVerletList& operator=(const HalfVerletList&) = delete;
 
@@ -80,7 +83,7 @@ public:
     void build(const double* positions, idx_t numPositions, idx_t begin, idx_t end, real_t cutoff,
                real_t cellRatio, const real_t* gridMin, const real_t* gridMax, idx_t maxNeigh = 60)
     {
-        impl::check(mrmd_nlist_build(impl::context(), &list_, positions, numPositions, begin, end, cutoff,
+        gb300::check(mrmd_nlist_build(gb300::context(), &list_, positions, numPositions, begin, end, cutoff,
                                      cellRatio, gridMin, gridMax, maxNeigh),
                     "HalfVerletList::build");
     }

@@ -13,13 +13,13 @@ namespace io
 inline void dumpThermoForce(const std::string& filename, const action::ThermodynamicForce& thermodynamicForce,
                             const idx_t& typeId)
 {
-    impl::check(mrmd_tf_dump(impl::context(), thermodynamicForce.raw(), filename.c_str(), typeId),
+    gb300::check(mrmd_tf_dump(gb300::context(), thermodynamicForce.raw(), filename.c_str(), typeId),
                 "dumpThermoForce");
 }
 
 inline void dumpThermoForce(const std::string& filename, const action::ThermodynamicForce& thermodynamicForce)
 {
-    impl::check(mrmd_tf_dump(impl::context(), thermodynamicForce.raw(), filename.c_str(), -1), "dumpThermoForce");
+    gb300::check(mrmd_tf_dump(gb300::context(), thermodynamicForce.raw(), filename.c_str(), -1), "dumpThermoForce");
 }
 }  // namespace io
 }  // namespace mrmd

@@ -24,7 +24,7 @@ inline action::ThermodynamicForce restoreThermoForce(
     if (targetDensities.size() != thermodynamicForceModulations.size())
         throw Error(MRMD_ERR_ARG, "restoreThermoForce: one modulation per target density");
     mrmd_tf* tf = nullptr;
-    impl::check(mrmd_tf_restore(impl::context(), &tf, filename.c_str(), &subdomain.s, idx_t(targetDensities.size()),
+    gb300::check(mrmd_tf_restore(gb300::context(), &tf, filename.c_str(), &subdomain.s, idx_t(targetDensities.size()),
                                 targetDensities.data(), thermodynamicForceModulations.data(),
                                 enforceSymmetry ? 1 : 0, usePeriodicity ? 1 : 0, maxNumForces),
                 "restoreThermoForce");
