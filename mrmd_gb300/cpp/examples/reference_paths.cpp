@@ -39,6 +39,7 @@
 #include "data/Molecules.hpp"
 #include "data/Subdomain.hpp"
 #include "datatypes.hpp"
+#include "initialization.hpp"
 #include "weighting_function/Slab.hpp"
 
 using namespace mrmd;
@@ -262,11 +263,13 @@ int main(int argc, char** argv)
     std::string json = "{";
     try
     {
+        mrmd::initialize(argc, argv);
         if (nve(json)) return 1;
         json += ", ";
         if (adress(argv[1], json)) return 1;
         json += ", ";
         coulomb(json);
+        mrmd::finalize();
     }
     catch (const Error& e)
     {
