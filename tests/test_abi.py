@@ -65,3 +65,21 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_abi, "_lib", None)
     with pytest.raises(_abi.MrmdError):
         _abi.lib()
+
+
+def test_library_exports_nothing_undeclared(lib):
+    """Every exported mrmd_* symbol is declared in include/*.h: no entry point
+    outside the documented boundary."""
+    import shutil
+    import subprocess
+
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    from mrmd_gb300 import build as B
+
+    out = subprocess.run([nm, "-D", "--defined-only", B.LIB], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.split() and line.split()[-1].startswith("mrmd_")}
+    assert exported, "no mrmd_* exports found"
+    undeclared = sorted(exported - set(declared_functions()))
+    assert not undeclared, undeclared
