@@ -406,6 +406,7 @@ def adress_main(args, rank, world, local_rank):
         f"{ADRESS_WORKLOAD}; scaled to {n:,} molecules in {c['box'][0]:.1f}x{c['box'][1]:.1f}x{c['box'][2]:.1f}, "
         f"atomistic slab {c['at']:.1f}")
     res = {}
+    forces = {}
     for form in [f.strip() for f in args.forms.split(",") if f.strip()]:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
         s = M.AdResSSystem(pos, vel, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], c["hy"], c["nu"],
@@ -427,7 +428,11 @@ def adress_main(args, rank, world, local_rank):
                           temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
                           tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
                           tf_update_interval=c["U"], rebuild_interval=c["K"], sort_every=5, graph_steps=50, ctx=ctx)
-        b.run(max(args.warmup, 50), energies=False)
+        # the first step's forces act on identical positions in both forms (the
+        # pre-force integration is FP64 in both)
+        b.run(1, energies=False)
+        forces[form] = b.state()[2]
+        b.run(max(args.warmup, 50) - 1, energies=False)
         with ClockSampler(local_rank) as clk:
             ms, wall, e, launches = time_run(torch, M, b, args.steps, stream)
         st = b.stats()
@@ -435,6 +440,14 @@ def adress_main(args, rank, world, local_rank):
                                            clocks=clk.summary(), stats={"pairs": st["pairs"],
                                                                         "ghost_molecules": st["ghost_molecules"]})
         b.close()
+    ferr = None
+    if "fp64" in forces and "mixed" in forces:
+        fa, fb = forces["fp64"], forces["mixed"]
+        d = np.linalg.norm(fa - fb, axis=1)
+        mag = np.linalg.norm(fa, axis=1)
+        rms = float(np.sqrt((mag ** 2).mean()))
+        ferr = {"max_abs_over_rms": float(d.max() / rms),
+                "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
     cpu = None
     if not args.no_cpu:
         ncores, model = cpu_info()
@@ -452,7 +465,8 @@ def adress_main(args, rank, world, local_rank):
         "config": {"workload": workload, "molecules": n, "form": head,
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "kernel_launches": res[f]["launches"], "list_pairs": res[f]["stats"]["pairs"],
-                                 "ghost_molecules": res[f]["stats"]["ghost_molecules"]} for f in res}},
+                                 "ghost_molecules": res[f]["stats"]["ghost_molecules"]} for f in res},
+                   "force_error_mixed_vs_fp64": ferr},
         "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": cpu}), flush=True)
 
 
