@@ -570,7 +570,8 @@ typedef struct {
                                  as 0); 2 = 8 x 4 cluster pairs: one warp per 8 molecules,
                                  a row of (4-slot j-cluster, 32-bit pair mask) entries,
                                  threadsPerRow 4 (mixed form: pairs beyond 1.4 sigma in
-                                 FP32) */
+                                 FP32); its clusters are compact only for molecules in
+                                 cell order (sortEvery > 0, or given in cell order) */
     int32_t reserved0;
 } mrmd_batch_tuning;
 
