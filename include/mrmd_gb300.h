@@ -259,10 +259,10 @@ typedef struct {
 
 typedef struct mrmd_lj mrmd_lj;
 /* LennardJones(cappingDistance, rc, sigma, epsilon, numTypes, isShifted)
- * (action/LennardJones.hpp:127-132, LennardJones.cpp:254-324): vectors of
+ * (action/LennardJones.hpp:127-132, LennardJones.cpp:46-56,81-116): vectors of
  * numTypes^2 entries.  numTypesIndex is the multiplier of type_i in the
  * table index (the reference's LennardJones fixes it to 1,
- * LennardJones.cpp:260; LJ_IdealGas uses numTypes, LJ_IdealGas.cpp:139). */
+ * action/LennardJones.cpp:52; LJ_IdealGas uses numTypes, LJ_IdealGas.cpp:139). */
 int mrmd_lj_create(mrmd_ctx* ctx, mrmd_lj** out, int64_t numTypes, int64_t numTypesIndex,
                    const double* cappingDistance, const double* rc, const double* sigma,
                    const double* epsilon, int isShifted);

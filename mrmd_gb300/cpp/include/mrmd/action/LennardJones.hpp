@@ -18,7 +18,7 @@ public:
     {
     }
     // LennardJones(cappingDistance[], rc[], sigma[], epsilon[], numTypes, isShifted);
-    // the reference indexes its table with numTypes_ fixed to 1 (LennardJones.cpp:260)
+    // the reference indexes its table with numTypes_ fixed to 1 (action/LennardJones.cpp:52)
     LennardJones(const std::vector<real_t>& cappingDistance, const std::vector<real_t>& rc,
                  const std::vector<real_t>& sigma, const std::vector<real_t>& epsilon, const idx_t& numTypes,
                  const bool isShifted)

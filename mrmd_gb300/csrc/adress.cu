@@ -73,7 +73,8 @@ struct LJIGArgs
     const int32_t* counts;
     const int32_t* nbrs;
     int64_t cap;
-    int64_t nMol;
+    int64_t nMol;      // list rows
+    int64_t begin;     // molecule of list row 0
     const LJDev* table;
     int32_t numTypes;
     double rcSqr;
@@ -91,19 +92,20 @@ __global__ void __launch_bounds__(128) k_ljig(LJIGArgs A)
     // action/LJ_IdealGas.cpp:52-225, one thread per local molecule alpha
     __shared__ double red[64];
     double sumEnergy = 0.0, dummy = 0.0;
-    const int64_t alpha = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (alpha < A.nMol)
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row < A.nMol)
     {
+        const int64_t alpha = A.begin + row;
         double fA[3] = {0.0, 0.0, 0.0};
         const double modA = A.m.modulatedLambda[alpha];
         int binAlpha = -1;
         if (is_hy(modA)) binAlpha = comp_bin(A.m.lambda[alpha]);
         const double4 gA = reinterpret_cast<const double4*>(A.m.gradLambda)[alpha];
         const int64_t sA = A.m.atomsOffset[alpha], eA = sA + A.m.numAtoms[alpha];
-        const int32_t cnt = A.counts[alpha];
+        const int32_t cnt = A.counts[row];
         for (int32_t k = 0; k < cnt; ++k)
         {
-            const int64_t beta = A.nbrs[mrmd_dev::nbr_row(alpha, A.cap) + 32 * (int64_t)k];
+            const int64_t beta = A.nbrs[mrmd_dev::nbr_row(row, A.cap) + 32 * (int64_t)k];
             double fB[3] = {0.0, 0.0, 0.0};
             const double modB = A.m.modulatedLambda[beta];
             if (is_cg(modA) && is_cg(modB)) continue;
@@ -322,6 +324,7 @@ int ljig_run_async(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nl
     A.nbrs = nl->nbrs;
     A.cap = nl->maxNeighbors;
     A.nMol = nl->rows;
+    A.begin = nl->begin;
     A.table = s->dTable;
     A.numTypes = (int32_t)s->numTypes;
     A.rcSqr = s->rcSqr;
@@ -377,7 +380,7 @@ int mrmd_ljig_run(mrmd_ctx* ctx, mrmd_ljig* s, mrmd_molecules* m, const mrmd_nli
     // action/LJ_IdealGas.cpp:227-260
     if (!ctx || !s || !m || !nl || !a) return MRMD_ERR_ARG;
     MRMD_CHECK_ARG(precision == MRMD_PREC_FP64 || precision == MRMD_PREC_MIXED, ctx, "bad precision");
-    MRMD_CHECK_ARG(nl->rows <= m->numLocal, ctx, "list has more rows than local molecules");
+    MRMD_TRY(check_list_fits(ctx, nl, m->numLocal, m->numLocal + m->numGhost));
     double* ev = ctx->devScalars + 32;
     MRMD_CUDA(ctx, cudaMemsetAsync(ev, 0, sizeof(double), ctx->stream));
     MRMD_TRY(ljig_run_async(ctx, s, m, nl, a, precision, ev, nullptr, nullptr));

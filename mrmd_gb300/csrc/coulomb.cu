@@ -12,6 +12,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "nlist_impl.cuh"
 
 using namespace mrmd_impl;
 
@@ -62,18 +63,19 @@ __global__ void __launch_bounds__(TBC) k_dsf_apply(const double4* __restrict__ p
                                                   const double* __restrict__ charge, const mrmd_coulomb_dsf_params c,
                                                   const int32_t* __restrict__ counts,
                                                   const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
-                                                  double* __restrict__ ev)
+                                                  int64_t begin, double* __restrict__ ev)
 {
     __shared__ double red[64];
     double energy = 0.0, virial = 0.0;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n)
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row < n)
     {
+        const int64_t i = begin + row;  // list row `row` belongs to particle begin + row
         const double4 pi = pos[i];
         const double qi = charge[i];
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        const int32_t cnt = counts[i];
-        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
+        const int32_t cnt = counts[row];
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(row, cap);
         for (int32_t k = 0; k < cnt; ++k)
         {
             const int32_t j = __ldg(col + 32 * (int64_t)k);
@@ -145,7 +147,7 @@ int mrmd_coulomb_dsf_apply(mrmd_ctx* ctx, const mrmd_coulomb_dsf_params* c, mrmd
                            double* energy, double* virial)
 {
     if (!ctx || !c || !a || !nl) return MRMD_ERR_ARG;
-    MRMD_CHECK_ARG(nl->rows <= a->numLocal, ctx, "list has more rows than local atoms");
+    MRMD_TRY(check_list_fits(ctx, nl, a->numLocal, a->numLocal + a->numGhost));
     double* ev = ctx->devScalars + 12;
     MRMD_CUDA(ctx, cudaMemsetAsync(ev, 0, 2 * sizeof(double), ctx->stream));
     const int64_t n = nl->rows;
@@ -153,7 +155,7 @@ int mrmd_coulomb_dsf_apply(mrmd_ctx* ctx, const mrmd_coulomb_dsf_params* c, mrmd
     {
         k_dsf_apply<<<(unsigned)div_up(n, TBC), TBC, 0, ctx->stream>>>(
             reinterpret_cast<const double4*>(a->pos), a->force, a->charge, *c, nl->counts, nl->nbrs,
-            nl->maxNeighbors, n, ev);
+            nl->maxNeighbors, n, nl->begin, ev);
         MRMD_TRY(after_launch(ctx, "coulomb_dsf"));
     }
     if (energy || virial)

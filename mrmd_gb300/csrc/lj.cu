@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "lj_impl.cuh"
+#include "nlist_impl.cuh"
 
 using namespace mrmd_impl;
 
@@ -34,7 +35,7 @@ void lj_force_energy_host(const mrmd_lj_params* t, double distSqr, int64_t typeI
 void lj_table_host(mrmd_lj_params* out, int64_t numTypes, const double* cap, const double* rc,
                    const double* sigma, const double* epsilon, int isShifted)
 {
-    // constructor action/LennardJones.cpp:289-324, precompute :269-287
+    // constructor action/LennardJones.cpp:81-116, precompute :61-79
     for (int64_t t = 0; t < numTypes * numTypes; ++t)
     {
         const double sig2 = sigma[t] * sigma[t];
@@ -75,18 +76,20 @@ __global__ void __launch_bounds__(LJ_TB) k_lj_fp64(
     const double4* __restrict__ pos, double* __restrict__ force, const int32_t* __restrict__ type,
     const LJDev p0, const LJDev* __restrict__ table, int32_t numTypesIndex, double rcSqr,
     const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
-    mrmd_dev::Pred pred, double* __restrict__ ev)
+    int64_t begin, mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
     double energy = 0.0, virial = 0.0;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n)
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row < n)
     {
+        // list row `row` belongs to particle begin + row (the list's range)
+        const int64_t i = begin + row;
         const double4 pi = pos[i];
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        const int32_t cnt = counts[i];
+        const int32_t cnt = counts[row];
         const int32_t ti = MULTI ? type[i] * numTypesIndex : 0;
-        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(row, cap);
         for (int32_t k = 0; k < cnt; ++k)
         {
             const int32_t j = __ldg(col + 32 * (int64_t)k);
@@ -136,7 +139,7 @@ int lj_apply_fp64(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_nl
 #define LJ_LAUNCH(P, M)                                                                                \
     k_lj_fp64<P, M><<<grid, LJ_TB, 0, ctx->stream>>>(pos, a->force, a->type, lj->p0, lj->dTable,         \
                                                      (int32_t)lj->numTypesIndex, lj->rcSqr, nl->counts, \
-                                                     nl->nbrs, nl->maxNeighbors, n, dp, ev)
+                                                     nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev)
     if (usePred && multi) LJ_LAUNCH(true, true);
     else if (usePred) LJ_LAUNCH(true, false);
     else if (multi) LJ_LAUNCH(false, true);
@@ -164,7 +167,7 @@ int mrmd_lj_create(mrmd_ctx* ctx, mrmd_lj** out, int64_t numTypes, int64_t numTy
     lj_table_host(lj->table.data(), numTypes, cappingDistance, rc, sigma, epsilon, isShifted);
     double rcMax = rc[0];
     for (int64_t t = 1; t < n2; ++t) rcMax = std::fmax(rcMax, rc[t]);
-    lj->rcSqr = rcMax * rcMax;  // LennardJones.cpp:262-263
+    lj->rcSqr = rcMax * rcMax;  // action/LennardJones.cpp:54-55
     std::vector<LJDev> dev((size_t)n2);
     for (int64_t t = 0; t < n2; ++t) dev[(size_t)t] = to_dev(lj->table[(size_t)t]);
     lj->p0 = dev[0];
@@ -204,7 +207,7 @@ int mrmd_lj_apply(mrmd_ctx* ctx, mrmd_lj* lj, mrmd_atoms* a, const mrmd_nlist* n
     if (!ctx || !lj || !a || !nl) return MRMD_ERR_ARG;
     MRMD_CHECK_ARG(pred_valid(pred), ctx, "bad predicate");
     MRMD_CHECK_ARG(precision == MRMD_PREC_FP64 || precision == MRMD_PREC_MIXED, ctx, "bad precision");
-    MRMD_CHECK_ARG(nl->rows <= a->numLocal, ctx, "list has more rows than local atoms");
+    MRMD_TRY(check_list_fits(ctx, nl, a->numLocal, a->numLocal + a->numGhost));
     double* ev = ctx->devScalars + 16;
     MRMD_CUDA(ctx, cudaMemsetAsync(ev, 0, 2 * sizeof(double), ctx->stream));
     if (precision == MRMD_PREC_FP64)

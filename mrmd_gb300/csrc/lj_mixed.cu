@@ -100,18 +100,21 @@ template <bool PRED>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
     double* __restrict__ force, const LJDev p, RcSq rc2, const int32_t* __restrict__ counts,
-    const int32_t* __restrict__ nbrs, int64_t cap, int64_t n, mrmd_dev::Pred pred, double* __restrict__ ev)
+    const int32_t* __restrict__ nbrs, int64_t cap, int64_t n, int64_t begin, mrmd_dev::Pred pred,
+    double* __restrict__ ev)
 {
     __shared__ double red[64];
     Acc acc;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n)
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row < n)
     {
+        // list row `row` belongs to particle begin + row (the list's range)
+        const int64_t i = begin + row;
         const float4 hi_i = hi[i], lo_i = lo[i];
         double4 pi;
         if (PRED) pi = pos[i];
-        const int32_t cnt = counts[i];
-        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(i, cap);
+        const int32_t cnt = counts[row];
+        const int32_t* __restrict__ col = nbrs + mrmd_dev::nbr_row(row, cap);
         for (int32_t k = 0; k < cnt; ++k)
         {
             const int32_t j = __ldg(col + 32 * (int64_t)k);
@@ -280,10 +283,10 @@ int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_
     const double4* pos = reinterpret_cast<const double4*>(a->pos);
     if (usePred)
         k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                               nl->nbrs, nl->maxNeighbors, n, dp, ev);
+                                                               nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev);
     else
         k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                                nl->nbrs, nl->maxNeighbors, n, dp, ev);
+                                                                nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev);
     return after_launch(ctx, "lj_mixed_half");
 }
 

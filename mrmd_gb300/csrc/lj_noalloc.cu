@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
+#include "nlist_impl.cuh"
 
 using namespace mrmd_impl;
 
@@ -67,7 +68,7 @@ int mrmd_lj_apply_mixed_noalloc(mrmd_ctx* ctx, mrmd_lj* lj, mrmd_atoms* a, const
 {
     if (!ctx || !lj || !a || !nl) return MRMD_ERR_ARG;
     MRMD_CHECK_ARG(pred_valid(pred), ctx, "bad predicate");
-    MRMD_CHECK_ARG(nl->rows <= a->numLocal, ctx, "list has more rows than local atoms");
+    MRMD_TRY(check_list_fits(ctx, nl, a->numLocal, a->numLocal + a->numGhost));
     if (lj->numTypes > 1) return set_error(ctx, MRMD_ERR_ARG, "mixed precision supports one atom type");
     const int64_t nAll = a->numLocal + a->numGhost;
     if (nAll > MRMD_LJ_NOALLOC_MAX_ATOMS)

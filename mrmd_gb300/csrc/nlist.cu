@@ -60,14 +60,18 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v)
 
 // morton != 0: the key is the Morton (Z-order) code of the cell coordinates,
 // so that particles sorted by it form compact blocks in space.
+// nonfinite (may be null): set to 1 when a position is NaN or infinite (such
+// a particle is binned into a clamped cell and never becomes a neighbour).
 __global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGrid g,
-                             int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount, int morton)
+                             int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount, int morton,
+                             int32_t* __restrict__ nonfinite)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
         int32_t c;
         const double4 p = pos[i];
+        if (nonfinite && !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) *nonfinite = 1;
         if (morton)
         {
             const uint32_t cx = (uint32_t)cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x);
@@ -223,7 +227,8 @@ __global__ void __launch_bounds__(128) k_build_list(
     }
 }
 
-int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton)
+int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton,
+                    int32_t* nonfinite)
 {
     g = grid;
     // Morton keys need at most 10 bits per axis; the key range is then a
@@ -263,7 +268,8 @@ int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid
     if (n > 0)
     {
         k_cell_count<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n,
-                                                                   g, cellOf, cellStart, morton ? 1 : 0);
+                                                                   g, cellOf, cellStart, morton ? 1 : 0,
+                                                                   nonfinite);
         MRMD_TRY(after_launch(ctx, "cell_count"));
     }
     MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, nkeys + 1, nullptr));
@@ -323,7 +329,10 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
                     int64_t end, double rlist, const CellGrid& grid, int64_t maxNeighbors, bool full)
 {
     CellList* cl = static_cast<CellList*>(nl->cells);
-    MRMD_TRY(cl->build(ctx, pos4, nPos, grid));
+    // [0] longest row, [2] non-finite position flag
+    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
+    MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 3 * sizeof(int32_t), ctx->stream));
+    MRMD_TRY(cl->build(ctx, pos4, nPos, grid, false, maxCount + 2));
     const int64_t rows = end - begin;
     // FP32 error band: coordinates are stored relative to the grid origin
     // (|c| <= extent), each rounding error <= 2^-24 |c|, so |dx_f - dx| <=
@@ -334,7 +343,6 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
     const double rsq = rlist * rlist;
     const float rsqLo = (float)std::fmax(0.0, (rsq - 2.0 * band) * (1.0 - 1e-6));
     const float rsqHi = (float)((rsq + 2.0 * band) * (1.0 + 1e-6));
-    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
     int64_t cap = maxNeighbors > 0 ? maxNeighbors : 64;
     for (int attempt = 0; attempt < 4; ++attempt)
     {
@@ -352,9 +360,11 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
                     end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount);
             MRMD_TRY(after_launch(ctx, "build_list"));
         }
-        int32_t hMax = 0;
-        MRMD_CUDA(ctx, cudaMemcpyAsync(&hMax, maxCount, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        int32_t h[3] = {0, 0, 0};
+        MRMD_CUDA(ctx, cudaMemcpyAsync(h, maxCount, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (h[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
+        const int32_t hMax = h[0];
         if (hMax <= cap)
         {
             nl->rows = rows;
@@ -380,7 +390,10 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
                      int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid)
 {
     CellList* cl = static_cast<CellList*>(nearList->cells);
-    MRMD_TRY(cl->build(ctx, pos4, nPos, grid));
+    // [0], [1] longest near and far rows, [2] non-finite position flag
+    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
+    MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 3 * sizeof(int32_t), ctx->stream));
+    MRMD_TRY(cl->build(ctx, pos4, nPos, grid, false, maxCount + 2));
     const int64_t rows = end - begin;
     // the same FP32 error band as build_half_list
     const double delta = std::ldexp(grid.extent, -22);
@@ -389,7 +402,6 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
     const float rsqLo = (float)std::fmax(0.0, (rsq - 2.0 * band) * (1.0 - 1e-6));
     const float rsqHi = (float)((rsq + 2.0 * band) * (1.0 + 1e-6));
     const float nearSqF = (float)(rnear * rnear);
-    int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
     int64_t capN = nearList->maxNeighbors > 0 ? nearList->maxNeighbors : 32;
     int64_t capF = farList->maxNeighbors > 0 ? farList->maxNeighbors : 64;
     for (int attempt = 0; attempt < 4; ++attempt)
@@ -405,9 +417,10 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
                 farList->counts, farList->nbrs);
             MRMD_TRY(after_launch(ctx, "build_split_list"));
         }
-        int32_t hMax[2] = {0, 0};
-        MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        int32_t hMax[3] = {0, 0, 0};
+        MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hMax[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
         if (hMax[0] <= capN && hMax[1] <= capF)
         {
             nearList->rows = farList->rows = rows;
@@ -433,6 +446,19 @@ int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl)
     MRMD_CUDA(ctx, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     nl->totalPairs = (int64_t)h;
+    return MRMD_OK;
+}
+
+int check_list_fits(mrmd_ctx* ctx, const mrmd_nlist* nl, int64_t numLocal, int64_t nAll)
+{
+    if (nl->begin < 0 || nl->rows < 0 || nl->begin + nl->rows > numLocal)
+        return set_error(ctx, MRMD_ERR_ARG, "list rows [%lld, %lld) exceed the %lld local particles",
+                         (long long)nl->begin, (long long)(nl->begin + nl->rows), (long long)numLocal);
+    const CellList* cl = static_cast<const CellList*>(nl->cells);
+    if (nl->rows > 0 && cl && cl->numParticles > nAll)
+        return set_error(ctx, MRMD_ERR_ARG,
+                         "list was built over %lld particles but only %lld (local + ghost) are present",
+                         (long long)cl->numParticles, (long long)nAll);
     return MRMD_OK;
 }
 

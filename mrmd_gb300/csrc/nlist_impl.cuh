@@ -53,7 +53,10 @@ struct CellList
 
     // morton: order the cells along a Z-order curve instead of row-major (for
     // sorting particles; list builds need the row-major order)
-    int build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton = false);
+    // nonfinite (device, may be null): set to 1 when a position is NaN or
+    // infinite; the caller clears it and reads it at its next sync.
+    int build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid& grid, bool morton = false,
+              int32_t* nonfinite = nullptr);
     void release();
 };
 
@@ -67,5 +70,9 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
                      int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid);
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl);
+// MRMD_ERR_ARG unless the list's rows [begin, begin + rows) are particles
+// below numLocal and every neighbour index it can hold (the candidates it
+// was built over) is below nAll.
+int check_list_fits(mrmd_ctx* ctx, const mrmd_nlist* nl, int64_t numLocal, int64_t nAll);
 int permute_atoms(mrmd_ctx* ctx, mrmd_atoms* a, mrmd_atoms* shadow, const int32_t* perm, int64_t n);
 }  // namespace mrmd_impl

@@ -120,7 +120,7 @@ void orc_lj_force_energy(const orc_lj_params* t, double distSqr, int64_t typeIdx
 void orc_lj_init(orc_lj_params* out, int64_t numTypes, const double* cap, const double* rc,
                  const double* sigma, const double* epsilon, int isShifted)
 {
-    /* action/LennardJones.cpp:289-324 */
+    /* action/LennardJones.cpp:81-116 */
     for (int64_t t = 0; t < numTypes * numTypes; ++t)
     {
         double sig2 = sigma[t] * sigma[t];
@@ -133,7 +133,7 @@ void orc_lj_init(orc_lj_params* out, int64_t numTypes, const double* cap, const 
         out[t].rcSqr = rc[t] * rc[t];
         out[t].cappingDistance = cap[t];
     }
-    /* operator(), action/LennardJones.cpp:269-287 */
+    /* operator(), action/LennardJones.cpp:61-79 */
     for (int64_t t = 0; t < numTypes * numTypes; ++t)
     {
         double capDist = out[t].cappingDistance;

@@ -90,7 +90,7 @@ typedef struct {
     double shift, energyAtCappingPoint;
 } orc_lj_params;
 
-/* Constructor + per-type precompute, action/LennardJones.cpp:269-324.
+/* Constructor + per-type precompute, action/LennardJones.cpp:61-116.
  * All vectors have numTypes*numTypes entries. */
 void orc_lj_init(orc_lj_params* out, int64_t numTypes, const double* cappingDistance,
                  const double* rc, const double* sigma, const double* epsilon, int isShifted);
@@ -124,7 +124,7 @@ int orc_pred_eval2(const orc_pred* p, double x1, double y1, double z1, double x2
 
 /* LennardJones::apply_if, action/LennardJones.hpp:135-206.  `numTypesIndex`
  * is the multiplier used for typeIdx (the reference fixes it to 1,
- * action/LennardJones.cpp:260).  counts[i], nbrs[i*cap + n] is the half list.
+ * action/LennardJones.cpp:52).  counts[i], nbrs[i*cap + n] is the half list.
  * Forces accumulate; energy and virial are returned for this call only. */
 void orc_lj_apply(const orc_lj_params* table, int64_t numTypesIndex, double rcSqr,
                   orc_atoms* atoms, const int32_t* counts, const int32_t* nbrs, int64_t cap,

@@ -31,6 +31,34 @@ def expect_float_eq(actual, expected):
     assert abs(int(biased(ai)) - int(biased(ei))) <= 4, f"{actual} != {expected} (4 float ULPs)"
 
 
+# Per-atom force error: max_i |F_i - R_i| / max(|R_i|, floor * rms|R|).  The
+# floor only matters for atoms whose net reference force nearly vanishes
+# (there the error is set by the size of the pair terms, not by |R_i|).
+def per_atom_rel_err(F, R, floor=0.0):
+    F = np.asarray(F, dtype=np.float64).reshape(-1, 3)
+    R = np.asarray(R, dtype=np.float64).reshape(-1, 3)
+    nr = np.linalg.norm(R, axis=1)
+    rms = float(np.sqrt((nr ** 2).mean())) if len(nr) else 0.0
+    den = np.maximum(nr, floor * rms)
+    d = np.linalg.norm(F - R, axis=1)
+    zero = den == 0.0
+    if np.any(d[zero] != 0.0):
+        return float("inf")
+    den[zero] = 1.0
+    return float((d / den).max()) if len(d) else 0.0
+
+
+# FP64 parity bar: per atom, relative to the atom's own force (floored at
+# 1e-4 of the RMS force for atoms whose force nearly cancels).
+FP64_RTOL = 1e-10
+FP64_FLOOR = 1e-4
+
+
+def assert_fp64_forces(F, R, what=""):
+    err = per_atom_rel_err(F, R, FP64_FLOOR)
+    assert err <= FP64_RTOL, f"{what} per-atom FP64 force error {err:.3e} > {FP64_RTOL}"
+
+
 @pytest.fixture(scope="session")
 def espp():
     import json

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures from the MRMD reference's own tests.
 
-Run once in a checkout that has the MRMD source tree (default location given by
-``--reference``); the outputs are committed so that tests run without it.
+Run once where the MRMD source tree is available, passing its root as
+``--reference``; the outputs are committed so that tests run without it.
 
 * ``espp_positions.npz``: the 32,768 positions of
   ``tests/LennardJones/positions.txt`` (ESPResSo++ reference configuration,
@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the MRMD source tree")
     args = ap.parse_args()
     src_dir = os.path.join(args.reference, "tests", "LennardJones")
 

@@ -4,7 +4,7 @@ integrator against the oracle, through the C ABI."""
 import numpy as np
 import pytest
 
-from conftest import expect_float_eq
+from conftest import assert_fp64_forces, expect_float_eq
 
 pytestmark = pytest.mark.gpu
 
@@ -168,11 +168,9 @@ def test_lj_ideal_gas_random_vs_oracle(M, orc, apm):
         m.setForce(0.0)
         Eo = ljo.run(mo, co, no, ao)
         Eg = ljg.run(m, vl, a)
-        scale = max(np.abs(ao.force[: ao.n]).max(), 1.0)
-        assert np.abs(a.getForce() - ao.force[: ao.n]).max() <= 1e-10 * scale
+        assert_fp64_forces(a.getForce(), ao.force[: ao.n], "LJ_IdealGas atoms")
         dm = m.download()
-        mscale = max(np.abs(mo.force[:nm]).max(), 1.0)
-        assert np.abs(dm["force"] - mo.force[:nm]).max() <= 1e-10 * mscale
+        assert_fp64_forces(dm["force"], mo.force[:nm], "LJ_IdealGas molecules")
         assert abs(Eg - Eo) <= 1e-10 * max(abs(Eo), 1.0)
     comp = ljg.compensation()
     np.testing.assert_allclose(comp["mean"], ljo.mean, rtol=1e-10, atol=1e-12)

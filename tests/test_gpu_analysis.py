@@ -2,7 +2,7 @@
 and the same observables recorded inside the fused LJ NVE step.
 
 Known answers: analysis/KineticEnergy.test.cpp:22-50 and
-analysis/SystemMomentum.test.cpp:22-45 of the reference.  Sums over many
+analysis/SystemMomentum.test.cpp:23-42 of the reference.  Sums over many
 atoms are compared with the oracle's serial sums at 1e-12 relative (the
 device sums in a fixed tree order, the oracle in index order)."""
 import numpy as np

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, assert_fp64_forces
 
 pytestmark = pytest.mark.gpu
 
@@ -106,8 +106,7 @@ def test_cpp_reference_include_paths(tmp_path, orc):
     assert a["pairs"] == int(co.sum()) and a["bins"] == tf.force.shape[0]
     assert abs(a["energy"] - E) <= 1e-10 * max(abs(E), 1.0)
     f = np.loadtxt(tmp_path / "adress_forces.txt")
-    scale = max(np.abs(ao.force[:n]).max(), 1.0)
-    assert np.abs(f - ao.force[:n]).max() <= 1e-10 * scale
+    assert_fp64_forces(f, ao.force[:n], "drop-in AdResS step")
 
     # CoulombDSF pair function (device exp against the host's: last bits)
     o = orc.CoulombDSF(2.5, 0.3)

@@ -2,19 +2,19 @@
 
 Bars: ghost sets, cell ids and neighbour pair sets are bit-exact; the
 integrators and the ghost update / fold-back are bitwise equal (same FP64
-operation order); FP64 forces, energy and virial agree to 1e-10 relative
-(only the summation order differs); the mixed form stays within 1e-6 of the
+operation order); FP64 forces agree to 1e-10 relative per atom (floored at
+1e-4 of the RMS force), energy and virial to 1e-10 relative (only the
+summation order differs); the mixed form stays within 1e-6 of the
 FP64 forces normalised by the RMS force (the precision bound), with the
 per-atom relative error reported.
 """
 import numpy as np
 import pytest
 
-from conftest import expect_float_eq
+from conftest import FP64_RTOL, assert_fp64_forces, expect_float_eq, per_atom_rel_err
 
 pytestmark = pytest.mark.gpu
 
-FP64_RTOL = 1e-10
 
 
 @pytest.fixture(scope="module")
@@ -116,13 +116,12 @@ def test_espp_energy_and_fp64_forces(M, orc, espp):
     assert abs(lj.getEnergy() - Eo) <= FP64_RTOL * abs(Eo)
     assert abs(lj.getVirial() - Wo) <= FP64_RTOL * abs(Wo)
     Fg = ag.getForce()
-    scale = np.abs(ao.force[: ao.n]).max()
-    assert np.abs(Fg - ao.force[: ao.n]).max() <= FP64_RTOL * scale
+    assert_fp64_forces(Fg, ao.force[: ao.n], "ESPP before fold-back")
     # fold ghost forces back: gather order is the reference's serial order
     gl.contributeBackGhostToReal(ag)
     orc.ghost_to_real(ao, corr)
     Fg = ag.getForce()
-    assert np.abs(Fg - ao.force[: ao.n]).max() <= FP64_RTOL * scale
+    assert_fp64_forces(Fg[: ao.numLocal], ao.force[: ao.numLocal], "ESPP")
     assert np.all(Fg[ao.numLocal:] == 0)
 
 
@@ -177,8 +176,7 @@ def test_fp64_apply_if_random(M, orc, cap, shifted, pkind):
     ag.setForce(0.0)
     lj.apply_if(ag, vl, pg)
     Fg = ag.getForce()
-    scale = np.abs(ao.force[: ao.n]).max()
-    assert np.abs(Fg - ao.force[: ao.n]).max() <= FP64_RTOL * scale
+    assert_fp64_forces(Fg, ao.force[: ao.n])
     assert abs(lj.getEnergy() - Eo) <= FP64_RTOL * max(abs(Eo), 1.0)
     assert abs(lj.getVirial() - Wo) <= FP64_RTOL * max(abs(Wo), 1.0)
 
@@ -217,8 +215,7 @@ def test_fp64_multi_type_random(M, orc, num_types_index):
     ag.setForce(0.0)
     lj.apply(ag, vl)
     Fg = ag.getForce()
-    scale = np.abs(ao.force[: ao.n]).max()
-    assert np.abs(Fg - ao.force[: ao.n]).max() <= FP64_RTOL * scale
+    assert_fp64_forces(Fg, ao.force[: ao.n])
     assert abs(lj.getEnergy() - Eo) <= FP64_RTOL * max(abs(Eo), 1.0)
     assert abs(lj.getVirial() - Wo) <= FP64_RTOL * max(abs(Wo), 1.0)
     with pytest.raises(M.MrmdError):
@@ -251,6 +248,75 @@ def test_mixed_precision_force_error(M, orc, espp):
     assert d.max() / rms <= 1e-6, d.max() / rms
     assert abs(lj.getEnergy() - Eo) <= 1e-7 * abs(Eo)
     assert abs(lj.getVirial() - Wo) <= 1e-7 * abs(Wo)
+
+
+def test_list_rows_offset_by_begin(M, orc):
+    """A list built over particles [begin, end) with begin > 0: its row r is
+    particle begin + r, as in the reference, which indexes Cabana's list by
+    absolute particle (LennardJones.hpp:146-170; the rows outside
+    [begin, end) are empty).  FP64 per atom against the oracle run on the
+    same list in absolute form, and the mixed form within its bar."""
+    L, rc, skin = 12.0, 2.5, 0.3
+    pos = random_fluid(1200, L, 31)
+    b, e = 300, 900
+    sd_o = orc.subdomain([0, 0, 0], [L] * 3, rc + skin)
+    sd_g = M.Subdomain([0, 0, 0], [L] * 3, rc + skin)
+    ao = orc.Atoms.from_positions(pos, capacity=8000)
+    corr = orc.create_ghosts(ao, sd_o)
+    co, no = orc.build_half_list(ao.pos, ao.n, b, e, rc + skin, sd_o.minGhostCorner,
+                                 sd_o.maxGhostCorner, 1.0, 96)
+    ca = np.zeros(ao.numLocal, np.int32)
+    na = np.zeros((ao.numLocal, no.shape[1]), np.int32)
+    ca[b:e], na[b:e] = co, no
+    tab = orc.lj_table(0.0, rc, 1.0, 1.0, 1, True)
+    Eo, Wo = lj_forces_oracle(orc, ao, corr, ca, na, tab, rc)
+    ag = M.Atoms.from_arrays(pos, capacity=8000)
+    gl = M.GhostLayer()
+    gl.createGhostAtoms(ag, sd_g)
+    vl = M.HalfVerletList()
+    vl.build(ag, b, e, rc + skin, 1.0, sd_g.minGhostCorner, sd_g.maxGhostCorner, 60)
+    assert vl.total_pairs == int(co.sum())
+    lj = M.LennardJones(rc, 1.0, 1.0, is_shifted=True)
+    ag.setForce(0.0)
+    lj.apply(ag, vl)
+    Fg = ag.getForce()
+    assert_fp64_forces(Fg, ao.force[: ao.n], "begin > 0")
+    assert np.all(Fg[:b][np.all(ao.force[:b] == 0, axis=1)] == 0)
+    assert abs(lj.getEnergy() - Eo) <= FP64_RTOL * abs(Eo)
+    assert abs(lj.getVirial() - Wo) <= FP64_RTOL * abs(Wo)
+    ag.setForce(0.0)
+    lj.apply(ag, vl, precision=M.PREC_MIXED)
+    Fm = ag.getForce()
+    rms = np.sqrt((np.linalg.norm(ao.force[: ao.n], axis=1) ** 2).mean())
+    assert np.linalg.norm(Fm - ao.force[: ao.n], axis=1).max() / rms <= 1e-6
+    assert abs(lj.getEnergy() - Eo) <= 1e-7 * abs(Eo)
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_nonfinite_position_reported_at_list_build(M, bad):
+    """A NaN or infinite coordinate, written into the host array before the
+    upload, makes the next list build return MRMD_ERR_NONFINITE (the
+    reference asserts on NaN forces, LJ_IdealGas.cpp:140-155); the context
+    stays usable."""
+    L, rc, skin = 12.0, 2.5, 0.3
+    pos = random_fluid(1200, L, 41)
+    pos[517, 1] = bad
+    sd = M.Subdomain([0, 0, 0], [L] * 3, rc + skin)
+    ag = M.Atoms.from_arrays(pos, capacity=8000)
+    gl = M.GhostLayer()
+    gl.createGhostAtoms(ag, sd)
+    vl = M.HalfVerletList()
+    with pytest.raises(M.MrmdError) as ei:
+        vl.build(ag, 0, ag.numLocalAtoms, rc + skin, 1.0, sd.minGhostCorner, sd.maxGhostCorner, 60)
+    assert ei.value.code == -4
+    # the same context builds a clean list afterwards
+    ok = random_fluid(1200, L, 41)
+    a2 = M.Atoms.from_arrays(ok, capacity=8000)
+    g2 = M.GhostLayer()
+    g2.createGhostAtoms(a2, sd)
+    v2 = M.HalfVerletList()
+    v2.build(a2, 0, a2.numLocalAtoms, rc + skin, 1.0, sd.minGhostCorner, sd.maxGhostCorner, 60)
+    assert v2.total_pairs > 0
 
 
 def test_integrators_bitwise(M, orc, espp):

@@ -207,3 +207,25 @@ def test_elongated_box_linear_sort_fallback(M):
     assert np.abs(fm - fr).max() / rms < 3e-6
     e = mix.run(30)
     assert np.all(np.isfinite(e))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonfinite_state_reported_by_the_stepper(M, precision):
+    """An infinite velocity, set on the host, makes a position infinite after
+    the first drift; the stepper reports MRMD_ERR_NONFINITE at the next list
+    rebuild (every 10 steps), within the same run call."""
+    prec = M.PREC_FP64 if precision == "fp64" else M.PREC_MIXED
+    pos, L = fcc(6)
+    vel = mb_velocities(len(pos), 0.728, 9)
+    vel[100, 0] = np.inf
+    s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec)
+    with pytest.raises(M.MrmdError) as ei:
+        s.run(25)
+    assert ei.value.code == -4
+    # a NaN position fails at the first build
+    pos2 = pos.copy()
+    pos2[7, 2] = np.nan
+    s2 = M.LJSystem(pos2, mb_velocities(len(pos), 0.728, 9), [0, 0, 0], [L] * 3, precision=prec)
+    with pytest.raises(M.MrmdError) as ei:
+        s2.run(1)
+    assert ei.value.code == -4

@@ -435,7 +435,7 @@ def test_normal_generator_accuracy_and_moments(orc):
 
 
 def test_analysis_kats(orc):
-    """analysis/KineticEnergy.test.cpp:22-50 and SystemMomentum.test.cpp:22-45,
+    """analysis/KineticEnergy.test.cpp:22-50 and SystemMomentum.test.cpp:23-42,
     and getPressure (analysis/Pressure.cpp:23-51) on a hand-computed case."""
     a = orc.Atoms(3)
     a.vel[:3] = [[2, 0, 0], [-0.0, -8, -0.0], [0, 0, 16]]
