@@ -33,7 +33,8 @@ enum {
     MRMD_ERR_TIMEOUT = -5,        /* a bounded device wait gave up                      */
     MRMD_ERR_CUDA = -6,           /* CUDA runtime error (see mrmd_ctx_last_error)      */
     MRMD_ERR_STATE = -7,          /* call order violated (e.g. no ghosts created yet)   */
-    MRMD_ERR_CAPACITY = -8        /* fixed capacity exceeded (no growth allowed here)   */
+    MRMD_ERR_CAPACITY = -8,       /* fixed capacity exceeded (no growth allowed here)   */
+    MRMD_ERR_BOUNDS = -9          /* bounds-checked build: an index was out of range    */
 };
 
 /* Precision of the pair arithmetic. */
@@ -76,6 +77,14 @@ int mrmd_ctx_set_sync(mrmd_ctx* ctx, int sync);
 /* The CUDA stream (cudaStream_t) all kernels of this context run on. */
 void* mrmd_ctx_stream(mrmd_ctx* ctx);
 const char* mrmd_ctx_last_error(mrmd_ctx* ctx);
+/* 1 in the bounds-checked debug build (libmrmd_gb300_bounds.so, compiled with
+ * -DMRMD_BOUNDS_CHECK; the counterpart of the reference's
+ * Kokkos_ENABLE_DEBUG_BOUNDS_CHECK CI build, .github/workflows/validate.yml:40),
+ * 0 otherwise.  In that build every kernel index into a particle, cell or
+ * list array is checked first; the first violation is recorded with its
+ * source line, the access is skipped and the entry point returns
+ * MRMD_ERR_BOUNDS at its next synchronisation. */
+int mrmd_bounds_checked(void);
 /* Number of kernel launches issued by this context so far. */
 int64_t mrmd_ctx_launch_count(mrmd_ctx* ctx);
 const char* mrmd_version(void);

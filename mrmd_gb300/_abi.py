@@ -10,7 +10,10 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libmrmd_gb300.so")
+# MRMD_GB300_BOUNDS_CHECK=1 loads the bounds-checked debug build instead
+# (python -m mrmd_gb300.build --bounds-check).
+LIB_PATH = os.path.join(_HERE, "libmrmd_gb300_bounds.so" if os.environ.get("MRMD_GB300_BOUNDS_CHECK") == "1"
+                        else "libmrmd_gb300.so")
 
 c_double_p = C.POINTER(C.c_double)
 c_int64_p = C.POINTER(C.c_int64)
@@ -20,6 +23,7 @@ MRMD_OK = 0
 ERRORS = {
     -1: "MRMD_ERR_ARG", -2: "MRMD_ERR_OOM", -3: "MRMD_ERR_NLIST_OVERFLOW", -4: "MRMD_ERR_NONFINITE",
     -5: "MRMD_ERR_TIMEOUT", -6: "MRMD_ERR_CUDA", -7: "MRMD_ERR_STATE", -8: "MRMD_ERR_CAPACITY",
+    -9: "MRMD_ERR_BOUNDS",
 }
 PREC_FP64, PREC_MIXED = 0, 1
 PRED_ALWAYS, PRED_EITHER_IN_SLAB, PRED_BOTH_IN_SLAB, PRED_IN_SLAB, PRED_IN_OPEN_INTERVAL = range(5)
@@ -153,6 +157,7 @@ SIGNATURES = {
     "mrmd_ctx_set_sync": (_i, [_v, _i]),
     "mrmd_ctx_stream": (_v, [_v]),
     "mrmd_ctx_last_error": (C.c_char_p, [_v]),
+    "mrmd_bounds_checked": (_i, []),
     "mrmd_ctx_launch_count": (_i64, [_v]),
     "mrmd_atoms_alloc": (_i, [_v, P(AtomsS), _i64]),
     "mrmd_atoms_free": (_i, [_v, P(AtomsS)]),

@@ -40,10 +40,17 @@ def _headers():
     return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
+# The bounds-checked debug build (-DMRMD_BOUNDS_CHECK: every kernel index into
+# a particle, cell or list array is checked, see MRMD_IN_BOUNDS) goes to its
+# own object folder and library, loaded when MRMD_GB300_BOUNDS_CHECK=1.
+OBJ_BOUNDS = os.path.join(PKG, "_build_bounds")
+LIB_BOUNDS = os.path.join(PKG, "libmrmd_gb300_bounds.so")
+
+
+def _compile(src: str, extra: list[str], objdir: str = OBJ) -> str:
+    obj = os.path.join(objdir, os.path.basename(src).replace(".cu", ".o"))
     newest = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
-    if os.path.exists(obj) and os.path.getmtime(obj) >= newest and not extra:
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest and (not extra or objdir != OBJ):
         return obj
     cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -79,24 +86,29 @@ def build_examples() -> list[str]:
     return outs
 
 
-def build(verbose: bool = False, extra: list[str] | None = None) -> str:
-    os.makedirs(OBJ, exist_ok=True)
+def build(verbose: bool = False, extra: list[str] | None = None, bounds_check: bool = False) -> str:
+    objdir, lib = (OBJ_BOUNDS, LIB_BOUNDS) if bounds_check else (OBJ, LIB)
+    os.makedirs(objdir, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    extra = list(extra or [])
+    extra = list(extra or []) + (["-DMRMD_BOUNDS_CHECK"] if bounds_check else [])
     with cf.ThreadPoolExecutor(max_workers=min(16, len(sources))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), sources))
-    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)) or extra:
-        tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, extra, objdir), sources))
+    stale = not (os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs))
+    if stale or (extra and not bounds_check):
+        tmp = lib + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
         if verbose:
-            print(f"built {LIB}")
-    build_examples()
-    return LIB
+            print(f"built {lib}")
+    if not bounds_check:
+        build_examples()
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, extra=sys.argv[1:]))
+    args = sys.argv[1:]
+    bounds = "--bounds-check" in args
+    print(build(verbose=True, extra=[a for a in args if a != "--bounds-check"], bounds_check=bounds))

@@ -125,7 +125,7 @@ __device__ __forceinline__ int32_t rep_cell(const RepDev& R, const double4& p)
     for (int d = 0; d < 3; ++d)
     {
         const double t = floor(__dmul_rn(__dsub_rn(coord(p, d), R.gmn[d]), R.grdx[d]));
-        c[d] = t < 0.0 ? 0 : (t > (double)(R.gn[d] - 1) ? R.gn[d] - 1 : (int)t);
+        c[d] = t >= 0.0 ? (t > (double)(R.gn[d] - 1) ? R.gn[d] - 1 : (int)t) : 0;  // NaN: cell 0
     }
     return R.cellBase + (c[0] * R.gn[1] + c[1]) * R.gn[2] + c[2];
 }

@@ -194,6 +194,67 @@ __device__ __forceinline__ bool pred2(const Pred& p, double x1, double y1, doubl
 }
 }  // namespace mrmd_dev
 
+// ------------------------------------------------- bounds-checked build --
+// Compiled with -DMRMD_BOUNDS_CHECK (mrmd_gb300/build.py --bounds-check), every
+// MRMD_IN_BOUNDS(idx, n) tests 0 <= idx < n before the access it guards; the
+// first violation of a translation unit is recorded (source line, index,
+// bound) and the guarded access is skipped, so the kernel completes and the
+// host reports MRMD_ERR_BOUNDS at its next synchronisation.  In the normal
+// build the macro is `true` and costs nothing.
+#ifdef MRMD_BOUNDS_CHECK
+namespace mrmd_dev
+{
+// [0] source line + 1 (0: no violation), [1] index, [2] bound; one copy per
+// translation unit (internal linkage)
+static __device__ long long g_bounds_rec[3];
+
+__device__ __noinline__ inline bool bounds_fail(long long idx, long long n, int line)
+{
+    if (atomicCAS(reinterpret_cast<unsigned long long*>(&g_bounds_rec[0]), 0ull,
+                  (unsigned long long)(line + 1)) == 0ull)
+    {
+        g_bounds_rec[1] = idx;
+        g_bounds_rec[2] = n;
+    }
+    return false;
+}
+}  // namespace mrmd_dev
+#define MRMD_IN_BOUNDS(idx, n)                                                     \
+    ((((long long)(idx)) >= 0 && ((long long)(idx)) < ((long long)(n))) ||        \
+     mrmd_dev::bounds_fail((long long)(idx), (long long)(n), __LINE__))
+
+namespace mrmd_impl
+{
+void bounds_register(const char* file, int (*read)(long long*), int (*clear)());
+}
+namespace
+{
+int bounds_read_tu(long long* out)
+{
+    return cudaMemcpyFromSymbol(out, mrmd_dev::g_bounds_rec, 3 * sizeof(long long)) == cudaSuccess ? 0 : -1;
+}
+int bounds_clear_tu()
+{
+    const long long z[3] = {0, 0, 0};
+    return cudaMemcpyToSymbol(mrmd_dev::g_bounds_rec, z, sizeof(z)) == cudaSuccess ? 0 : -1;
+}
+struct BoundsRegistrar
+{
+    BoundsRegistrar() { mrmd_impl::bounds_register(__BASE_FILE__, &bounds_read_tu, &bounds_clear_tu); }
+};
+BoundsRegistrar g_boundsRegistrar;
+}  // namespace
+#else
+#define MRMD_IN_BOUNDS(idx, n) true
+#endif
+
+namespace mrmd_impl
+{
+// MRMD_ERR_BOUNDS with the first recorded violation of any translation unit
+// (bounds-checked build; MRMD_OK otherwise).  Call after a synchronisation.
+int bounds_check(mrmd_ctx* ctx);
+}
+
 inline mrmd_dev::Pred to_dev_pred(const mrmd_pred* p)
 {
     mrmd_dev::Pred d{};

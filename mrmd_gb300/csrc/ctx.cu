@@ -1,5 +1,7 @@
 // Context, error reporting, scratch memory and exclusive scans.
 #include <cstdarg>
+#include <cstring>
+#include <vector>
 
 #include "common.cuh"
 
@@ -37,7 +39,48 @@ int after_launch(mrmd_ctx* ctx, const char* what)
 int finish(mrmd_ctx* ctx, const char* what)
 {
     if (!ctx->sync) return MRMD_OK;
-    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), what);
+    MRMD_TRY(check_cuda(ctx, cudaStreamSynchronize(ctx->stream), what));
+    return bounds_check(ctx);
+}
+
+namespace
+{
+struct BoundsTU
+{
+    const char* file;
+    int (*read)(long long*);
+    int (*clear)();
+};
+
+std::vector<BoundsTU>& bounds_registry()
+{
+    static std::vector<BoundsTU> r;
+    return r;
+}
+}  // namespace
+
+void bounds_register(const char* file, int (*read)(long long*), int (*clear)())
+{
+    bounds_registry().push_back(BoundsTU{file, read, clear});
+}
+
+int bounds_check(mrmd_ctx* ctx)
+{
+#ifdef MRMD_BOUNDS_CHECK
+    for (const BoundsTU& t : bounds_registry())
+    {
+        long long rec[3] = {0, 0, 0};
+        if (t.read(rec) != 0) return set_error(ctx, MRMD_ERR_CUDA, "bounds record of %s unreadable", t.file);
+        if (rec[0] == 0) continue;
+        t.clear();
+        const char* base = std::strrchr(t.file, '/');
+        return set_error(ctx, MRMD_ERR_BOUNDS, "bounds check: %s:%lld index %lld outside [0, %lld)",
+                         base ? base + 1 : t.file, rec[0] - 1, rec[1], rec[2]);
+    }
+#else
+    (void)ctx;
+#endif
+    return MRMD_OK;
 }
 
 int dmalloc(mrmd_ctx* ctx, void** p, size_t bytes)
@@ -296,6 +339,15 @@ int mrmd_ctx_set_sync(mrmd_ctx* ctx, int sync)
 void* mrmd_ctx_stream(mrmd_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
 const char* mrmd_ctx_last_error(mrmd_ctx* ctx) { return ctx ? ctx->lastError : "null context"; }
+
+int mrmd_bounds_checked(void)
+{
+#ifdef MRMD_BOUNDS_CHECK
+    return 1;
+#else
+    return 0;
+#endif
+}
 
 int64_t mrmd_ctx_launch_count(mrmd_ctx* ctx) { return ctx ? ctx->launches : 0; }
 

@@ -98,7 +98,7 @@ __global__ void k_ghost_copy(mrmd_atoms a, int32_t* __restrict__ corr, int64_t n
         const double x = comp(reinterpret_cast<const double4*>(a.pos)[i], axis);
         const int64_t off = offsets[i];
         const int32_t real = corr[i] == -1 ? (int32_t)i : corr[i];
-        if (x < minInner)
+        if (x < minInner && MRMD_IN_BOUNDS(n + (off & 0xffffffffLL), a.capacity))
         {
             const int64_t dst = n + (off & 0xffffffffLL);
             copy_atom(a, dst, i);
@@ -107,7 +107,7 @@ __global__ void k_ghost_copy(mrmd_atoms a, int32_t* __restrict__ corr, int64_t n
             reinterpret_cast<double4*>(a.pos)[dst] = p;
             corr[dst] = real;
         }
-        if (x >= maxInner)
+        if (x >= maxInner && MRMD_IN_BOUNDS(n + numLo + (off >> 32), a.capacity))
         {
             const int64_t dst = n + numLo + (off >> 32);
             copy_atom(a, dst, i);
@@ -132,7 +132,10 @@ __global__ void k_csr_count(const int32_t* __restrict__ corr, int64_t nLocal, in
 {
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nGhost;
          g += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd(&cnt[corr[nLocal + g]], 1);
+    {
+        const int32_t r = corr[nLocal + g];
+        if (MRMD_IN_BOUNDS(r, nLocal)) atomicAdd(&cnt[r], 1);
+    }
 }
 
 __global__ void k_csr_fill(const int32_t* __restrict__ corr, int64_t nLocal, int64_t nGhost,
@@ -143,8 +146,9 @@ __global__ void k_csr_fill(const int32_t* __restrict__ corr, int64_t nLocal, int
          g += (int64_t)gridDim.x * blockDim.x)
     {
         const int32_t r = corr[nLocal + g];
+        if (!MRMD_IN_BOUNDS(r, nLocal)) continue;
         const int32_t k = atomicAdd(&cursor[r], 1);
-        list[start[r] + k] = (int32_t)(nLocal + g);
+        if (MRMD_IN_BOUNDS(start[r] + k, nGhost)) list[start[r] + k] = (int32_t)(nLocal + g);
     }
 }
 
@@ -176,12 +180,13 @@ __global__ void k_ghost_update(double4* __restrict__ pos, const int32_t* __restr
          g += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t idx = nLocal + g;
+        if (!MRMD_IN_BOUNDS(corr[idx], nLocal)) continue;
         pos[idx] = ghost_position(pos[idx], pos[corr[idx]], L, delta);
     }
 }
 
 __global__ void k_ghost_reduce(double4* __restrict__ force, const int32_t* __restrict__ start,
-                               const int32_t* __restrict__ list, int64_t nLocal)
+                               const int32_t* __restrict__ list, int64_t nLocal, int64_t nGhost)
 {
     // communication/AccumulateForce.cpp:25-47, gathered per real atom in
     // ascending ghost order (the serial order of the reference loop)
@@ -194,6 +199,7 @@ __global__ void k_ghost_reduce(double4* __restrict__ force, const int32_t* __res
         for (int32_t k = s; k < e; ++k)
         {
             const int32_t g = list[k];
+            if (!MRMD_IN_BOUNDS(g - nLocal, nGhost)) continue;
             const double4 fg = force[g];
             f.x = __dadd_rn(f.x, fg.x);
             f.y = __dadd_rn(f.y, fg.y);
@@ -478,7 +484,7 @@ int mrmd_ghost_reduce_force(mrmd_ctx* ctx, const mrmd_ghost_layer* g, mrmd_atoms
         return set_error(ctx, MRMD_ERR_STATE, "ghost layer does not match atoms (recreate ghosts)");
     if (a->numGhost == 0 || a->numLocal == 0) return MRMD_OK;
     k_ghost_reduce<<<grid_for(ctx, a->numLocal, TB), TB, 0, ctx->stream>>>(
-        reinterpret_cast<double4*>(a->force), g->ghostStart, g->ghostList, a->numLocal);
+        reinterpret_cast<double4*>(a->force), g->ghostStart, g->ghostList, a->numLocal, a->numGhost);
     MRMD_TRY(after_launch(ctx, "ghost_reduce"));
     return finish(ctx, "ghost_reduce");
 }

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(LJ_TB) k_lj_fp64(
     const double4* __restrict__ pos, double* __restrict__ force, const int32_t* __restrict__ type,
     const LJDev p0, const LJDev* __restrict__ table, int32_t numTypesIndex, double rcSqr,
     const int32_t* __restrict__ counts, const int32_t* __restrict__ nbrs, int64_t cap, int64_t n,
-    int64_t begin, mrmd_dev::Pred pred, double* __restrict__ ev)
+    int64_t begin, int64_t nAll, mrmd_dev::Pred pred, double* __restrict__ ev)
 {
     __shared__ double red[64];
     double energy = 0.0, virial = 0.0;
@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(LJ_TB) k_lj_fp64(
         for (int32_t k = 0; k < cnt; ++k)
         {
             const int32_t j = __ldg(col + 32 * (int64_t)k);
+            if (!MRMD_IN_BOUNDS(j, nAll)) continue;
             const double4 pj = mrmd_dev::ldg4(pos + j);
             if (PRED && !mrmd_dev::pred2(pred, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z)) continue;
             const double dx = pi.x - pj.x;
@@ -139,7 +140,7 @@ int lj_apply_fp64(mrmd_ctx* ctx, const mrmd_lj* lj, mrmd_atoms* a, const mrmd_nl
 #define LJ_LAUNCH(P, M)                                                                                \
     k_lj_fp64<P, M><<<grid, LJ_TB, 0, ctx->stream>>>(pos, a->force, a->type, lj->p0, lj->dTable,         \
                                                      (int32_t)lj->numTypesIndex, lj->rcSqr, nl->counts, \
-                                                     nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev)
+                                                     nl->nbrs, nl->maxNeighbors, n, nl->begin, a->numLocal + a->numGhost, dp, ev)
     if (usePred && multi) LJ_LAUNCH(true, true);
     else if (usePred) LJ_LAUNCH(true, false);
     else if (multi) LJ_LAUNCH(false, true);

@@ -100,7 +100,7 @@ template <bool PRED>
 __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     const float4* __restrict__ hi, const float4* __restrict__ lo, const double4* __restrict__ pos,
     double* __restrict__ force, const LJDev p, RcSq rc2, const int32_t* __restrict__ counts,
-    const int32_t* __restrict__ nbrs, int64_t cap, int64_t n, int64_t begin, mrmd_dev::Pred pred,
+    const int32_t* __restrict__ nbrs, int64_t cap, int64_t n, int64_t begin, int64_t nAll, mrmd_dev::Pred pred,
     double* __restrict__ ev)
 {
     __shared__ double red[64];
@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
         for (int32_t k = 0; k < cnt; ++k)
         {
             const int32_t j = __ldg(col + 32 * (int64_t)k);
+            if (!MRMD_IN_BOUNDS(j, nAll)) continue;
             if (PRED)
             {
                 const double4 pj = mrmd_dev::ldg4(pos + j);
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
     const float4* __restrict__ x2, double4* __restrict__ force, const LJDev p,
     RcSq rc2, float rsplitSq, const int32_t* __restrict__ countsN, const int32_t* __restrict__ nbrsN, int64_t capN,
     const int32_t* __restrict__ countsF, const int32_t* __restrict__ nbrsF, int64_t capF, int64_t n,
-    double* __restrict__ ev)
+    int64_t nAll, double* __restrict__ ev)
 {
     __shared__ double red[64];
     Acc acc;
@@ -185,7 +186,9 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
             for (; k + 1 < cnt; k += 2)
             {
                 prefetch_list(col, k, cnt);
-                const int32_t j0 = __ldg(col + 32 * (int64_t)k), j1 = __ldg(col + 32 * (int64_t)(k + 1));
+                int32_t j0 = __ldg(col + 32 * (int64_t)k), j1 = __ldg(col + 32 * (int64_t)(k + 1));
+                if (!MRMD_IN_BOUNDS(j0, nAll)) j0 = (int32_t)i;  // self: outside the cutoff test
+                if (!MRMD_IN_BOUNDS(j1, nAll)) j1 = (int32_t)i;
                 const float4 h0 = __ldg(x2 + 2 * j0), l0 = __ldg(x2 + 2 * j0 + 1);
                 const float4 h1 = __ldg(x2 + 2 * j1), l1 = __ldg(x2 + 2 * j1 + 1);
                 one(h0, l0);
@@ -193,7 +196,8 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
             }
             if (k < cnt)
             {
-                const int32_t j = __ldg(col + 32 * (int64_t)k);
+                int32_t j = __ldg(col + 32 * (int64_t)k);
+                if (!MRMD_IN_BOUNDS(j, nAll)) j = (int32_t)i;
                 one(__ldg(x2 + 2 * j), __ldg(x2 + 2 * j + 1));
             }
         }
@@ -207,7 +211,11 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
                 prefetch_list(col, k, cnt);
                 int32_t j[2];
 #pragma unroll
-                for (int u = 0; u < 2; ++u) j[u] = __ldg(col + 32 * (int64_t)(k + u));
+                for (int u = 0; u < 2; ++u)
+                {
+                    j[u] = __ldg(col + 32 * (int64_t)(k + u));
+                    if (!MRMD_IN_BOUNDS(j[u], nAll)) j[u] = (int32_t)i;
+                }
                 float4 h[2], l[2];
 #pragma unroll
                 for (int u = 0; u < 2; ++u)
@@ -220,7 +228,8 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
             }
             for (; k < cnt; ++k)
             {
-                const int32_t j0 = __ldg(col + 32 * (int64_t)k);
+                int32_t j0 = __ldg(col + 32 * (int64_t)k);
+                if (!MRMD_IN_BOUNDS(j0, nAll)) j0 = (int32_t)i;
                 one(__ldg(x2 + 2 * j0), __ldg(x2 + 2 * j0 + 1));
             }
         }
@@ -251,7 +260,7 @@ __global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
 }  // namespace
 
 int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
-                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate)
+                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate, int64_t nAll)
 {
     const int64_t n = nearList->rows;
     if (n == 0) return MRMD_OK;
@@ -262,7 +271,7 @@ int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev&
     k_lj_mixed_split<A><<<grid, MX_TB, 0, ctx->stream>>>(x2, reinterpret_cast<double4*>(force4), p, rc2,             \
                                                          rsplitSq, nearList->counts, nearList->nbrs,                 \
                                                          nearList->maxNeighbors, farList->counts, farList->nbrs,     \
-                                                         farList->maxNeighbors, n, ev)
+                                                         farList->maxNeighbors, n, nAll, ev)
     if (accumulate)
         SPLIT_LAUNCH(true);
     else
@@ -283,10 +292,10 @@ int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_
     const double4* pos = reinterpret_cast<const double4*>(a->pos);
     if (usePred)
         k_lj_mixed_half<true><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                               nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev);
+                                                               nl->nbrs, nl->maxNeighbors, n, nl->begin, a->numLocal + a->numGhost, dp, ev);
     else
         k_lj_mixed_half<false><<<grid, MX_TB, 0, ctx->stream>>>(hi, lo, pos, a->force, lj->p0, rc2, nl->counts,
-                                                                nl->nbrs, nl->maxNeighbors, n, nl->begin, dp, ev);
+                                                                nl->nbrs, nl->maxNeighbors, n, nl->begin, a->numLocal + a->numGhost, dp, ev);
     return after_launch(ctx, "lj_mixed_half");
 }
 

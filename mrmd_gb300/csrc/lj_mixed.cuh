@@ -49,8 +49,10 @@ int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams
 // Full-list mixed pair force over a near/far split list (build_split_list):
 // pairs at r >= rsplit in FP32 (pair_far), the others double-float.  x2 holds
 // the split coordinates interleaved, hi of particle j at x2[2j], lo at x2[2j+1].
+// nAll: particles (local + ghost) the lists index.
 int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
-                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate);
+                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate,
+                   int64_t nAll);
 
 // The r_split of lj_mixed_split for LJ parameters sigma and capping distance:
 // 1.4 sigma, and beyond the capping distance (the FP32 path has no cap).

@@ -103,6 +103,7 @@ __global__ void k_ghost_update_split(double4* __restrict__ pos, const int32_t* _
          g += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t idx = nLocal + g;
+        if (!MRMD_IN_BOUNDS(corr[idx], nLocal)) continue;
         const double4 p = ghost_position(pos[idx], pos[corr[idx]], L, delta);
         pos[idx] = p;
         split_store(p, sp, x2, idx);
@@ -291,7 +292,7 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool splitDone = false)
         const int64_t nAll = a->numLocal + a->numGhost;
         if (!splitDone) MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + 1, 2));
         return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
-                              &md->farList, ev, false);
+                              &md->farList, ev, false, nAll);
     }
     MRMD_TRY(lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev));
     return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
@@ -715,7 +716,7 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
         if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
         if (md->cfg.precision == MRMD_PREC_MIXED)
             return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
-                                  &md->farList, ev, false);
+                                  &md->farList, ev, false, a->numLocal + a->numGhost);
         return lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev);
     }
     const int oldSync = ctx->sync;

@@ -64,7 +64,7 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v)
 // a particle is binned into a clamped cell and never becomes a neighbour).
 __global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGrid g,
                              int32_t* __restrict__ cellOf, int32_t* __restrict__ cellCount, int morton,
-                             int32_t* __restrict__ nonfinite)
+                             int32_t* __restrict__ nonfinite, int64_t nkeys)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -84,36 +84,42 @@ __global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGri
             c = cell_of(p, g);
         }
         cellOf[i] = c;
-        atomicAdd(&cellCount[c], 1);
+        if (MRMD_IN_BOUNDS(c, nkeys)) atomicAdd(&cellCount[c], 1);
     }
 }
 
 __global__ void k_cell_scatter(const int32_t* __restrict__ cellOf, int64_t n,
                                const int32_t* __restrict__ cellStart, int32_t* __restrict__ cursor,
-                               int32_t* __restrict__ sorted)
+                               int32_t* __restrict__ sorted, int64_t nkeys)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
         const int32_t c = cellOf[i];
-        sorted[cellStart[c] + atomicAdd(&cursor[c], 1)] = (int32_t)i;
+        if (!MRMD_IN_BOUNDS(c, nkeys)) continue;
+        const int64_t slot = cellStart[c] + atomicAdd(&cursor[c], 1);
+        if (MRMD_IN_BOUNDS(slot, n)) sorted[slot] = (int32_t)i;
     }
 }
 
 // Stable order inside each cell: every slot of the (unordered) scatter
 // output counts the smaller ids of its cell and moves its id to that rank.
 __global__ void k_cell_rank(const int32_t* __restrict__ cellOf, const int32_t* __restrict__ cellStart,
-                            const int32_t* __restrict__ unordered, int64_t n, int32_t* __restrict__ sorted)
+                            const int32_t* __restrict__ unordered, int64_t n, int32_t* __restrict__ sorted,
+                            int64_t nkeys)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
          s += (int64_t)gridDim.x * blockDim.x)
     {
         const int32_t v = unordered[s];
+        if (!MRMD_IN_BOUNDS(v, n)) continue;
         const int32_t c = cellOf[v];
+        if (!MRMD_IN_BOUNDS(c, nkeys)) continue;
         const int32_t b = cellStart[c], e = cellStart[c + 1];
+        if (!MRMD_IN_BOUNDS(b, n + 1) || !MRMD_IN_BOUNDS(e, n + 1)) continue;
         int32_t rank = 0;
         for (int32_t t = b; t < e; ++t) rank += unordered[t] < v;
-        sorted[b + rank] = v;
+        if (MRMD_IN_BOUNDS(b + rank, n)) sorted[b + rank] = v;
     }
 }
 
@@ -124,6 +130,7 @@ __global__ void k_cell_gather(const double4* __restrict__ pos, const int32_t* __
          s += (int64_t)gridDim.x * blockDim.x)
     {
         const int32_t j = sorted[s];
+        if (!MRMD_IN_BOUNDS(j, n)) continue;
         const double4 p = pos[j];
         spos[s] = make_float4((float)(p.x - origin.x), (float)(p.y - origin.y), (float)(p.z - origin.z),
                               __int_as_float(j));
@@ -144,7 +151,7 @@ __global__ void __launch_bounds__(128) k_build_list(
     const double4* __restrict__ pos, const int32_t* __restrict__ cellOf,
     const int32_t* __restrict__ cellStart, const float4* __restrict__ spos, CellGrid g,
     int64_t begin, int64_t end, double rsq, float rsqLo, float rsqHi, int64_t cap,
-    int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount,
+    int32_t* __restrict__ counts, int32_t* __restrict__ nbrs, int32_t* __restrict__ maxCount, int64_t nPos,
     float nearSqF = 0.0f, int64_t capFar = 0, int32_t* __restrict__ countsFar = nullptr,
     int32_t* __restrict__ nbrsFar = nullptr)
 {
@@ -154,6 +161,7 @@ __global__ void __launch_bounds__(128) k_build_list(
         const double4 pi = pos[i];
         const float xi = (float)(pi.x - g.mn.x), yi = (float)(pi.y - g.mn.y), zi = (float)(pi.z - g.mn.z);
         const int32_t ci = cellOf[i];
+        if (!MRMD_IN_BOUNDS(ci, g.ncell)) continue;
         const int cz = ci % g.n.z;
         const int cy = (ci / g.n.z) % g.n.y;
         const int cx = ci / (g.n.z * g.n.y);
@@ -164,7 +172,7 @@ __global__ void __launch_bounds__(128) k_build_list(
         const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
         auto candidate = [&](const float4& q) {
             const int32_t j = __float_as_int(q.w);
-            if (j == (int32_t)i) return;
+            if (j == (int32_t)i || !MRMD_IN_BOUNDS(j, nPos)) return;
             // lexicographic (x, y, z): float order is exact unless equal
             if (!FULL && q.x < xi) return;
             const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
@@ -202,6 +210,7 @@ __global__ void __launch_bounds__(128) k_build_list(
                 {
                     const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
                     const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
+                    if (!MRMD_IN_BOUNDS(s0, nPos + 1) || !MRMD_IN_BOUNDS(s1, nPos + 1)) continue;
                     // four candidates loaded per iteration: the loop is bound by
                     // the latency of these loads, not by the arithmetic
                     int32_t s = s0;
@@ -269,7 +278,7 @@ int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid
     {
         k_cell_count<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4), n,
                                                                    g, cellOf, cellStart, morton ? 1 : 0,
-                                                                   nonfinite);
+                                                                   nonfinite, nkeys);
         MRMD_TRY(after_launch(ctx, "cell_count"));
     }
     MRMD_TRY(scan_exclusive_i32(ctx, cellStart, cellStart, nkeys + 1, nullptr));
@@ -278,9 +287,9 @@ int CellList::build(mrmd_ctx* ctx, const double* pos4, int64_t n, const CellGrid
         // unordered scatter into `spos` storage (reused as int32 scratch), then
         // stable ranks into `sorted`
         int32_t* unordered = reinterpret_cast<int32_t*>(spos);
-        k_cell_scatter<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, n, cellStart, cursor, unordered);
+        k_cell_scatter<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, n, cellStart, cursor, unordered, nkeys);
         MRMD_TRY(after_launch(ctx, "cell_scatter"));
-        k_cell_rank<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, cellStart, unordered, n, sorted);
+        k_cell_rank<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(cellOf, cellStart, unordered, n, sorted, nkeys);
         MRMD_TRY(after_launch(ctx, "cell_rank"));
         k_cell_gather<<<grid_for(ctx, n, TB), TB, 0, ctx->stream>>>(reinterpret_cast<const double4*>(pos4),
                                                                     sorted, n, g.mn, spos);
@@ -353,16 +362,17 @@ int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t n
             if (full)
                 k_build_list<true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                     reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
-                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount);
+                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount, nPos);
             else
                 k_build_list<false><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                     reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin,
-                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount);
+                    end, rsq, rsqLo, rsqHi, cap, nl->counts, nl->nbrs, maxCount, nPos);
             MRMD_TRY(after_launch(ctx, "build_list"));
         }
         int32_t h[3] = {0, 0, 0};
         MRMD_CUDA(ctx, cudaMemcpyAsync(h, maxCount, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        MRMD_TRY(bounds_check(ctx));
         if (h[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
         const int32_t hMax = h[0];
         if (hMax <= cap)
@@ -413,13 +423,14 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
         {
             k_build_list<true, true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                 reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin, end,
-                rsq, rsqLo, rsqHi, capN, nearList->counts, nearList->nbrs, maxCount, nearSqF, capF,
+                rsq, rsqLo, rsqHi, capN, nearList->counts, nearList->nbrs, maxCount, nPos, nearSqF, capF,
                 farList->counts, farList->nbrs);
             MRMD_TRY(after_launch(ctx, "build_split_list"));
         }
         int32_t hMax[3] = {0, 0, 0};
         MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        MRMD_TRY(bounds_check(ctx));
         if (hMax[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
         if (hMax[0] <= capN && hMax[1] <= capF)
         {

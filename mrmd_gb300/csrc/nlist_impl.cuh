@@ -22,11 +22,13 @@ struct CellGrid
 // so that every pair within delta is within `reach` cells per axis.
 CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, int reach = 1);
 
-// cell = clamp(floor((x - min) * rdx), 0, n - 1) per axis, id (ix*ny + iy)*nz + iz
+// cell = clamp(floor((x - min) * rdx), 0, n - 1) per axis, id (ix*ny + iy)*nz + iz.
+// A NaN coordinate goes to cell 0: the comparisons are written so that NaN
+// fails `t >= 0` (a double-to-int conversion of NaN is not a valid cell).
 __device__ __forceinline__ int32_t cell_coord(double x, double mn, double rdx, int n)
 {
     const double t = floor(__dmul_rn(__dsub_rn(x, mn), rdx));
-    int c = t < 0.0 ? 0 : (t > (double)(n - 1) ? n - 1 : (int)t);
+    int c = t >= 0.0 ? (t > (double)(n - 1) ? n - 1 : (int)t) : 0;
     return c;
 }
 

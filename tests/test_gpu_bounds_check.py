@@ -1,0 +1,79 @@
+"""The bounds-checked debug build (libmrmd_gb300_bounds.so, -DMRMD_BOUNDS_CHECK).
+
+The counterpart of the reference's Kokkos_ENABLE_DEBUG_BOUNDS_CHECK CI build
+(.github/workflows/validate.yml:40): every kernel index into a particle, cell
+or list array is tested before the access; the first violation is recorded
+(file, line, index, bound), the access is skipped and the entry point returns
+MRMD_ERR_BOUNDS at its next synchronisation.
+
+The check runs in a child process that loads only the bounds-checked library
+and refuses to continue unless mrmd_bounds_checked() reports it, so the bad
+index below never reaches a kernel without its guard.
+"""
+import os
+import subprocess
+import sys
+import textwrap
+
+import pytest
+
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+CHILD = textwrap.dedent(r"""
+    import ctypes, sys
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import mrmd_gb300 as M
+    ctx = M.default_context()
+    if ctx.lib.mrmd_bounds_checked() != 1:
+        print("not the bounds-checked library")
+        sys.exit(3)
+    L, rc, skin = 12.0, 2.5, 0.3
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0, L, (1000, 3))
+    sd = M.Subdomain([0, 0, 0], [L] * 3, rc + skin)
+    a = M.Atoms.from_arrays(pos, capacity=8000)
+    gl = M.GhostLayer()
+    gl.createGhostAtoms(a, sd)
+    assert a.numGhostAtoms > 0
+    gl.updateGhostAtoms(a, sd)          # clean: no violation
+    # a host-made bad entry: the first ghost's real atom set far beyond the
+    # local atoms, written into the device array from the host
+    cudart = None
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            cudart = ctypes.CDLL(name)
+            break
+        except OSError:
+            pass
+    bad = np.array([1 << 30], dtype=np.int32)
+    dst = ctypes.c_void_p(ctypes.cast(gl.s.correspondingRealAtom, ctypes.c_void_p).value + 4 * a.numLocalAtoms)
+    assert cudart.cudaMemcpy(dst, bad.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(4), 1) == 0
+    try:
+        gl.updateGhostAtoms(a, sd)
+    except M.MrmdError as e:
+        assert e.code == -9, e
+        assert "ghost.cu" in str(e) and str(1 << 30) in str(e), e
+        print("reported:", e)
+    else:
+        print("no violation reported")
+        sys.exit(4)
+    # the record is cleared once reported; the context keeps working
+    good = np.array([0], dtype=np.int32)
+    assert cudart.cudaMemcpy(dst, good.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(4), 1) == 0
+    gl.updateGhostAtoms(a, sd)
+    print("ok")
+""")
+
+
+def test_bounds_build_reports_a_bad_ghost_index():
+    from mrmd_gb300 import build as B
+
+    B.build(bounds_check=True)
+    env = dict(os.environ, MRMD_GB300_BOUNDS_CHECK="1")
+    r = subprocess.run([sys.executable, "-c", f"ROOT = {ROOT!r}\n" + CHILD], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "reported: MRMD_ERR_BOUNDS" in r.stdout and r.stdout.strip().endswith("ok"), r.stdout
