@@ -468,9 +468,10 @@ typedef struct {
     int32_t sortAtoms;       /* k > 0: permute atoms into cell order at every k-th rebuild; 0: never */
     int64_t maxNeighbors;    /* initial list capacity (grown on overflow) */
     int32_t observe;         /* record kinetic energy and momentum of every step */
-    int32_t reserved0;
+    int32_t gatherNeighbours; /* mixed form: 1 = read neighbour records through the cache
+                                 from the int32 lists instead of shared-memory tiles */
     double splitRadius;      /* mixed form: pairs beyond it are evaluated in FP32, closer
-                                ones in double-float; 0 = 1.4 sigma (at least 1.05 x the
+                                ones in double-float; 0 = 1.5 sigma (at least 1.05 x the
                                 capping distance); >= rc: every pair in double-float */
 } mrmd_md_config;
 
@@ -503,6 +504,17 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2);
  * form's list is split by distance; this is its near part). */
 const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md);
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
+/* Mixed form's tile list: [0] tiles, [1] members of the largest tile,
+ * [2] 1 when the pair kernel reads shared-memory tiles, 0 when it gathers
+ * through the int32 lists (a tile over capacity, or gatherNeighbours). */
+int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out3);
+/* The stepper's current neighbour pairs as canonical keys a * 2^32 + b of
+ * unordered pairs of original atom indices (a < b; ghosts mapped to their
+ * real atom), one key per list entry as the pair kernel reads it (the mixed
+ * form's full list holds every pair twice), sorted.  keys may be NULL to
+ * query *count; otherwise cap >= *count entries are written.  For tests and
+ * diagnostics. */
+int mrmd_md_pair_keys(mrmd_ctx* ctx, mrmd_md* md, int64_t* keys, int64_t cap, int64_t* count);
 
 /* ------------------------------------------ fused AdResS stepper -- */
 /* The AdResS LJ <-> ideal-gas step composed from LJ_IdealGas::run

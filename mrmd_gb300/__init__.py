@@ -718,7 +718,7 @@ class LJSystem:
     def __init__(self, pos, vel, box_min, box_max, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
                  capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
                  rebuild_interval=10, use_graph=True, sort_atoms=4, max_neighbors=0, mass=None,
-                 observe=False, split_radius=0.0, ctx: Context | None = None):
+                 observe=False, split_radius=0.0, gather_neighbours=False, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -737,6 +737,7 @@ class LJSystem:
         cfg.maxNeighbors = int(max_neighbors)
         cfg.observe = int(bool(observe))
         cfg.splitRadius = float(split_radius)
+        cfg.gatherNeighbours = int(bool(gather_neighbours))
         self.cfg = cfg
         h = C.c_void_p()
         m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())
@@ -787,6 +788,23 @@ class LJSystem:
         self.ctx.lib.mrmd_md_stats(self.h, _ip(out))
         return dict(steps=int(out[0]), rebuilds=int(out[1]), pairs=int(out[2]), ghosts=int(out[3]),
                     list_capacity=int(out[4]))
+
+    def tile_stats(self):
+        """Mixed form: tiles, members of the largest tile, and whether the pair
+        kernel reads shared-memory tiles (True) or gathers through the cache."""
+        out = np.zeros(3, dtype=np.int64)
+        self.ctx.lib.mrmd_md_tile_stats(self.h, _ip(out))
+        return dict(tiles=int(out[0]), max_members=int(out[1]), tiled=bool(out[2]))
+
+    def pair_keys(self):
+        """Sorted canonical keys a * 2^32 + b (a < b, original atom indices) of
+        every entry of the current list, as the pair kernel reads it."""
+        cnt = C.c_int64()
+        self.ctx.check(self.ctx.lib.mrmd_md_pair_keys(self.ctx.h, self.h, None, 0, C.byref(cnt)), "pair_keys")
+        keys = np.zeros(max(cnt.value, 1), dtype=np.int64)
+        self.ctx.check(self.ctx.lib.mrmd_md_pair_keys(self.ctx.h, self.h, _ip(keys), len(keys), C.byref(cnt)),
+                       "pair_keys")
+        return keys[: cnt.value]
 
     def close(self):
         if getattr(self, "h", None):

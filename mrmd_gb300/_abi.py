@@ -95,7 +95,7 @@ class MDConfigS(C.Structure):
                 ("cappingDistance", C.c_double), ("shifted", C.c_int32),
                 ("precision", C.c_int32), ("dt", C.c_double), ("rebuildInterval", C.c_int64),
                 ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64),
-                ("observe", C.c_int32), ("reserved0", C.c_int32), ("splitRadius", C.c_double)]
+                ("observe", C.c_int32), ("gatherNeighbours", C.c_int32), ("splitRadius", C.c_double)]
 
 
 class AdResSConfigS(C.Structure):
@@ -276,6 +276,8 @@ SIGNATURES = {
     "mrmd_diff_get_state": (_i, [_v, _v, c_double_p, c_double_p]),
     "mrmd_md_atoms": (P(AtomsS), [_v]),
     "mrmd_md_nlist": (P(NListS), [_v]),
+    "mrmd_md_tile_stats": (_i, [_v, c_int64_p]),
+    "mrmd_md_pair_keys": (_i, [_v, _v, c_int64_p, _i64, c_int64_p]),
 }
 
 _lib = None

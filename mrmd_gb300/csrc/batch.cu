@@ -694,8 +694,9 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             const float4 hj = B.hi[j], lj = B.lo[j];
             if (B.farF32 && ownIsSelf)
             {
-                // beyond r_split: plain FP32 (the pair force is small there,
-                // see pair_far); the weights enter with their FP32 heads
+                // beyond r_split: plain FP32 (the LJ pair force is at most
+                // |F(r_split)| there, 1.67 epsilon/sigma at 1.4 sigma); the
+                // weights enter with their FP32 heads
                 const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
                 const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
                 const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);

@@ -134,8 +134,8 @@ __device__ __forceinline__ double slab_m2(const SlabDev& s, double x)
 }
 
 // The FP32 copies of the LJDiff factors used for pairs beyond r_split in the
-// mixed form (the pair force and its derivatives are small there: see
-// pair_far in lj_mixed.cuh).
+// mixed form (the pair force and its derivatives are small there: at most
+// |F(r_split)| = 1.67 epsilon/sigma at 1.4 sigma).
 struct LJDiffF
 {
     float ff1, ff2, ef1, ef2, shift, ff1s, ff2s, ef1s, ef2s, shifts, invEps, rcSq;

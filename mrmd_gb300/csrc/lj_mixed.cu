@@ -65,15 +65,6 @@ int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams
 namespace
 {
 constexpr int MX_TB = 128;
-constexpr int LIST_PREFETCH = 4;  // list entries ahead of the pair loop
-
-// The warp's list entries k of a 32-row tile are one 128-byte line, read
-// once from DRAM: fetch the line LIST_PREFETCH entries ahead into L1.
-__device__ __forceinline__ void prefetch_list(const int32_t* col, int32_t k, int32_t cnt)
-{
-    if (k + LIST_PREFETCH < cnt)
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(col + 32 * (int64_t)(k + LIST_PREFETCH)));
-}
 
 struct Acc
 {
@@ -88,12 +79,6 @@ struct Acc
         df_acc(w, -0.5f * q.ff.h * q.r2h);
     }
 
-    __device__ __forceinline__ void add_force(const PairMixed& q)
-    {
-        df_acc_prod(fx, q.dh.x, q.dl.x, q.ff);
-        df_acc_prod(fy, q.dh.y, q.dl.y, q.ff);
-        df_acc_prod(fz, q.dh.z, q.dl.z, q.ff);
-    }
 };
 
 template <bool PRED>
@@ -144,141 +129,7 @@ __global__ void __launch_bounds__(MX_TB) k_lj_mixed_half(
     }
 }
 
-// Full list split into near and far rows: the near rows (pairs closer than
-// r_split + skin at the rebuild) take the double-float path unless the pair
-// has since moved beyond r_split; the far rows take the FP32 path unless it
-// has come closer.  Per-lane decisions keep every pair on the right path;
-// the split only keeps the warps' lanes on the same path.
-template <bool ACCUM>
-__global__ void __launch_bounds__(MX_TB, 10) k_lj_mixed_split(
-    const float4* __restrict__ x2, double4* __restrict__ force, const LJDev p,
-    RcSq rc2, float rsplitSq, const int32_t* __restrict__ countsN, const int32_t* __restrict__ nbrsN, int64_t capN,
-    const int32_t* __restrict__ countsF, const int32_t* __restrict__ nbrsF, int64_t capF, int64_t n,
-    int64_t nAll, double* __restrict__ ev)
-{
-    __shared__ double red[64];
-    Acc acc;
-    FarAcc fa;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n)
-    {
-        const float4 hi_i = x2[2 * i], lo_i = x2[2 * i + 1];
-        // Energy and virial of every pair are summed in FP32 per atom: the
-        // rounding (about 1e-7 of a per-atom sum, random in sign across
-        // atoms) leaves the system totals within about 1e-10 relative;
-        // forces of close pairs stay double-float.
-        auto one = [&](const float4& h, const float4& l) {
-            if (pair_far(hi_i, lo_i, h, l, p, rc2, rsplitSq, fa) == 2)
-            {
-                PairMixed q;
-                if (pair_mixed(hi_i, lo_i, h, l, p, rc2, q))
-                {
-                    acc.add_force(q);
-                    fa.e += q.e;
-                    fa.w = __fmaf_rn(-0.5f * q.ff.h, q.r2h, fa.w);
-                }
-            }
-        };
-        {
-            const int32_t cnt = countsN[i];
-            const int32_t* __restrict__ col = nbrsN + mrmd_dev::nbr_row(i, capN);
-            int32_t k = 0;
-            for (; k + 1 < cnt; k += 2)
-            {
-                prefetch_list(col, k, cnt);
-                int32_t j0 = __ldg(col + 32 * (int64_t)k), j1 = __ldg(col + 32 * (int64_t)(k + 1));
-                if (!MRMD_IN_BOUNDS(j0, nAll)) j0 = (int32_t)i;  // self: outside the cutoff test
-                if (!MRMD_IN_BOUNDS(j1, nAll)) j1 = (int32_t)i;
-                const float4 h0 = __ldg(x2 + 2 * j0), l0 = __ldg(x2 + 2 * j0 + 1);
-                const float4 h1 = __ldg(x2 + 2 * j1), l1 = __ldg(x2 + 2 * j1 + 1);
-                one(h0, l0);
-                one(h1, l1);
-            }
-            if (k < cnt)
-            {
-                int32_t j = __ldg(col + 32 * (int64_t)k);
-                if (!MRMD_IN_BOUNDS(j, nAll)) j = (int32_t)i;
-                one(__ldg(x2 + 2 * j), __ldg(x2 + 2 * j + 1));
-            }
-        }
-        {
-            // far rows: two gathers in flight before the (short) FP32 pairs
-            const int32_t cnt = countsF[i];
-            const int32_t* __restrict__ col = nbrsF + mrmd_dev::nbr_row(i, capF);
-            int32_t k = 0;
-            for (; k + 1 < cnt; k += 2)
-            {
-                prefetch_list(col, k, cnt);
-                int32_t j[2];
-#pragma unroll
-                for (int u = 0; u < 2; ++u)
-                {
-                    j[u] = __ldg(col + 32 * (int64_t)(k + u));
-                    if (!MRMD_IN_BOUNDS(j[u], nAll)) j[u] = (int32_t)i;
-                }
-                float4 h[2], l[2];
-#pragma unroll
-                for (int u = 0; u < 2; ++u)
-                {
-                    h[u] = __ldg(x2 + 2 * j[u]);
-                    l[u] = __ldg(x2 + 2 * j[u] + 1);
-                }
-#pragma unroll
-                for (int u = 0; u < 2; ++u) one(h[u], l[u]);
-            }
-            for (; k < cnt; ++k)
-            {
-                int32_t j0 = __ldg(col + 32 * (int64_t)k);
-                if (!MRMD_IN_BOUNDS(j0, nAll)) j0 = (int32_t)i;
-                one(__ldg(x2 + 2 * j0), __ldg(x2 + 2 * j0 + 1));
-            }
-        }
-        df_acc(acc.fx, fa.fx);
-        df_acc(acc.fy, fa.fy);
-        df_acc(acc.fz, fa.fz);
-        df_acc(acc.e, fa.e);
-        df_acc(acc.w, fa.w);
-        double4 f = make_double4((double)acc.fx.h + (double)acc.fx.l, (double)acc.fy.h + (double)acc.fy.l,
-                                 (double)acc.fz.h + (double)acc.fz.l, 0.0);
-        if (ACCUM)
-        {
-            const double4 o = force[i];
-            f.x += o.x;
-            f.y += o.y;
-            f.z += o.z;
-        }
-        force[i] = f;
-    }
-    double e = 0.5 * ((double)acc.e.h + (double)acc.e.l), w = 0.5 * ((double)acc.w.h + (double)acc.w.l);
-    mrmd_dev::block_sum2(e, w, red);
-    if (threadIdx.x == 0)
-    {
-        atomicAdd(ev + 0, e);
-        atomicAdd(ev + 1, w);
-    }
-}
 }  // namespace
-
-int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
-                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate, int64_t nAll)
-{
-    const int64_t n = nearList->rows;
-    if (n == 0) return MRMD_OK;
-    const unsigned grid = (unsigned)div_up(n, MX_TB);
-    const RcSq rc2 = make_rcsq(rcSqr);
-    const float rsplitSq = (float)(rsplit * rsplit);
-#define SPLIT_LAUNCH(A)                                                                                              \
-    k_lj_mixed_split<A><<<grid, MX_TB, 0, ctx->stream>>>(x2, reinterpret_cast<double4*>(force4), p, rc2,             \
-                                                         rsplitSq, nearList->counts, nearList->nbrs,                 \
-                                                         nearList->maxNeighbors, farList->counts, farList->nbrs,     \
-                                                         farList->maxNeighbors, n, nAll, ev)
-    if (accumulate)
-        SPLIT_LAUNCH(true);
-    else
-        SPLIT_LAUNCH(false);
-#undef SPLIT_LAUNCH
-    return after_launch(ctx, "lj_mixed_split");
-}
 
 int lj_mixed_half(mrmd_ctx* ctx, const float4* hi, const float4* lo, const mrmd_lj* lj, mrmd_atoms* a,
                   const mrmd_nlist* nl, const mrmd_pred* pred, double* ev)

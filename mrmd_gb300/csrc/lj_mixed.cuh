@@ -46,15 +46,7 @@ __host__ __device__ inline SplitParams make_split(double scale, double invScale)
 int split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitParams& sp, float4* hi, float4* lo,
                  int stride = 1);
 
-// Full-list mixed pair force over a near/far split list (build_split_list):
-// pairs at r >= rsplit in FP32 (pair_far), the others double-float.  x2 holds
-// the split coordinates interleaved, hi of particle j at x2[2j], lo at x2[2j+1].
-// nAll: particles (local + ghost) the lists index.
-int lj_mixed_split(mrmd_ctx* ctx, const float4* x2, double* force4, const LJDev& p, double rcSqr, double rsplit,
-                   const mrmd_nlist* nearList, const mrmd_nlist* farList, double* ev, bool accumulate,
-                   int64_t nAll);
-
-// The r_split of lj_mixed_split for LJ parameters sigma and capping distance:
+// The r_split of the mixed pair kernels for LJ parameters sigma and capping distance:
 // 1.4 sigma, and beyond the capping distance (the FP32 path has no cap).
 inline double lj_split_radius(double sigma, double cappingDistance)
 {
@@ -144,41 +136,6 @@ __device__ __forceinline__ bool pair_mixed(const float4& hi_i, const float4& lo_
         o.e = p.eCapf - (dist.h - p.capDistf) * p.capCoeff_f - p.shiftf;
     }
     return true;
-}
-
-// FP32 sums of the pairs evaluated in plain FP32 (pair_far).
-struct FarAcc
-{
-    float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, w = 0.f;
-};
-
-// Pairs at r >= r_split in plain FP32: there the LJ pair force is at most
-// |F(r_split)| (1.67 epsilon/sigma at 1.4 sigma), so the FP32 rounding of
-// r^2, u = 1/r^2 and the force factor (about 5e-7 relative) and of the FP32
-// sums stays below 1e-7 of the RMS force of a dense LJ fluid; the close pairs,
-// whose forces are large, keep the double-float path.  Returns 0 when the
-// pair is outside the cutoff, 1 when it was added to `a`, 2 when it needs
-// pair_mixed (r < r_split, or r^2 within the FP32 error band of rc^2, where
-// the cutoff test must see the double-float r^2).
-__device__ __forceinline__ int pair_far(const float4& hi_i, const float4& lo_i, const float4& hj, const float4& lj,
-                                        const LJDev& p, RcSq rc2, float rsplitSq, FarAcc& a)
-{
-    const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
-    const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
-    const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
-    const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz));
-    if (r2 > rc2.h * 1.0000005f) return 0;
-    if (r2 < rsplitSq || r2 >= rc2.h * 0.9999995f) return 2;
-    const float u = __fdividef(1.0f, r2);
-    const float u3 = u * u * u;
-    // forceFactor = u^3 (ff1 u^3 - ff2) u (action/LennardJones.hpp:60-66)
-    const float ff = u3 * u * __fmaf_rn(p.ff1h, u3, -p.ff2h);
-    a.fx = __fmaf_rn(dx, ff, a.fx);
-    a.fy = __fmaf_rn(dy, ff, a.fy);
-    a.fz = __fmaf_rn(dz, ff, a.fz);
-    a.e += __fmaf_rn(u3, __fmaf_rn(p.ef1f, u3, -p.ef2f), -p.shiftf);
-    a.w = __fmaf_rn(-0.5f * ff, r2, a.w);
-    return 1;
 }
 
 // s += (dh + dl) * ff in double-float (FMA TwoProd of the heads, first-order

@@ -12,6 +12,7 @@
 // reference's (two kicks with the same force, then the drift), so fusing
 // post(s-1) with pre(s) changes no bit.  The K-1 steps between rebuilds
 // are captured once per rebuild and replayed as one CUDA graph.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -19,6 +20,7 @@
 #include "integrate_impl.cuh"
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
+#include "lj_tile.cuh"
 #include "ghost_impl.cuh"
 #include "nlist_impl.cuh"
 #include "reduce_impl.cuh"
@@ -41,18 +43,15 @@ __device__ __forceinline__ void observe_add(double (&o)[4], const double4& v, do
     o[3] += v.z;
 }
 
-// Split coordinates (hi, lo) of one position into the interleaved record.
-__device__ __forceinline__ void split_store(const double4& x, const SplitParams& sp, float4* __restrict__ x2,
-                                            int64_t i)
+// Tile-kernel records (A, B) of one position.
+__device__ __forceinline__ void split_store(const double4& x, const SplitParams& sp, float4* __restrict__ recA,
+                                            float2* __restrict__ recB, int64_t i)
 {
-    float4 h, l;
-    split_one(x.x - sp.origin.x, sp, h.x, l.x);
-    split_one(x.y - sp.origin.y, sp, h.y, l.y);
-    split_one(x.z - sp.origin.z, sp, h.z, l.z);
-    h.w = 0.0f;
-    l.w = 0.0f;
-    x2[2 * i] = h;
-    x2[2 * i + 1] = l;
+    float4 a;
+    float2 b;
+    tile_split(x, sp, a, b);
+    recA[i] = a;
+    recB[i] = b;
 }
 
 // OBS: the velocities after the post-kick are the full-step velocities of
@@ -65,7 +64,7 @@ template <bool OBS, bool SPLIT>
 __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restrict__ vel, double4* __restrict__ force,
                                    const double* __restrict__ mass, const double* __restrict__ dtfmOf, int64_t n,
                                    double dt, int postKick, double* partial, unsigned* ticket, double* rec,
-                                   SplitParams sp, float4* __restrict__ x2)
+                                   SplitParams sp, float4* __restrict__ recA, float2* __restrict__ recB)
 {
     double o[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -81,7 +80,7 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
         pos[i] = x;
         vel[i] = v;
         force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-        if (SPLIT) split_store(x, sp, x2, i);
+        if (SPLIT) split_store(x, sp, recA, recB, i);
     }
     if (OBS) grid_sum<4>(o, partial, ticket, rec + 2);
 }
@@ -97,7 +96,7 @@ __global__ void k_kick_factors(const double* __restrict__ mass, int64_t n, doubl
 // coordinates.
 __global__ void k_ghost_update_split(double4* __restrict__ pos, const int32_t* __restrict__ corr, int64_t nLocal,
                                      int64_t nGhost, double3 L, double3 delta, SplitParams sp,
-                                     float4* __restrict__ x2)
+                                     float4* __restrict__ recA, float2* __restrict__ recB)
 {
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nGhost;
          g += (int64_t)gridDim.x * blockDim.x)
@@ -106,7 +105,7 @@ __global__ void k_ghost_update_split(double4* __restrict__ pos, const int32_t* _
         if (!MRMD_IN_BOUNDS(corr[idx], nLocal)) continue;
         const double4 p = ghost_position(pos[idx], pos[corr[idx]], L, delta);
         pos[idx] = p;
-        split_store(p, sp, x2, idx);
+        split_store(p, sp, recA, recB, idx);
     }
 }
 
@@ -198,9 +197,12 @@ struct mrmd_md
     CellGrid grid{};
     int32_t* orig = nullptr;     // original index of each local atom
     int32_t* origTmp = nullptr;
-    float4* split = nullptr;     // [capacity][2] hi, lo interleaved
+    float4* recA = nullptr;      // mixed: tile-kernel records of local + ghost atoms
+    float2* recB = nullptr;
     int64_t splitCap = 0;
-    SplitParams sp{};
+    SplitParams sp{};            // mixed: the tile kernel's coordinate split
+    TileList tiles;              // mixed: the split list as shared-memory tiles
+    TileParams tp{};
     double* dEnergy = nullptr;   // [energyCap][REC] per-step records
     int64_t energyCap = 0;
     double* hEnergy = nullptr;   // pinned
@@ -262,6 +264,9 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
         MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
                                   md->rsplit + 0.5 * md->cfg.skin, md->grid));
         MRMD_TRY(list_total_pairs(ctx, &md->farList));
+        if (!md->cfg.gatherNeighbours)
+            MRMD_TRY(tile_list_build(ctx, &md->tiles, &md->list, &md->farList, nAll));
+        md->tp = make_tile_params(md->lj->p0, md->lj->rcSqr, md->rsplit, md->farList.maxNeighbors);
     }
     else
     {
@@ -271,10 +276,12 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
     MRMD_TRY(list_total_pairs(ctx, &md->list));
     if (full && nAll > md->splitCap)
     {
-        dfree(md->split);
-        md->split = nullptr;
+        dfree(md->recA);
+        md->recA = nullptr;
+        md->recB = nullptr;
         const int64_t c = nAll + nAll / 8 + 64;
-        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->split), sizeof(float4) * 2 * (size_t)c));
+        MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&md->recA), (sizeof(float4) + sizeof(float2)) * (size_t)c));
+        md->recB = reinterpret_cast<float2*>(md->recA + c);
         md->splitCap = c;
     }
     md->rebuilds++;
@@ -290,9 +297,9 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool splitDone = false)
     if (md->cfg.precision == MRMD_PREC_MIXED)
     {
         const int64_t nAll = a->numLocal + a->numGhost;
-        if (!splitDone) MRMD_TRY(split_coords(ctx, a->pos, nAll, md->sp, md->split, md->split + 1, 2));
-        return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
-                              &md->farList, ev, false, nAll);
+        if (!splitDone) MRMD_TRY(tile_split_coords(ctx, a->pos, nAll, md->sp, md->recA, md->recB));
+        return lj_tile_forces(ctx, &md->tiles, &md->list, &md->farList, md->recA, md->recB, a->force, md->tp, ev,
+                              nAll, md->cfg.gatherNeighbours != 0);
     }
     MRMD_TRY(lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev));
     return mrmd_ghost_reduce_force(ctx, &md->ghosts, a);
@@ -310,7 +317,7 @@ int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec, bo
     k_fused_kick_drift<O, S><<<grid, TB, 0, ctx->stream>>>(                                                     \
         reinterpret_cast<double4*>(a->pos), reinterpret_cast<double4*>(a->vel),                                 \
         reinterpret_cast<double4*>(a->force), a->mass, md->dtfm, md->n, md->cfg.dt, postKick ? 1 : 0,         \
-        md->dPartial, md->dTicket, prevRec, md->sp, md->split)
+        md->dPartial, md->dTicket, prevRec, md->sp, md->recA, md->recB)
     if (obs && split) KD_LAUNCH(true, true);
     else if (obs) KD_LAUNCH(true, false);
     else if (split) KD_LAUNCH(false, true);
@@ -342,7 +349,8 @@ int md_plain_step(mrmd_ctx* ctx, mrmd_md* md, double* rec, double* prevRec, bool
         k_ghost_update_split<<<grid_for(ctx, a->numGhost, TB), TB, 0, ctx->stream>>>(
             reinterpret_cast<double4*>(a->pos), g->correspondingRealAtom, a->numLocal, a->numGhost,
             make_double3(sd.diameter[0], sd.diameter[1], sd.diameter[2]),
-            make_double3(0.1 * sd.diameter[0], 0.1 * sd.diameter[1], 0.1 * sd.diameter[2]), md->sp, md->split);
+            make_double3(0.1 * sd.diameter[0], 0.1 * sd.diameter[1], 0.1 * sd.diameter[2]), md->sp, md->recA,
+            md->recB);
         MRMD_TRY(after_launch(ctx, "ghost_update_split"));
     }
     return md_forces(ctx, md, rec, true);
@@ -447,7 +455,8 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
         // fewer candidates than 3^3 cells of the full radius)
         md->grid = make_grid(md->sd.minGhostCorner, md->sd.maxGhostCorner, rlist,
                              cfg->precision == MRMD_PREC_MIXED ? 2 : 1);
-        md->sp = split_params(md->sd.minGhostCorner, md->grid.extent * 1.25 + 8.0);
+        if (!tile_split_params(md->sd.minGhostCorner, md->grid.extent * 1.25 + 8.0, rlist, &md->sp))
+            rc = set_error(ctx, MRMD_ERR_ARG, "box too large for the mixed form's coordinate split");
     }
     std::vector<double> m((size_t)n, 1.0);
     if (mass)
@@ -463,7 +472,7 @@ int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int6
     if (rc == MRMD_OK) rc = mrmd_ghost_layer_alloc(ctx, &md->ghosts, cap);
     if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->list);
     if (rc == MRMD_OK) rc = mrmd_nlist_init(ctx, &md->farList);
-    md->rsplit = cfg->splitRadius > 0.0 ? cfg->splitRadius : lj_split_radius(cfg->sigma, cfg->cappingDistance);
+    md->rsplit = cfg->splitRadius > 0.0 ? cfg->splitRadius : 1.5 * cfg->sigma;
     if (md->rsplit < 1.05 * cfg->cappingDistance) md->rsplit = 1.05 * cfg->cappingDistance;
     if (rc == MRMD_OK)
     {
@@ -513,9 +522,10 @@ int mrmd_md_destroy(mrmd_ctx* ctx, mrmd_md* md)
     mrmd_nlist_free(ctx, &md->farList);
     mrmd_lj_destroy(ctx, md->lj);
     md->sortCells.release();
+    md->tiles.release();
     dfree(md->orig);
     dfree(md->origTmp);
-    dfree(md->split);
+    dfree(md->recA);
     dfree(md->dEnergy);
     dfree(md->dPartial);
     dfree(md->dtfm);
@@ -715,8 +725,8 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
     {
         if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
         if (md->cfg.precision == MRMD_PREC_MIXED)
-            return lj_mixed_split(ctx, md->split, a->force, md->lj->p0, md->lj->rcSqr, md->rsplit, &md->list,
-                                  &md->farList, ev, false, a->numLocal + a->numGhost);
+            return lj_tile_forces(ctx, &md->tiles, &md->list, &md->farList, md->recA, md->recB, a->force, md->tp,
+                                  ev, a->numLocal + a->numGhost, md->cfg.gatherNeighbours != 0);
         return lj_apply_fp64(ctx, md->lj, a, &md->list, nullptr, ev);
     }
     const int oldSync = ctx->sync;
@@ -741,5 +751,109 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
 
 const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md) { return md ? &md->atoms : nullptr; }
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md) { return md ? &md->list : nullptr; }
+
+int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out3)
+{
+    if (!md || !out3) return MRMD_ERR_ARG;
+    const bool mixed = md->cfg.precision == MRMD_PREC_MIXED;
+    out3[0] = mixed ? md->tiles.tiles : 0;
+    out3[1] = mixed ? md->tiles.maxMembers : 0;
+    out3[2] = mixed && md->tiles.valid && !md->cfg.gatherNeighbours ? 1 : 0;
+    return MRMD_OK;
+}
+
+}  // extern "C"
+
+namespace
+{
+// Entries of a list in a 32-row tile layout (element type T, `cap` elements
+// per row), with the row counts.
+template <typename T>
+int download_rows(mrmd_ctx* ctx, const T* dev, const int32_t* devCounts, int64_t rows, int64_t cap,
+                  std::vector<int32_t>& counts, std::vector<T>& entries)
+{
+    counts.assign((size_t)rows, 0);
+    entries.assign((size_t)(div_up(rows, 32) * 32 * cap), T{});
+    if (rows == 0) return MRMD_OK;
+    MRMD_TRY(d2h(ctx, counts.data(), devCounts, sizeof(int32_t) * (size_t)rows));
+    if (cap > 0) MRMD_TRY(d2h(ctx, entries.data(), dev, sizeof(T) * entries.size()));
+    return MRMD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mrmd_md_pair_keys(mrmd_ctx* ctx, mrmd_md* md, int64_t* keys, int64_t cap, int64_t* count)
+{
+    if (!ctx || !md || !count) return MRMD_ERR_ARG;
+    if (md->needRebuild || !md->forceValid) return set_error(ctx, MRMD_ERR_STATE, "no list: run or eval first");
+    const mrmd_atoms* a = &md->atoms;
+    const int64_t n = a->numLocal, nAll = a->numLocal + a->numGhost;
+    std::vector<int32_t> orig((size_t)n), corr((size_t)nAll);
+    MRMD_TRY(d2h(ctx, orig.data(), md->orig, sizeof(int32_t) * (size_t)n));
+    MRMD_TRY(d2h(ctx, corr.data(), md->ghosts.correspondingRealAtom, sizeof(int32_t) * (size_t)nAll));
+    const bool mixed = md->cfg.precision == MRMD_PREC_MIXED;
+    const bool tiled = mixed && md->tiles.valid && !md->cfg.gatherNeighbours;
+    std::vector<int32_t> members, memberCount;
+    if (tiled)
+    {
+        const int64_t tiles = md->tiles.tiles;
+        members.resize((size_t)(tiles * TILE_CAP));
+        memberCount.resize((size_t)tiles);
+        MRMD_TRY(d2h(ctx, members.data(), md->tiles.members, sizeof(int32_t) * members.size()));
+        MRMD_TRY(d2h(ctx, memberCount.data(), md->tiles.memberCount, sizeof(int32_t) * memberCount.size()));
+    }
+    std::vector<int64_t> out;
+    auto add = [&](int64_t i, int64_t j) -> int {
+        if (j < 0 || j >= nAll) return set_error(ctx, MRMD_ERR_STATE, "list entry %lld outside the atoms", (long long)j);
+        const int64_t r = j < n ? j : corr[(size_t)j];
+        if (r < 0 || r >= n) return set_error(ctx, MRMD_ERR_STATE, "ghost %lld without a real atom", (long long)j);
+        const int64_t oi = orig[(size_t)i], oj = orig[(size_t)r];
+        out.push_back(oi < oj ? (oi << 32) | oj : (oj << 32) | oi);
+        return MRMD_OK;
+    };
+    const mrmd_nlist* lists[2] = {&md->list, mixed ? &md->farList : nullptr};
+    for (int w = 0; w < 2; ++w)
+    {
+        const mrmd_nlist* nl = lists[w];
+        if (!nl || nl->rows == 0) continue;
+        std::vector<int32_t> counts;
+        if (tiled)
+        {
+            const int64_t nch = w == 0 ? md->tiles.nearChunksPerRow : md->tiles.farChunksPerRow;
+            std::vector<uint4> e;
+            MRMD_TRY(download_rows(ctx, w == 0 ? md->tiles.nearChunks : md->tiles.farChunks, nl->counts, nl->rows,
+                                   nch, counts, e));
+            for (int64_t i = 0; i < nl->rows; ++i)
+            {
+                const int64_t t = i / TILE_ROWS;
+                for (int64_t k = 0; k < counts[(size_t)i]; ++k)
+                {
+                    const uint4 c = e[(size_t)chunk_word(i, k >> 3, nch)];
+                    const uint32_t word = (k & 7) < 2 ? c.x : (k & 7) < 4 ? c.y : (k & 7) < 6 ? c.z : c.w;
+                    const int64_t slot = (word >> (16 * (k & 1))) & 0xffffu;
+                    if (slot >= memberCount[(size_t)t]) return set_error(ctx, MRMD_ERR_STATE, "slot beyond the tile");
+                    MRMD_TRY(add(i, members[(size_t)(t * TILE_CAP + slot)]));
+                }
+            }
+        }
+        else
+        {
+            const int64_t lcap = nl->maxNeighbors;
+            std::vector<int32_t> e;
+            MRMD_TRY(download_rows(ctx, nl->nbrs, nl->counts, nl->rows, lcap, counts, e));
+            for (int64_t i = 0; i < nl->rows; ++i)
+                for (int64_t k = 0; k < counts[(size_t)i]; ++k)
+                    MRMD_TRY(add(i, e[(size_t)((i >> 5) * (lcap << 5) + (k << 5) + (i & 31))]));
+        }
+    }
+    std::sort(out.begin(), out.end());
+    *count = (int64_t)out.size();
+    if (!keys) return MRMD_OK;
+    if (cap < *count) return set_error(ctx, MRMD_ERR_CAPACITY, "pair key capacity %lld < %lld", (long long)cap,
+                                       (long long)*count);
+    std::memcpy(keys, out.data(), sizeof(int64_t) * out.size());
+    return MRMD_OK;
+}
 
 }  // extern "C"

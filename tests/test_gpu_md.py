@@ -2,6 +2,8 @@
 import numpy as np
 import pytest
 
+from conftest import per_atom_rel_err
+
 pytestmark = pytest.mark.gpu
 
 
@@ -229,3 +231,62 @@ def test_nonfinite_state_reported_by_the_stepper(M, precision):
     with pytest.raises(M.MrmdError) as ei:
         s2.run(1)
     assert ei.value.code == -4
+
+
+def espp_oracle(orc, espp, shifted=True):
+    """Oracle half list (canonical pair keys) and FP64 forces of the ESPP
+    system (tests/LennardJones/positions.txt of the reference)."""
+    g, pos = espp
+    L, rc, skin = g["box"], g["rc"], g["skin"]
+    sd = orc.subdomain([0, 0, 0], [L] * 3, rc + skin)
+    ao = orc.Atoms.from_positions(pos, capacity=60000)
+    corr = orc.create_ghosts(ao, sd)
+    co, no = orc.build_half_list(ao.pos, ao.n, 0, ao.numLocal, rc + skin, sd.minGhostCorner,
+                                 sd.maxGhostCorner, 1.0, 64)
+    keys = orc.canonical_pairs(co, no, corr, ao.numLocal)
+    ao.force[:] = 0
+    E, W = orc.lj_apply(orc.lj_table(0.0, rc, 1.0, 1.0, 1, shifted), rc * rc, ao, co, no)
+    orc.ghost_to_real(ao, corr)
+    return pos, L, keys, ao.force[: ao.numLocal].copy(), E, W
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed", "mixed_gather"])
+def test_stepper_list_is_the_oracle_pair_set(M, orc, espp, form):
+    """The list the stepper's pair kernel reads (the FP64 half list; the mixed
+    form's near + far full list, decoded from its shared-memory tiles or from
+    the int32 lists), mapped to unordered pairs of original atom indices, is
+    the oracle's half-list pair set bit for bit: once per pair in the half
+    list, twice in the full list."""
+    pos, L, ko, _, _, _ = espp_oracle(orc, espp)
+    prec = M.PREC_FP64 if form == "fp64" else M.PREC_MIXED
+    s = M.LJSystem(pos, np.zeros_like(pos), [0, 0, 0], [L] * 3, precision=prec,
+                   gather_neighbours=form == "mixed_gather")
+    s.eval_forces()
+    kg = s.pair_keys()
+    if form == "fp64":
+        np.testing.assert_array_equal(kg, ko)
+    else:
+        assert len(kg) == 2 * len(ko)
+        np.testing.assert_array_equal(kg[0::2], ko)
+        np.testing.assert_array_equal(kg[1::2], ko)
+        assert s.tile_stats()["tiled"] == (form == "mixed")
+
+
+def test_mixed_tile_forces_per_atom_against_oracle(M, orc, espp):
+    """Mixed form on the ESPP system against the oracle's FP64 forces, per atom:
+    |dF_i| <= 1e-6 max(|F_i|, 0.1 rms|F|); the tile and the gather form read the
+    same records in the same order and agree bitwise; energy and virial
+    (double-float sums of u^3 and u^6) within 1e-9 relative."""
+    pos, L, _, fo, Eo, Wo = espp_oracle(orc, espp)
+    vel = np.zeros_like(pos)
+    t = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED)
+    g = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED, gather_neighbours=True)
+    et, wt = t.eval_forces()
+    eg, wg = g.eval_forces()
+    ft, fg = t.state()[2], g.state()[2]
+    assert t.tile_stats()["tiled"] and not g.tile_stats()["tiled"]
+    np.testing.assert_array_equal(ft, fg)
+    err = per_atom_rel_err(ft, fo, 0.1)
+    assert err <= 1e-6, err
+    assert abs(et - Eo) <= 1e-9 * abs(Eo) and abs(wt - Wo) <= 1e-9 * abs(Wo), (et, Eo, wt, Wo)
+    assert abs(et - eg) <= 1e-12 * abs(et)
