@@ -12,9 +12,10 @@
 //   forces summed in FP32.
 // - Energy and virial: E = ef1 u^6 - ef2 u^3 - shift and -2W = ff1 u^6 - ff2 u^3
 //   per uncapped pair (action/LennardJones.hpp:52-78), so the kernel sums
-//   u^3, u^6 and the pair count per atom in double-float (Fast2Sum against a
-//   power-of-two offset larger than any partial sum, so that every addition
-//   is error-free in its head) and forms E and W once per block in FP64.
+//   u^3, u^6 and the pair count per atom in double-float (these terms are
+//   positive: Fast2Sum against a power-of-two offset above any row's sum
+//   makes every head addition error-free) and forms E and W once per block
+//   in FP64.
 //   Capped pairs (inside the capping distance) add their energy and
 //   forceFactor * r^2 to separate double-float sums.
 // All per-pair work runs on the FP32 pipe: GB300's FP64 rate is a small
@@ -75,15 +76,6 @@ TileParams make_tile_params(const LJDev& p, double rcSqr, double rsplit, int64_t
     std::frexp(n * u3max * u3max, &e6);
     t.bias3 = (float)std::ldexp(1.0, e3);
     t.bias6 = (float)std::ldexp(1.0, e6);
-    // Offset of the near-pair force heads: a power of two above 64 times the
-    // largest pair force |F(r_min)| (the capping coefficient inside the cap),
-    // so that a row's partial sum stays below half of it.
-    const double um = 1.0 / rmin2;
-    const double fmax = std::fmax(std::fabs(um * um * um * um * (p.ff1 * um * um * um - p.ff2)) * std::sqrt(rmin2),
-                                  std::fabs(p.capCoeff));
-    int ef = 0;
-    std::frexp(64.0 * fmax, &ef);
-    t.biasF = (float)std::ldexp(1.0, ef);
     return t;
 }
 }  // namespace mrmd_impl
@@ -271,9 +263,7 @@ __device__ __forceinline__ bool pair_geom(const float4& ai, const float2& bi, co
 
 struct Sums
 {
-    // double-float pairs, heads offset by biasF (Fast2Sum: every head
-    // addition is error-free while |partial sum| < biasF / 2)
-    float fxh, fxl = 0.f, fyh, fyl = 0.f, fzh, fzl = 0.f;
+    float fxh = 0.f, fxl = 0.f, fyh = 0.f, fyl = 0.f, fzh = 0.f, fzl = 0.f;  // double-float pairs
     float gx = 0.f, gy = 0.f, gz = 0.f;    // FP32 pairs
     float s3h, s3l = 0.f, s6h, s6l = 0.f;  // biased sums of u^3, u^6
     int32_t cnt = 0;                       // uncapped pairs in range
@@ -289,15 +279,16 @@ __device__ __forceinline__ void biased_add(float& sh, float& sl, float x)
 }
 
 // s += (dh + dl) * (f0 + f1): FMA TwoProd of the head product, first-order
-// cross terms and the Fast2Sum error into the low part
+// cross terms and the TwoSum error into the low part (TwoSum, not an offset
+// Fast2Sum: a close contact's pair force can exceed any fixed offset)
 __device__ __forceinline__ void acc_prod(float& sh, float& sl, float dh, float dl, float f0, float f1)
 {
     const float p = __fmul_rn(dh, f0);
     float e = __fmaf_rn(dh, f0, -p);
     e = __fmaf_rn(dh, f1, __fmaf_rn(dl, f0, e));
-    const float t = __fadd_rn(sh, p);
-    sl = __fadd_rn(sl, __fadd_rn(e, __fsub_rn(p, __fsub_rn(t, sh))));
-    sh = t;
+    const df t = two_sum(sh, p);
+    sl = __fadd_rn(sl, __fadd_rn(e, t.l));
+    sh = t.h;
 }
 
 template <bool CAP>
@@ -439,7 +430,6 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_lj_tile(
     Sums s;
     s.s3h = tp.bias3;
     s.s6h = tp.bias6;
-    s.fxh = s.fyh = s.fzh = tp.biasF;
     if (row < rows)
     {
         const float4 ai = __ldg(recA + row);
@@ -490,10 +480,9 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_lj_tile(
 #pragma unroll 2
             for (int32_t k = 0; k < cf; ++k) pair(__ldg(fI + 32 * (int64_t)k), false);
         }
-        // F = (head - biasF) + far sum + low part; the head difference is
-        // exact (Sterbenz: the head stays within [biasF / 2, 2 biasF])
+        // F = near double-float sum + far FP32 sum
         auto comp = [&](float h, float l, float gsum) -> double {
-            const df t = two_sum(__fsub_rn(h, tp.biasF), gsum);
+            const df t = two_sum(h, gsum);
             return df_as_f64(t.h, __fadd_rn(t.l, l));
         };
         force[row] = make_double4(comp(s.fxh, s.fxl, s.gx), comp(s.fyh, s.fyl, s.gy), comp(s.fzh, s.fzl, s.gz), 0.0);

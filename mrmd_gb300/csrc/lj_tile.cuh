@@ -92,7 +92,6 @@ struct TileParams
     RcSq rc2;
     float rsplitSq;
     float bias3, bias6;  // offsets of the u^3, u^6 sums (make_tile_params)
-    float biasF;         // offset of the double-float force heads
 };
 
 TileParams make_tile_params(const LJDev& p, double rcSqr, double rsplit, int64_t farCapacity);
