@@ -326,9 +326,13 @@ __device__ __forceinline__ void near_pair(const Geom& g, const TileParams& tp, S
         const float tl = __fadd_rn(ts.l, __fsub_rn(qa, tp.p.ff2l));
         f0 = __fmul_rn(p4, ts.h);
         f1 = __fmaf_rn(p4, tl, __fmaf_rn(q4, ts.h, __fmaf_rn(p4, ts.h, -f0)));
+        // u^3 = p3 + q3 and u^6 = p3^2 + 2 p3 q3 (+ the rounding of p3^2): the
+        // head p3 alone carries the seed reciprocal's error, which q3 corrects
         biased_add(s.s3h, s.s3l, p3);
         s.s3l = __fadd_rn(s.s3l, q3);
-        biased_add(s.s6h, s.s6l, __fmul_rn(p3, p3));
+        const float u6 = __fmul_rn(p3, p3);
+        biased_add(s.s6h, s.s6l, u6);
+        s.s6l = __fadd_rn(s.s6l, __fmaf_rn(__fadd_rn(p3, p3), q3, __fmaf_rn(p3, p3, -u6)));
         s.cnt += 1;
     }
     acc_prod(s.fxh, s.fxl, g.dhx, g.dlx, f0, f1);
