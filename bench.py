@@ -259,30 +259,76 @@ def time_run(torch, M, sysm, steps, stream):
 
 
 DRIFT_SETUP = ("32,000 atoms (fcc 20^3, same density, T 0.728 start), 2,000 FP64 steps to equilibrate, then "
-               "200,000 steps (1000 tau) per form from that state; drift = slope of a least-squares line "
-               "through (E_pot + E_kin)/N of every step, both summed on the device inside the step")
+               "200,000 steps (1000 tau) per form from that state, for 3 velocity seeds (mean and sd reported); "
+               "drift = slope of a least-squares line through (E_pot + E_kin)/N of every step, both summed on "
+               "the device inside the step")
+MIXED_DTYPE = ("f64 state; pair arithmetic f32 beyond 1.5 sigma, double-float closer; energy/virial sums "
+               "double-float")
 
 
-def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005):
+DRIFT_SEEDS = (7, 8, 9)
+
+
+def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005, seeds=DRIFT_SEEDS):
     """Energy drift per atom per 1000 tau of each form, from the per-step
-    records of the observing stepper (no host transfer inside the run)."""
+    records of the observing stepper (no host transfer inside the run), for
+    each seed of the initial velocities: mean, standard deviation and the
+    per-seed values."""
     pos, L = fcc(cells)
-    vel = mb_velocities(len(pos), 0.728, 7)
-    eq = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64, ctx=ctx)
-    eq.run(equil, energies=False)
-    p, v, _ = eq.state()
-    eq.close()
-    out = {}
+    per = {f: [] for f in forms}
+    fluct = {f: [] for f in forms}
+    for seed in seeds:
+        vel = mb_velocities(len(pos), 0.728, seed)
+        eq = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64, ctx=ctx)
+        eq.run(equil, energies=False)
+        p, v, _ = eq.state()
+        eq.close()
+        for form in forms:
+            prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
+            s = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=prec, observe=True, ctx=ctx)
+            rec = s.run_observed(steps)
+            s.close()
+            et = (rec[:, 0] + rec[:, 2]) / len(p)
+            t = np.arange(steps) * dt
+            per[form].append(float(np.polyfit(t, et, 1)[0]) * 1000.0)
+            fluct[form].append(float(et.std()))
+    return {f: dict(drift=float(np.mean(per[f])), drift_sd=float(np.std(per[f], ddof=1)) if len(per[f]) > 1 else None,
+                    drift_per_seed=per[f], fluct=float(np.mean(fluct[f]))) for f in forms}
+
+
+def adress_batch_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
+    """The AdResS workload (scaled to `molecules` at density 0.5) on the batched
+    engine with one replica, both forms: ms per step, atom-steps/s and the
+    force error of the mixed form against FP64 on the first step's identical
+    positions."""
+    c = adress_config(molecules)
+    pos, vel = adress_initial(100, c)
+    n = len(pos)
+    out, forces = {}, {}
     for form in forms:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
-        s = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=prec, observe=True, ctx=ctx)
-        rec = s.run_observed(steps)
-        s.close()
-        et = (rec[:, 0] + rec[:, 2]) / len(p)
-        t = np.arange(steps) * dt
-        slope = float(np.polyfit(t, et, 1)[0])
-        out[form] = dict(drift=slope * 1000.0, fluct=float(et.std()))
-    return out
+        rep = M.Replica(n, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], 1234)
+        b = M.BatchSystem([rep], pos, vel, hybrid_diameter=c["hy"], nu=c["nu"], rc=c["rc"], skin=c["skin"],
+                          capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
+                          temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
+                          tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
+                          tf_update_interval=c["U"], rebuild_interval=c["K"], sort_every=5, graph_steps=50, ctx=ctx)
+        b.run(1, energies=False)
+        forces[form] = b.state()[2]
+        b.run(warmup - 1, energies=False)
+        ms, wall, e, launches = time_run(torch, M, b, steps, stream)
+        out[form] = {"ms_per_step": ms / steps, "atom_steps_per_s": n * steps / (ms * 1e-3)}
+        b.close()
+    res = {"molecules": n, "forms": out, "engine": "batched engine, one replica, CUDA graphs of 50 steps"}
+    if {"fp64", "mixed"} <= out.keys():
+        res["mixed_over_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+        fa, fb = forces["fp64"], forces["mixed"]
+        d = np.linalg.norm(fa - fb, axis=1)
+        mag = np.linalg.norm(fa, axis=1)
+        rms = float(np.sqrt((mag ** 2).mean()))
+        res["force_error_mixed_vs_fp64"] = {"max_abs_over_rms": float(d.max() / rms),
+                                            "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
+    return res
 
 
 def time_pair_kernel(torch, sysm, stream, reps=20):
@@ -755,7 +801,7 @@ def precision_main(args, rank, world, local_rank):
     line = {"metric": METRIC, "value": out["mixed"]["atom_steps_per_s"], "unit": METRIC, "n_gpus": 1,
             "steps": args.steps, "warmup": 0, "ms_per_step": out["mixed"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 state; pair arithmetic f32 beyond 1.4 sigma, f32 double-float closer",
+            "dtype": MIXED_DTYPE,
             "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
             "config": {"workload": PRECISION_WORKLOAD, "atoms": n, "forms": out,
                        "mixed_over_fp64": out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"],
@@ -779,6 +825,7 @@ def main():
                     help="adress workload: molecules (default 34,560; the box is scaled at density 0.5)")
     ap.add_argument("--cells", type=int, default=100, help="fcc cells per edge (100 -> 4,000,000 atoms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-adress", action="store_true", help="lj workload: skip the AdResS sub-results")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the baseline")
     ap.add_argument("--forms", default="fp64,mixed")
     ap.add_argument("--fit-iterations", type=int, default=5,
@@ -862,10 +909,17 @@ def main():
                 "max_per_atom_relative": float((d / np.maximum(mag, 1e-300)).max()),
                 "max_relative_floor_0.1rms": float((d / np.maximum(mag, 0.1 * rms)).max())}
 
-    # NVE energy drift of each form on a separate equilibrated system
+    # NVE energy drift of each form on separate equilibrated systems
     drift = nve_drift(M, ctx, list(res)) if rank == 0 else {}
     for f in res:
         res[f]["drift"] = drift.get(f, {}).get("drift")
+
+    # the AdResS workload beside it (34,560 molecules and 4 M molecules)
+    adress = None
+    if rank == 0 and world == 1 and not args.no_adress:
+        adress = {"workload": ADRESS_WORKLOAD,
+                  "34560": adress_batch_leg(M, ctx, torch, stream, None, list(res)),
+                  "4000000": adress_batch_leg(M, ctx, torch, stream, 4_000_000, list(res))}
 
     # the pair kernel alone (dominant kernel) for the roofline
     kern_ms = time_pair_kernel(torch, sysm, stream)
@@ -878,9 +932,12 @@ def main():
     # pair from both ends, so that no force is scattered with atomics).
     nhalf = nbar / 2 if head == "mixed" else nbar
     bytes_per_atom = 24 + 24 + 4 * (1 + nhalf)
+    tiles = sysm.tile_stats() if head == "mixed" else None
     if head == "mixed":
-        kernel_bytes = 32 + 24 + 4 * (2 + nbar)  # split records, F, near/far counts, full list
-        kname = "lj_mixed_split"
+        # own 24-byte record, F (double4) written, near/far counts, 16-bit
+        # slots of the full list, and per tile member: its index and record
+        kernel_bytes = 24 + 32 + 8 + 2 * nbar + 28 * tiles["members"] / n
+        kname = "lj_tile"
     else:
         kernel_bytes = bytes_per_atom
         kname = "lj_fp64"
@@ -920,8 +977,7 @@ def main():
         "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f64 state; pair arithmetic f32 beyond 1.4 sigma, f32 double-float closer" if head == "mixed"
-                  else "f64"),
+        "dtype": (MIXED_DTYPE if head == "mixed" else "f64"),
         "data": "synthetic (seeded fcc lattice + Maxwell-Boltzmann velocities)",
         "config": {"workload": WORKLOAD if args.cells == 100 else WORKLOAD.replace(
                        "4,000,000 atoms (fcc 100^3", f"{n:,} atoms (fcc {args.cells}^3"),
@@ -929,8 +985,11 @@ def main():
                    "list_pairs": st["pairs"], "ghosts": st["ghosts"],
                    "forms": {f: {"atom_steps_per_s": res[f]["value"], "ms_per_step": res[f]["ms"] / args.steps,
                                  "nve_drift_per_atom_per_1000tau": res[f]["drift"],
+                                 "nve_drift_sd_over_seeds": drift.get(f, {}).get("drift_sd"),
+                                 "nve_drift_per_seed": drift.get(f, {}).get("drift_per_seed"),
                                  "nve_energy_fluctuation_per_atom": drift.get(f, {}).get("fluct"),
                                  "kernel_launches": res[f]["launches"]} for f in res},
+                   "tiles": tiles, "adress": adress,
                    "mixed_over_fp64": (res["mixed"]["value"] / res["fp64"]["value"]) if {"mixed", "fp64"} <= res.keys() else None,
                    "force_error_mixed_vs_fp64": ferr,
                    "nve_drift_measurement": DRIFT_SETUP},

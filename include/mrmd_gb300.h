@@ -506,8 +506,9 @@ const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md);
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
 /* Mixed form's tile list: [0] tiles, [1] members of the largest tile,
  * [2] 1 when the pair kernel reads shared-memory tiles, 0 when it gathers
- * through the int32 lists (a tile over capacity, or gatherNeighbours). */
-int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out3);
+ * through the int32 lists (a tile over capacity, or gatherNeighbours),
+ * [3] members of all tiles. */
+int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out4);
 /* The stepper's current neighbour pairs as canonical keys a * 2^32 + b of
  * unordered pairs of original atom indices (a < b; ghosts mapped to their
  * real atom), one key per list entry as the pair kernel reads it (the mixed

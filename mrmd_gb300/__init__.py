@@ -792,9 +792,9 @@ class LJSystem:
     def tile_stats(self):
         """Mixed form: tiles, members of the largest tile, and whether the pair
         kernel reads shared-memory tiles (True) or gathers through the cache."""
-        out = np.zeros(3, dtype=np.int64)
+        out = np.zeros(4, dtype=np.int64)
         self.ctx.lib.mrmd_md_tile_stats(self.h, _ip(out))
-        return dict(tiles=int(out[0]), max_members=int(out[1]), tiled=bool(out[2]))
+        return dict(tiles=int(out[0]), max_members=int(out[1]), tiled=bool(out[2]), members=int(out[3]))
 
     def pair_keys(self):
         """Sorted canonical keys a * 2^32 + b (a < b, original atom indices) of

@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(TILE_ROWS) k_tile_build(
     {
         memberCount[tile] = total < TILE_CAP ? total : TILE_CAP;
         atomicMax(&flags[0], total);
+        atomicAdd(&flags[2], total);
         if (bad) atomicOr(&flags[1], 1);
     }
     if (bad || row >= rows) return;
@@ -589,18 +590,20 @@ int tile_list_build(mrmd_ctx* ctx, TileList* tl, const mrmd_nlist* nearList, con
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_tile_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
+    // [0] largest tile, [1] a tile did not fit, [2] members of all tiles
     int32_t* flags = reinterpret_cast<int32_t*>(ctx->devScalars + 4);
-    MRMD_CUDA(ctx, cudaMemsetAsync(flags, 0, 2 * sizeof(int32_t), ctx->stream));
+    MRMD_CUDA(ctx, cudaMemsetAsync(flags, 0, 3 * sizeof(int32_t), ctx->stream));
     k_tile_build<<<(unsigned)tl->tiles, TILE_ROWS, smem, ctx->stream>>>(
         nearList->counts, nearList->nbrs, nearList->maxNeighbors, farList->counts, farList->nbrs,
         farList->maxNeighbors, rows, nAll, tl->members, tl->memberCount, tl->nearChunks, tl->nearChunksPerRow,
         tl->farChunks, tl->farChunksPerRow, flags);
     MRMD_TRY(after_launch(ctx, "tile_build"));
-    int32_t h[2] = {0, 0};
+    int32_t h[3] = {0, 0, 0};
     MRMD_CUDA(ctx, cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     MRMD_TRY(bounds_check(ctx));
     tl->maxMembers = h[0];
+    tl->totalMembers = h[2];
     tl->valid = h[1] == 0;
     return MRMD_OK;
 }

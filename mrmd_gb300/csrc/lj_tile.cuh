@@ -74,6 +74,7 @@ struct TileList
     int64_t tilesCap = 0, nearWords = 0, farWords = 0;  // allocated
     int64_t tiles = 0;
     int32_t maxMembers = 0;  // largest tile after the last build
+    int64_t totalMembers = 0;  // members of all tiles after the last build
     bool valid = false;      // every tile fits TILE_CAP
     void release();
 };
