@@ -891,6 +891,11 @@ def main():
 
     head = "mixed" if "mixed" in res else forms[0]
     sysm = systems[head]
+    # the pair kernel alone (dominant kernel) for the roofline, on the state the
+    # timed run left (atoms in the order of its last cell sort)
+    kern_ms = time_pair_kernel(torch, sysm, stream)
+    st = sysm.stats()
+    tiles = sysm.tile_stats() if head == "mixed" else None
 
     # force error of the mixed form against FP64 on identical positions
     ferr = None
@@ -921,9 +926,6 @@ def main():
                   "34560": adress_batch_leg(M, ctx, torch, stream, None, list(res)),
                   "4000000": adress_batch_leg(M, ctx, torch, stream, 4_000_000, list(res))}
 
-    # the pair kernel alone (dominant kernel) for the roofline
-    kern_ms = time_pair_kernel(torch, sysm, stream)
-    st = sysm.stats()
     nbar = st["pairs"] / n
     # Algorithmic bytes of the pair force per atom: the half-list FP64 layout,
     # positions (24 B) read and forces (24 B) written once, one int32 count and
@@ -932,7 +934,6 @@ def main():
     # pair from both ends, so that no force is scattered with atomics).
     nhalf = nbar / 2 if head == "mixed" else nbar
     bytes_per_atom = 24 + 24 + 4 * (1 + nhalf)
-    tiles = sysm.tile_stats() if head == "mixed" else None
     if head == "mixed":
         # own 24-byte record, F (double4) written, near/far counts, 16-bit
         # slots of the full list, and per tile member: its index and record
