@@ -262,10 +262,9 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
         // (the pair kernel decides per pair); the margin only keeps that rare.
         if (md->farList.maxNeighbors == 0) md->farList.maxNeighbors = md->cfg.maxNeighbors;
         MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
-                                  md->rsplit + 0.5 * md->cfg.skin, md->grid));
+                                  md->rsplit + 0.5 * md->cfg.skin, md->grid,
+                                  md->cfg.gatherNeighbours ? nullptr : &md->tiles));
         MRMD_TRY(list_total_pairs(ctx, &md->farList));
-        if (!md->cfg.gatherNeighbours)
-            MRMD_TRY(tile_list_build(ctx, &md->tiles, &md->list, &md->farList, nAll));
         md->tp = make_tile_params(md->lj->p0, md->lj->rcSqr, md->rsplit, md->farList.maxNeighbors);
     }
     else

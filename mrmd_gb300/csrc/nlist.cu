@@ -15,6 +15,7 @@
 
 #include "common.cuh"
 #include "nlist_impl.cuh"
+#include "lj_tile.cuh"
 
 using namespace mrmd_impl;
 
@@ -137,11 +138,6 @@ __global__ void k_cell_gather(const double4* __restrict__ pos, const int32_t* __
     }
 }
 
-__device__ __forceinline__ bool lex_above(const double4& pi, const double4& pj)
-{
-    return (pj.x > pi.x) || ((pj.x == pi.x) && ((pj.y > pi.y) || ((pj.y == pi.y) && (pj.z > pi.z))));
-}
-
 // SPLIT (full lists only): pairs with an FP32 distance below sqrt(nearSqF)
 // go to the first list, the others to the second (`capFar`, `countsFar`,
 // `nbrsFar`, overflow in maxCount[1]).  The split is a placement choice, not
@@ -158,40 +154,11 @@ __global__ void __launch_bounds__(128) k_build_list(
     for (int64_t i = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < end;
          i += (int64_t)gridDim.x * blockDim.x)
     {
-        const double4 pi = pos[i];
-        const float xi = (float)(pi.x - g.mn.x), yi = (float)(pi.y - g.mn.y), zi = (float)(pi.z - g.mn.z);
         const int32_t ci = cellOf[i];
         if (!MRMD_IN_BOUNDS(ci, g.ncell)) continue;
-        const int cz = ci % g.n.z;
-        const int cy = (ci / g.n.z) % g.n.y;
-        const int cx = ci / (g.n.z * g.n.y);
         int32_t cnt = 0, cntFar = 0;
         const int64_t row = i - begin;
-        const int R = g.reach;
-        const int axEnd = min(cx + R, g.n.x - 1);
-        const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
-        auto candidate = [&](const float4& q) {
-            const int32_t j = __float_as_int(q.w);
-            if (j == (int32_t)i || !MRMD_IN_BOUNDS(j, nPos)) return;
-            // lexicographic (x, y, z): float order is exact unless equal
-            if (!FULL && q.x < xi) return;
-            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-            const float d2f = dx * dx + dy * dy + dz * dz;
-            if (d2f > rsqHi) return;
-            bool keep;
-            if ((FULL || q.x > xi) && d2f < rsqLo)
-            {
-                keep = true;
-            }
-            else
-            {
-                const double4 pj = pos[j];
-                const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-                const double d2 =
-                    __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-                keep = (d2 <= rsq) && (FULL || lex_above(pi, pj));
-            }
-            if (!keep) return;
+        scan_candidates<FULL>(pos, cellStart, spos, g, i, ci, rsq, rsqLo, rsqHi, nPos, [&](int32_t j, float d2f) {
             if (SPLIT && d2f >= nearSqF)
             {
                 if (cntFar < capFar) nbrsFar[mrmd_dev::nbr_row(row, capFar) + 32 * (int64_t)cntFar] = j;
@@ -200,32 +167,7 @@ __global__ void __launch_bounds__(128) k_build_list(
             }
             if (cnt < cap) nbrs[mrmd_dev::nbr_row(row, cap) + 32 * (int64_t)cnt] = j;
             ++cnt;
-        };
-        for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
-        {
-            for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
-            {
-                // cells (ax, ay, az0..az1) are adjacent in the cell order, so
-                // their particles form one contiguous span of `spos`
-                {
-                    const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
-                    const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
-                    if (!MRMD_IN_BOUNDS(s0, nPos + 1) || !MRMD_IN_BOUNDS(s1, nPos + 1)) continue;
-                    // four candidates loaded per iteration: the loop is bound by
-                    // the latency of these loads, not by the arithmetic
-                    int32_t s = s0;
-                    for (; s + 3 < s1; s += 4)
-                    {
-                        const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
-                        candidate(q0);
-                        candidate(q1);
-                        candidate(q2);
-                        candidate(q3);
-                    }
-                    for (; s < s1; ++s) candidate(spos[s]);
-                }
-            }
-        }
+        });
         counts[row] = cnt < cap ? cnt : (int32_t)cap;
         if (cnt > cap) atomicMax(maxCount, cnt);
         if (SPLIT)
@@ -397,8 +339,9 @@ __global__ void k_count_sum(const int32_t* __restrict__ counts, int64_t n, unsig
 }
 
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
-                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid)
+                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid, TileList* tiles)
 {
+    if (tiles && begin != 0) return set_error(ctx, MRMD_ERR_ARG, "tile lists need rows from particle 0");
     CellList* cl = static_cast<CellList*>(nearList->cells);
     // [0], [1] longest near and far rows, [2] non-finite position flag
     int32_t* maxCount = reinterpret_cast<int32_t*>(ctx->devScalars);
@@ -418,8 +361,15 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
     {
         MRMD_TRY(ensure_list_storage(ctx, nearList, rows, capN));
         MRMD_TRY(ensure_list_storage(ctx, farList, rows, capF));
+        // [3..5]: the tile build's largest tile, overflow flag, member total
         MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 2 * sizeof(int32_t), ctx->stream));
-        if (rows > 0)
+        MRMD_CUDA(ctx, cudaMemsetAsync(maxCount + 3, 0, 3 * sizeof(int32_t), ctx->stream));
+        if (rows > 0 && tiles)
+        {
+            MRMD_TRY(tile_build_launch(ctx, tiles, pos4, cl, rows, rsq, rsqLo, rsqHi, nearSqF, capN, nearList, capF,
+                                       farList, maxCount, nPos));
+        }
+        else if (rows > 0)
         {
             k_build_list<true, true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                 reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin, end,
@@ -427,8 +377,8 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
                 farList->counts, farList->nbrs);
             MRMD_TRY(after_launch(ctx, "build_split_list"));
         }
-        int32_t hMax[3] = {0, 0, 0};
-        MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        int32_t hMax[6] = {0, 0, 0, 0, 0, 0};
+        MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         MRMD_TRY(bounds_check(ctx));
         if (hMax[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
@@ -436,6 +386,7 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
         {
             nearList->rows = farList->rows = rows;
             nearList->begin = farList->begin = begin;
+            if (tiles) tile_build_done(tiles, hMax[3], hMax[4] == 0, hMax[5]);
             return MRMD_OK;
         }
         if (hMax[0] > capN) capN = hMax[0] + hMax[0] / 8 + 4;

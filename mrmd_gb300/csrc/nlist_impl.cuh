@@ -40,6 +40,80 @@ __device__ __forceinline__ int32_t cell_of(const double4& p, const CellGrid& g)
     return (cx * g.n.y + cy) * g.n.z + cz;
 }
 
+__device__ __forceinline__ bool lex_above(const double4& pi, const double4& pj)
+{
+    return (pj.x > pi.x) || ((pj.x == pi.x) && ((pj.y > pi.y) || ((pj.y == pi.y) && (pj.z > pi.z))));
+}
+
+// The candidate scan of the list builds for particle i in cell ci: the cells
+// within g.reach per axis (only cell_x >= cell_x(i) for the half list), each
+// (x, y) column's z-range as one contiguous span of the cell-sorted `spos`.
+// keep(j, d2f) is called for every kept neighbour in scan order (d2f: FP32
+// distance squared).  Every decision is the FP64 predicate: an FP32
+// prefilter settles the clear cases (outside [rsqLo, rsqHi]) and the FP64
+// positions decide the rest.  FULL: every j != i within r; otherwise
+// Cabana's half-neighbour rule (x_j lexicographically above x_i).
+template <bool FULL, class Keep>
+__device__ __forceinline__ void scan_candidates(const double4* __restrict__ pos, const int32_t* __restrict__ cellStart,
+                                                const float4* __restrict__ spos, const CellGrid& g, int64_t i,
+                                                int32_t ci, double rsq, float rsqLo, float rsqHi, int64_t nPos,
+                                                Keep&& keep)
+{
+    const double4 pi = pos[i];
+    const float xi = (float)(pi.x - g.mn.x), yi = (float)(pi.y - g.mn.y), zi = (float)(pi.z - g.mn.z);
+    const int cz = ci % g.n.z;
+    const int cy = (ci / g.n.z) % g.n.y;
+    const int cx = ci / (g.n.z * g.n.y);
+    const int R = g.reach;
+    const int axEnd = min(cx + R, g.n.x - 1);
+    const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
+    auto candidate = [&](const float4& q) {
+        const int32_t j = __float_as_int(q.w);
+        if (j == (int32_t)i || !MRMD_IN_BOUNDS(j, nPos)) return;
+        // lexicographic (x, y, z): float order is exact unless equal
+        if (!FULL && q.x < xi) return;
+        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+        const float d2f = dx * dx + dy * dy + dz * dz;
+        if (d2f > rsqHi) return;
+        bool kept;
+        if ((FULL || q.x > xi) && d2f < rsqLo)
+        {
+            kept = true;
+        }
+        else
+        {
+            const double4 pj = pos[j];
+            const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+            kept = (d2 <= rsq) && (FULL || lex_above(pi, pj));
+        }
+        if (kept) keep(j, d2f);
+    };
+    for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
+    {
+        for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
+        {
+            // cells (ax, ay, az0..az1) are adjacent in the cell order, so
+            // their particles form one contiguous span of `spos`
+            const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
+            const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
+            if (!MRMD_IN_BOUNDS(s0, nPos + 1) || !MRMD_IN_BOUNDS(s1, nPos + 1)) continue;
+            // four candidates loaded per iteration: the loop is bound by the
+            // latency of these loads, not by the arithmetic
+            int32_t s = s0;
+            for (; s + 3 < s1; s += 4)
+            {
+                const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
+                candidate(q0);
+                candidate(q1);
+                candidate(q2);
+                candidate(q3);
+            }
+            for (; s < s1; ++s) candidate(spos[s]);
+        }
+    }
+}
+
 // Particles binned by cell: sorted[] holds particle ids in cell order
 // (ascending id inside a cell), spos[] their FP32 coordinates relative to
 // the grid origin with the id bit-cast into w.
@@ -66,11 +140,15 @@ struct CellList
 // (each pair twice, used by the mixed form so that no j-force is scattered).
 int build_half_list(mrmd_ctx* ctx, mrmd_nlist* nl, const double* pos4, int64_t nPos, int64_t begin,
                     int64_t end, double rlist, const CellGrid& grid, int64_t maxNeighbors, bool full);
+struct TileList;
 // Full list split by distance at build time: pairs closer than rnear (FP32
 // distance) in nearList, the rest within rlist in farList; the cell list of
 // nearList is used.  Each pair appears in exactly one of the two lists.
+// With `tiles` (begin = 0), the same kernel also builds the lists' tile form
+// (lj_tile.cuh).
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
-                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid);
+                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid,
+                     TileList* tiles = nullptr);
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl);
 // MRMD_ERR_ARG unless the list's rows [begin, begin + rows) are particles
 // below numLocal and every neighbour index it can hold (the candidates it
