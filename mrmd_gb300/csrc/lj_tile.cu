@@ -114,7 +114,7 @@ __device__ __forceinline__ uint32_t slot_hash(int32_t j)
 // flags[1]: longest near / far row when over capacity; flags[3]: largest
 // member count; flags[4]: a tile did not fit (its chunks stay unwritten;
 // the pair kernel then reads the int32 rows); flags[5]: members of all tiles.
-__global__ void __launch_bounds__(TILE_ROWS) k_build_tiled(
+__global__ void __launch_bounds__(TILE_ROWS, 4) k_build_tiled(
     const double4* __restrict__ pos, const int32_t* __restrict__ cellOf, const int32_t* __restrict__ cellStart,
     const float4* __restrict__ spos, CellGrid g, int64_t rows, double rsq, float rsqLo, float rsqHi, float nearSqF,
     int64_t nPos, int64_t capN, int32_t* __restrict__ countsN, int32_t* __restrict__ nbrsN, int64_t capF,
