@@ -82,8 +82,8 @@ TileParams make_tile_params(const LJDev& p, double rcSqr, double rsplit, int64_t
 
 namespace
 {
-constexpr int HT_BITS = 13;
-constexpr int HT = 1 << HT_BITS;  // hash slots per tile (load <= TILE_CAP / HT = 0.5)
+constexpr int HT_BITS = 12;
+constexpr int HT = 1 << HT_BITS;  // hash slots per tile (load <= TILE_CAP / HT = 0.75)
 
 __global__ void k_tile_split(const double4* __restrict__ pos, int64_t n, SplitParams sp, float4* __restrict__ recA,
                              float2* __restrict__ recB)

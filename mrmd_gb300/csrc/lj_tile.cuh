@@ -29,8 +29,9 @@
 namespace mrmd_impl
 {
 constexpr int TILE_ROWS = 256;
-// members per tile the 16-bit slots and the build's hash table allow
-constexpr int TILE_CAP = 4096;
+// members per tile the build's shared hash table allows (a 256-row tile of
+// the dense LJ fluid, rho 0.8442 and r_list 2.8 sigma, has about 1,400-2,200)
+constexpr int TILE_CAP = 3072;
 
 // Split parameters with the quantum Q = 2^-q of the tile kernel for list
 // radius rlist: the largest Q with 2^11 Q > rlist * 1.0625.  Coordinates
