@@ -104,23 +104,18 @@ __device__ __forceinline__ uint32_t slot_hash(int32_t j)
     return ((uint32_t)j * 2654435761u) >> (32 - HT_BITS);
 }
 
-// The split full list (near rows: FP32 distance below sqrt(nearSqF) at the
-// build) and its tile form in one pass, one block per tile of TILE_ROWS
-// rows.  Phase 1: each thread scans its row's candidates (the scan of
-// k_build_list), writes the kept pairs into the int32 near / far rows and
-// inserts them into a shared open-addressing table of the tile's members.
-// Phase 2 numbers the occupied table entries in table order (the member
-// slots).  Phase 3 rewrites each row as slots in 8-entry chunks.  flags[0],
-// flags[1]: longest near / far row when over capacity; flags[3]: largest
-// member count; flags[4]: a tile did not fit (its chunks stay unwritten;
-// the pair kernel then reads the int32 rows); flags[5]: members of all tiles.
-__global__ void __launch_bounds__(TILE_ROWS, 4) k_build_tiled(
-    const double4* __restrict__ pos, const int32_t* __restrict__ cellOf, const int32_t* __restrict__ cellStart,
-    const float4* __restrict__ spos, CellGrid g, int64_t rows, double rsq, float rsqLo, float rsqHi, float nearSqF,
-    int64_t nPos, int64_t capN, int32_t* __restrict__ countsN, int32_t* __restrict__ nbrsN, int64_t capF,
-    int32_t* __restrict__ countsF, int32_t* __restrict__ nbrsF, int32_t* __restrict__ flags,
-    int32_t* __restrict__ members, int32_t* __restrict__ memberCount, uint4* __restrict__ nearChunks, int64_t chN,
-    uint4* __restrict__ farChunks, int64_t chF)
+// The tile form of the split full list just built (k_build_list<1, 1>), one
+// block per tile of TILE_ROWS rows.  Phase 1 inserts every neighbour index of
+// the rows into a shared open-addressing table of the tile's members, phase 2
+// numbers the occupied entries in table order (the member slots), phase 3
+// rewrites each row as slots in 8-entry chunks.  flags[3]: largest member
+// count; flags[4]: a tile did not fit (its chunks stay unwritten; the pair
+// kernel then reads the int32 rows); flags[5]: members of all tiles.
+__global__ void __launch_bounds__(TILE_ROWS) k_tile_build(
+    const int32_t* __restrict__ countsN, const int32_t* __restrict__ nbrsN, int64_t capN,
+    const int32_t* __restrict__ countsF, const int32_t* __restrict__ nbrsF, int64_t capF, int64_t rows, int64_t nAll,
+    int32_t* __restrict__ flags, int32_t* __restrict__ members, int32_t* __restrict__ memberCount,
+    uint4* __restrict__ nearChunks, int64_t chN, uint4* __restrict__ farChunks, int64_t chF)
 {
     extern __shared__ int32_t keys[];                         // [HT]
     uint16_t* slot = reinterpret_cast<uint16_t*>(keys + HT);  // [HT]
@@ -133,7 +128,14 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_build_tiled(
     if (tid == 0) badS = 0;
     __syncthreads();
 
+    // most indices are already in the table (a member is the neighbour of
+    // about a dozen of the tile's rows): a plain read settles them
     auto insert = [&](int32_t j) {
+        if (j < 0 || j >= nAll)
+        {
+            badS = 1;
+            return;
+        }
         uint32_t h = slot_hash(j);
         for (int probe = 0; probe < HT; ++probe)
         {
@@ -149,31 +151,14 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_build_tiled(
         badS = 1;  // table full
     };
     int32_t cn = 0, cf = 0;
-    int32_t* colN = nbrsN + mrmd_dev::nbr_row(row, capN);
-    int32_t* colF = nbrsF + mrmd_dev::nbr_row(row, capF);
+    const int32_t* colN = nbrsN + mrmd_dev::nbr_row(row, capN);
+    const int32_t* colF = nbrsF + mrmd_dev::nbr_row(row, capF);
     if (row < rows)
     {
-        const int32_t ci = cellOf[row];
-        if (MRMD_IN_BOUNDS(ci, g.ncell))
-            scan_candidates<true>(pos, cellStart, spos, g, row, ci, rsq, rsqLo, rsqHi, nPos, [&](int32_t j, float d2f) {
-                if (d2f >= nearSqF)
-                {
-                    if (cf < capF) colF[32 * (int64_t)cf] = j;
-                    ++cf;
-                }
-                else
-                {
-                    if (cn < capN) colN[32 * (int64_t)cn] = j;
-                    ++cn;
-                }
-                insert(j);
-            });
-        countsN[row] = cn < capN ? cn : (int32_t)capN;
-        countsF[row] = cf < capF ? cf : (int32_t)capF;
-        if (cn > capN) atomicMax(&flags[0], cn);
-        if (cf > capF) atomicMax(&flags[1], cf);
-        cn = cn < capN ? cn : (int32_t)capN;
-        cf = cf < capF ? cf : (int32_t)capF;
+        cn = countsN[row];
+        cf = countsF[row];
+        for (int32_t k = 0; k < cn; ++k) insert(colN[32 * (int64_t)k]);
+        for (int32_t k = 0; k < cf; ++k) insert(colF[32 * (int64_t)k]);
     }
     __syncthreads();
 
@@ -568,9 +553,8 @@ int tile_split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitP
     return after_launch(ctx, "tile_split");
 }
 
-int tile_build_launch(mrmd_ctx* ctx, TileList* tl, const double* pos4, const CellList* cl, int64_t rows, double rsq,
-                      float rsqLo, float rsqHi, float nearSqF, int64_t capN, const mrmd_nlist* nearList, int64_t capF,
-                      const mrmd_nlist* farList, int32_t* flags, int64_t nPos)
+int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, const mrmd_nlist* nearList,
+                      const mrmd_nlist* farList, int32_t* flags)
 {
     tl->valid = false;
     tl->tiles = div_up(rows, TILE_ROWS);
@@ -584,6 +568,7 @@ int tile_build_launch(mrmd_ctx* ctx, TileList* tl, const double* pos4, const Cel
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&tl->memberCount), sizeof(int32_t) * (size_t)c));
         tl->tilesCap = c;
     }
+    const int64_t capN = nearList->maxNeighbors, capF = farList->maxNeighbors;
     tl->nearChunksPerRow = div_up(capN, 8);
     tl->farChunksPerRow = div_up(capF, 8);
     const int64_t rows32 = div_up(rows, 32) * 32;
@@ -604,17 +589,15 @@ int tile_build_launch(mrmd_ctx* ctx, TileList* tl, const double* pos4, const Cel
         tl->farWords = w;
     }
     const size_t smem = sizeof(int32_t) * HT + sizeof(uint16_t) * HT;
-    // the kernels' shared-memory limits (per device; set here, outside any
-    // stream capture)
+    // the pair kernel's shared-memory limit (per device; set here, outside
+    // any stream capture)
     const int maxPair = TILE_CAP * (int)(sizeof(float4) + sizeof(float2));
-    MRMD_CUDA(ctx, cudaFuncSetAttribute(k_build_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
-    k_build_tiled<<<(unsigned)tl->tiles, TILE_ROWS, smem, ctx->stream>>>(
-        reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, rows, rsq, rsqLo, rsqHi,
-        nearSqF, nPos, capN, nearList->counts, nearList->nbrs, capF, farList->counts, farList->nbrs, flags,
-        tl->members, tl->memberCount, tl->nearChunks, tl->nearChunksPerRow, tl->farChunks, tl->farChunksPerRow);
-    return after_launch(ctx, "build_tiled");
+    k_tile_build<<<(unsigned)tl->tiles, TILE_ROWS, smem, ctx->stream>>>(
+        nearList->counts, nearList->nbrs, capN, farList->counts, farList->nbrs, capF, rows, nAll, flags, tl->members,
+        tl->memberCount, tl->nearChunks, tl->nearChunksPerRow, tl->farChunks, tl->farChunksPerRow);
+    return after_launch(ctx, "tile_build");
 }
 
 void tile_build_done(TileList* tl, int32_t maxMembers, bool valid, int64_t totalMembers)

@@ -80,16 +80,14 @@ struct TileList
     void release();
 };
 
-struct CellList;
-// The list build of build_split_list with its tile form (one block per tile:
-// the distinct neighbours of its rows get slots through a shared-memory hash
-// table): sizes `tl` for capacities capN / capF and launches; flags are the
-// build's device flags (see k_build_tiled).  tile_build_done records the
-// flags the caller read back; tl->valid is false when a tile has more than
-// TILE_CAP members.
-int tile_build_launch(mrmd_ctx* ctx, TileList* tl, const double* pos4, const CellList* cl, int64_t rows, double rsq,
-                      float rsqLo, float rsqHi, float nearSqF, int64_t capN, const mrmd_nlist* nearList, int64_t capF,
-                      const mrmd_nlist* farList, int32_t* flags, int64_t nPos);
+// The tile form of a near/far split full list over rows [0, rows) of
+// particles [0, nAll), launched right after the list build (one block per
+// tile: the distinct neighbours of its rows get slots through a
+// shared-memory hash table); flags: the build's device flags (see
+// k_tile_build).  tile_build_done records what the caller read back;
+// tl->valid is false when a tile has more than TILE_CAP members.
+int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, const mrmd_nlist* nearList,
+                      const mrmd_nlist* farList, int32_t* flags);
 void tile_build_done(TileList* tl, int32_t maxMembers, bool valid, int64_t totalMembers);
 
 // Per-system constants of the pair kernel.

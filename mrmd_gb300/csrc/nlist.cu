@@ -364,18 +364,14 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
         // [3..5]: the tile build's largest tile, overflow flag, member total
         MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 2 * sizeof(int32_t), ctx->stream));
         MRMD_CUDA(ctx, cudaMemsetAsync(maxCount + 3, 0, 3 * sizeof(int32_t), ctx->stream));
-        if (rows > 0 && tiles)
-        {
-            MRMD_TRY(tile_build_launch(ctx, tiles, pos4, cl, rows, rsq, rsqLo, rsqHi, nearSqF, capN, nearList, capF,
-                                       farList, maxCount, nPos));
-        }
-        else if (rows > 0)
+        if (rows > 0)
         {
             k_build_list<true, true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                 reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin, end,
                 rsq, rsqLo, rsqHi, capN, nearList->counts, nearList->nbrs, maxCount, nPos, nearSqF, capF,
                 farList->counts, farList->nbrs);
             MRMD_TRY(after_launch(ctx, "build_split_list"));
+            if (tiles) MRMD_TRY(tile_build_launch(ctx, tiles, rows, nPos, nearList, farList, maxCount));
         }
         int32_t hMax[6] = {0, 0, 0, 0, 0, 0};
         MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));

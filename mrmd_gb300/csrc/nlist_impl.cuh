@@ -144,8 +144,8 @@ struct TileList;
 // Full list split by distance at build time: pairs closer than rnear (FP32
 // distance) in nearList, the rest within rlist in farList; the cell list of
 // nearList is used.  Each pair appears in exactly one of the two lists.
-// With `tiles` (begin = 0), the same kernel also builds the lists' tile form
-// (lj_tile.cuh).
+// With `tiles` (begin = 0), the lists' tile form (lj_tile.cuh) is built
+// right after them, before the one synchronisation of the build.
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
                      int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid,
                      TileList* tiles = nullptr);
