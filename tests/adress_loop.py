@@ -15,12 +15,13 @@ def random_system(n, box, seed):
 
 
 def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_min=(0.0, 0.0, 0.0),
-                tf_table=None, comp_frozen=False, on_step=None):
+                tf_table=None, comp_frozen=False, on_step=None, tf_out=None):
     """Returns positions, velocities, per-step energies, the TF table and the
     LJ_IdealGas mean compensation energies after nsteps.  tf_table sets the
     initial thermodynamic-force table; comp_frozen starts LJ_IdealGas at run 1
     so that its compensation means stay zero; on_step(st, positions) sees the
-    positions after every step."""
+    positions after every step; tf_out (a dict) receives the density profile
+    accumulated since the last update and its sample count."""
     n = len(pos)
     lo = np.asarray(box_min, dtype=np.float64)
     hi = lo + np.asarray(box, dtype=np.float64)
@@ -69,5 +70,8 @@ def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_
             tf.update(p["tfs"], p["tfr"])
         if on_step is not None:
             on_step(st, a.pos[:n])
+    if tf_out is not None:
+        tf_out["density"] = tf.density[:, 0].copy()
+        tf_out["samples"] = tf.samples()
     return (a.pos[:n].copy(), a.vel[:n].copy(), np.array(energies), tf.force[:, 0].copy(),
             ljig.mean[:, 0].copy())

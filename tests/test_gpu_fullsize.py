@@ -1,12 +1,14 @@
 """The 4,000,000-atom LJ fluid of the precision study at full size, through
 size-independent properties: mixed-form forces within 1e-6 of the FP64 form's
-(normalised by the RMS force), energies and virials within 1e-7, Newton's
+per atom (floored at 0.1 of the RMS force), energies and virials within 1e-9, Newton's
 third law (the FP64 half-list forces sum to zero up to rounding), and both
 lists holding every pair within the list radius (the full list has each pair
 twice: local-local pairs from both ends, local-ghost pairs once per end that
 is local)."""
 import numpy as np
 import pytest
+
+from conftest import per_atom_rel_err
 
 from test_gpu_md import fcc, mb_velocities
 
@@ -38,8 +40,9 @@ def test_lj_4m_mixed_vs_fp64(M):
     rms = float(np.sqrt((fr * fr).sum(1).mean()))
     err = float(np.linalg.norm(fm - fr, axis=1).max()) / rms
     assert err < 1e-6, err
-    assert abs(em - er) <= 1e-7 * abs(er)
-    assert abs(wm - wr) <= 1e-7 * abs(wr)
+    assert per_atom_rel_err(fm, fr, 0.1) < 1e-6
+    assert abs(em - er) <= 1e-9 * abs(er)
+    assert abs(wm - wr) <= 1e-9 * abs(wr)
     # Newton's third law: pair forces cancel (rounding of 4 M sums only)
     assert np.abs(fr.sum(0)).max() <= 1e-9 * rms * n
     half, full = ref.stats()["pairs"], mix.stats()["pairs"]

@@ -127,7 +127,18 @@ def test_mixed_cutoff_decision_at_scale(M):
     rms = np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean())
     err = np.linalg.norm(fm - fr, axis=1).max() / rms
     assert err < 1e-6, err
+    # per atom, floored at 0.1 of the RMS force (close contacts of the
+    # jittered lattice give forces of thousands here)
+    assert per_atom_rel_err(fm, fr, 0.1) < 1e-6
     assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
+
+
+def nve_drift_per_1000tau(rec, n, dt=0.005):
+    """Slope of a least-squares line through (E_pot + E_kin) / N of every
+    step, in epsilon per atom per 1000 tau."""
+    e = (rec[:, 0] + rec[:, 2]) / n
+    t = np.arange(len(e)) * dt
+    return float(np.polyfit(t, e, 1)[0]) * 1000.0
 
 
 def test_mixed_vs_fp64_forces_and_drift(M):
@@ -147,20 +158,28 @@ def test_mixed_vs_fp64_forces_and_drift(M):
     rms = np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean())
     err = np.linalg.norm(fm - fr, axis=1).max() / rms
     assert err < 1e-6, err
-    # NVE energy drift of the mixed form over 400 steps
-    e = mix.run(400)
-    _, vv, _ = mix.state()
+    assert per_atom_rel_err(fm, fr, 0.1) < 1e-6
+    # NVE energy drift over 100 tau (20,000 steps) of both forms from the same
+    # equilibrated state, from the device-summed per-step energies.  Limit:
+    # 5e-4 epsilon per atom per 1000 tau for each form, and the mixed form's
+    # drift within 5e-4 of the FP64 form's (the drift of this protocol comes
+    # from the force jump at rc and the fixed rebuild interval, not from the
+    # pair arithmetic)
     n = len(pos)
-    # total energy at the end vs start (potential from the run, kinetic at end)
-    assert np.all(np.isfinite(e))
+    drift = {}
+    for name, prec in (("fp64", M.PREC_FP64), ("mixed", M.PREC_MIXED)):
+        s = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=prec, observe=True)
+        drift[name] = nve_drift_per_1000tau(s.run_observed(20000), n)
+    assert abs(drift["fp64"]) <= 5e-4 and abs(drift["mixed"]) <= 5e-4, drift
+    assert abs(drift["mixed"] - drift["fp64"]) <= 5e-4, drift
 
 
 @pytest.mark.parametrize("split_radius,bound", [(0.0, 1e-6), (1.8, 5e-7), (2.8, 1e-8)])
 def test_mixed_split_radius_error(M, split_radius, bound):
     """The mixed form evaluates pairs beyond the split radius in FP32 (default
-    1.4 sigma) and closer pairs in double-float; a split radius at the list
+    1.5 sigma) and closer pairs in double-float; a split radius at the list
     radius keeps every pair in double-float.  Force error against FP64 on the
-    same positions, normalised by the RMS force."""
+    same positions, per atom, floored at 0.1 of the RMS force."""
     pos, L = fcc(8)
     vel = mb_velocities(len(pos), 0.728, 4)
     ref = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64)
@@ -172,10 +191,9 @@ def test_mixed_split_radius_error(M, split_radius, bound):
     er, wr = ref.eval_forces()
     _, _, fm = mix.state()
     _, _, fr = ref.state()
-    rms = np.sqrt((np.linalg.norm(fr, axis=1) ** 2).mean())
-    err = np.linalg.norm(fm - fr, axis=1).max() / rms
+    err = per_atom_rel_err(fm, fr, 0.1)
     assert err < bound, err
-    assert abs(em - er) <= 1e-6 * abs(er) and abs(wm - wr) <= 1e-6 * abs(wr)
+    assert abs(em - er) <= 1e-9 * abs(er) and abs(wm - wr) <= 1e-9 * abs(wr)
     assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
 
 
@@ -201,12 +219,13 @@ def test_elongated_box_linear_sort_fallback(M):
     assert np.abs(fm - fr).max() / rms < 1e-8
     assert abs(em - er) <= 1e-7 * abs(er)
     # the default split: this near-lattice gas has a small RMS force (about 1.6
-    # against 13.7 in the dense fluid), so the FP32 rounding of the pairs beyond
-    # 1.4 sigma is a larger share of it
+    # against 13.7 in the dense fluid); its per-atom error floored at 0.1 of
+    # that RMS force
     mix = M.LJSystem(pos, vel, [0, 0, 0], box, precision=M.PREC_MIXED)
     mix.eval_forces()
     _, _, fm = mix.state()
-    assert np.abs(fm - fr).max() / rms < 3e-6
+    assert np.abs(fm - fr).max() / rms < 1e-6
+    assert per_atom_rel_err(fm, fr, 0.1) < 1e-6
     e = mix.run(30)
     assert np.all(np.isfinite(e))
 
