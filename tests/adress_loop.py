@@ -72,6 +72,6 @@ def oracle_loop(orc, pos, vel, box, nsteps, p, slab_center=None, seed=None, box_
             on_step(st, a.pos[:n])
     if tf_out is not None:
         tf_out["density"] = tf.density[:, 0].copy()
-        tf_out["samples"] = tf.samples()
+        tf_out["samples"] = tf.samples
     return (a.pos[:n].copy(), a.vel[:n].copy(), np.array(energies), tf.force[:, 0].copy(),
             ljig.mean[:, 0].copy())
