@@ -507,8 +507,10 @@ const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md);
 /* Mixed form's tile list: [0] tiles, [1] members of the largest tile,
  * [2] 1 when the pair kernel reads shared-memory tiles, 0 when it gathers
  * through the int32 lists (a tile over capacity, or gatherNeighbours),
- * [3] members of all tiles. */
-int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out4);
+ * [3] members of all tiles, [4] tiles of the last rebuild that the one-pass
+ * tile build could not fit (the rebuild then made the int32 rows and their
+ * tile form), [5] rebuilds so far that needed that second path. */
+int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out6);
 /* The stepper's current neighbour pairs as canonical keys a * 2^32 + b of
  * unordered pairs of original atom indices (a < b; ghosts mapped to their
  * real atom), one key per list entry as the pair kernel reads it (the mixed

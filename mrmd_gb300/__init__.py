@@ -790,11 +790,14 @@ class LJSystem:
                     list_capacity=int(out[4]))
 
     def tile_stats(self):
-        """Mixed form: tiles, members of the largest tile, and whether the pair
-        kernel reads shared-memory tiles (True) or gathers through the cache."""
-        out = np.zeros(4, dtype=np.int64)
+        """Mixed form: tiles, members of the largest tile, whether the pair
+        kernel reads shared-memory tiles (True) or gathers through the cache,
+        members of all tiles, the tiles the last rebuild's one-pass build could
+        not fit, and the rebuilds so far that needed the int32 rows."""
+        out = np.zeros(6, dtype=np.int64)
         self.ctx.lib.mrmd_md_tile_stats(self.h, _ip(out))
-        return dict(tiles=int(out[0]), max_members=int(out[1]), tiled=bool(out[2]), members=int(out[3]))
+        return dict(tiles=int(out[0]), max_members=int(out[1]), tiled=bool(out[2]), members=int(out[3]),
+                    unfit_tiles=int(out[4]), two_pass_builds=int(out[5]))
 
     def pair_keys(self):
         """Sorted canonical keys a * 2^32 + b (a < b, original atom indices) of

@@ -553,8 +553,7 @@ int tile_split_coords(mrmd_ctx* ctx, const double* pos4, int64_t n, const SplitP
     return after_launch(ctx, "tile_split");
 }
 
-int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, const mrmd_nlist* nearList,
-                      const mrmd_nlist* farList, int32_t* flags)
+int tile_storage(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t capN, int64_t capF)
 {
     tl->valid = false;
     tl->tiles = div_up(rows, TILE_ROWS);
@@ -568,7 +567,6 @@ int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, c
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&tl->memberCount), sizeof(int32_t) * (size_t)c));
         tl->tilesCap = c;
     }
-    const int64_t capN = nearList->maxNeighbors, capF = farList->maxNeighbors;
     tl->nearChunksPerRow = div_up(capN, 8);
     tl->farChunksPerRow = div_up(capF, 8);
     const int64_t rows32 = div_up(rows, 32) * 32;
@@ -588,12 +586,21 @@ int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, c
         MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&tl->farChunks), sizeof(uint4) * (size_t)w));
         tl->farWords = w;
     }
-    const size_t smem = sizeof(int32_t) * HT + sizeof(uint16_t) * HT;
     // the pair kernel's shared-memory limit (per device; set here, outside
     // any stream capture)
     const int maxPair = TILE_CAP * (int)(sizeof(float4) + sizeof(float2));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
     MRMD_CUDA(ctx, cudaFuncSetAttribute(k_lj_tile<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxPair));
+    return MRMD_OK;
+}
+
+int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, const mrmd_nlist* nearList,
+                      const mrmd_nlist* farList, int32_t* flags)
+{
+    const int64_t capN = nearList->maxNeighbors, capF = farList->maxNeighbors;
+    MRMD_TRY(tile_storage(ctx, tl, rows, capN, capF));
+    if (rows == 0) return MRMD_OK;
+    const size_t smem = sizeof(int32_t) * HT + sizeof(uint16_t) * HT;
     k_tile_build<<<(unsigned)tl->tiles, TILE_ROWS, smem, ctx->stream>>>(
         nearList->counts, nearList->nbrs, capN, farList->counts, farList->nbrs, capF, rows, nAll, flags, tl->members,
         tl->memberCount, tl->nearChunks, tl->nearChunksPerRow, tl->farChunks, tl->farChunksPerRow);

@@ -77,15 +77,22 @@ struct TileList
     int32_t maxMembers = 0;  // largest tile after the last build
     int64_t totalMembers = 0;  // members of all tiles after the last build
     bool valid = false;      // every tile fits TILE_CAP
+    int64_t unfitTiles = 0;     // tiles the last one-pass build could not fit
+    int64_t twoPassBuilds = 0;  // builds that made the int32 rows and their tile form
     void release();
 };
 
+// Storage of tl for `rows` rows with near / far row capacities capN / capF
+// (entries); also raises the pair kernel's shared-memory limit.
+int tile_storage(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t capN, int64_t capF);
+
 // The tile form of a near/far split full list over rows [0, rows) of
-// particles [0, nAll), launched right after the list build (one block per
-// tile: the distinct neighbours of its rows get slots through a
-// shared-memory hash table); flags: the build's device flags (see
-// k_tile_build).  tile_build_done records what the caller read back;
-// tl->valid is false when a tile has more than TILE_CAP members.
+// particles [0, nAll), from its int32 rows, launched right after the list
+// build (one block per tile: the distinct neighbours of its rows get slots
+// through a shared-memory hash table); flags: the build's device flags (see
+// k_tile_build).  The one-pass build (tile_list_launch, nlist_impl.cuh) makes
+// the same form from the cell list.  tile_build_done records what the caller
+// read back; tl->valid is false when a tile has more than TILE_CAP members.
 int tile_build_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nAll, const mrmd_nlist* nearList,
                       const mrmd_nlist* farList, int32_t* flags);
 void tile_build_done(TileList* tl, int32_t maxMembers, bool valid, int64_t totalMembers);

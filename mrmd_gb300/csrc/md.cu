@@ -751,14 +751,16 @@ int mrmd_md_eval(mrmd_ctx* ctx, mrmd_md* md, int what, double* ev2)
 const mrmd_atoms* mrmd_md_atoms(const mrmd_md* md) { return md ? &md->atoms : nullptr; }
 const mrmd_nlist* mrmd_md_nlist(const mrmd_md* md) { return md ? &md->list : nullptr; }
 
-int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out4)
+int mrmd_md_tile_stats(const mrmd_md* md, int64_t* out6)
 {
-    if (!md || !out4) return MRMD_ERR_ARG;
+    if (!md || !out6) return MRMD_ERR_ARG;
     const bool mixed = md->cfg.precision == MRMD_PREC_MIXED;
-    out4[0] = mixed ? md->tiles.tiles : 0;
-    out4[1] = mixed ? md->tiles.maxMembers : 0;
-    out4[2] = mixed && md->tiles.valid && !md->cfg.gatherNeighbours ? 1 : 0;
-    out4[3] = mixed ? md->tiles.totalMembers : 0;
+    out6[0] = mixed ? md->tiles.tiles : 0;
+    out6[1] = mixed ? md->tiles.maxMembers : 0;
+    out6[2] = mixed && md->tiles.valid && !md->cfg.gatherNeighbours ? 1 : 0;
+    out6[3] = mixed ? md->tiles.totalMembers : 0;
+    out6[4] = mixed ? md->tiles.unfitTiles : 0;
+    out6[5] = mixed ? md->tiles.twoPassBuilds : 0;
     return MRMD_OK;
 }
 

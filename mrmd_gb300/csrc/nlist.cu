@@ -364,20 +364,40 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
         // [3..5]: the tile build's largest tile, overflow flag, member total
         MRMD_CUDA(ctx, cudaMemsetAsync(maxCount, 0, 2 * sizeof(int32_t), ctx->stream));
         MRMD_CUDA(ctx, cudaMemsetAsync(maxCount + 3, 0, 3 * sizeof(int32_t), ctx->stream));
-        if (rows > 0)
-        {
+        auto int32_rows = [&]() -> int {
             k_build_list<true, true><<<grid_for(ctx, rows, 128, 16), 128, 0, ctx->stream>>>(
                 reinterpret_cast<const double4*>(pos4), cl->cellOf, cl->cellStart, cl->spos, cl->g, begin, end,
                 rsq, rsqLo, rsqHi, capN, nearList->counts, nearList->nbrs, maxCount, nPos, nearSqF, capF,
                 farList->counts, farList->nbrs);
-            MRMD_TRY(after_launch(ctx, "build_split_list"));
-            if (tiles) MRMD_TRY(tile_build_launch(ctx, tiles, rows, nPos, nearList, farList, maxCount));
+            return after_launch(ctx, "build_split_list");
+        };
+        if (rows > 0)
+        {
+            if (tiles)
+                MRMD_TRY(tile_list_launch(ctx, tiles, rows, nPos, *cl, rsq, rsqLo, rsqHi, nearSqF, nearList,
+                                          farList, pos4, maxCount));
+            else
+                MRMD_TRY(int32_rows());
         }
         int32_t hMax[6] = {0, 0, 0, 0, 0, 0};
         MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         MRMD_TRY(bounds_check(ctx));
         if (hMax[2]) return set_error(ctx, MRMD_ERR_NONFINITE, "non-finite particle position at the list build");
+        if (tiles) tiles->unfitTiles = 0;
+        if (tiles && rows > 0 && hMax[4] != 0 && hMax[0] <= capN && hMax[1] <= capF)
+        {
+            // a tile did not fit the one-pass build: the int32 rows, then
+            // their tile form
+            tiles->unfitTiles = hMax[4];
+            tiles->twoPassBuilds++;
+            MRMD_CUDA(ctx, cudaMemsetAsync(maxCount + 3, 0, 3 * sizeof(int32_t), ctx->stream));
+            MRMD_TRY(int32_rows());
+            MRMD_TRY(tile_build_launch(ctx, tiles, rows, nPos, nearList, farList, maxCount));
+            MRMD_CUDA(ctx, cudaMemcpyAsync(hMax, maxCount, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+            MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            MRMD_TRY(bounds_check(ctx));
+        }
         if (hMax[0] <= capN && hMax[1] <= capF)
         {
             nearList->rows = farList->rows = rows;

@@ -45,14 +45,63 @@ __device__ __forceinline__ bool lex_above(const double4& pi, const double4& pj)
     return (pj.x > pi.x) || ((pj.x == pi.x) && ((pj.y > pi.y) || ((pj.y == pi.y) && (pj.z > pi.z))));
 }
 
-// The candidate scan of the list builds for particle i in cell ci: the cells
-// within g.reach per axis (only cell_x >= cell_x(i) for the half list), each
-// (x, y) column's z-range as one contiguous span of the cell-sorted `spos`.
-// keep(j, d2f) is called for every kept neighbour in scan order (d2f: FP32
-// distance squared).  Every decision is the FP64 predicate: an FP32
-// prefilter settles the clear cases (outside [rsqLo, rsqHi]) and the FP64
-// positions decide the rest.  FULL: every j != i within r; otherwise
-// Cabana's half-neighbour rule (x_j lexicographically above x_i).
+// The candidate spans of particle i in cell ci: the columns within g.reach
+// cells per axis (only cell_x >= cell_x(i) for the half list), each column's
+// z range [z0, z1] as one contiguous span [s0, s1) of the cell-sorted
+// particles.  span(ax, ay, c0, z0, z1, s0, s1) is called in scan order
+// (c0: the cell index of (ax, ay, 0)).
+template <bool FULL, class Span>
+__device__ __forceinline__ void for_each_span(const int32_t* __restrict__ cellStart, const CellGrid& g, int32_t ci,
+                                              int64_t nPos, Span&& span)
+{
+    const int cz = ci % g.n.z;
+    const int cy = (ci / g.n.z) % g.n.y;
+    const int cx = ci / (g.n.z * g.n.y);
+    const int R = g.reach;
+    const int axEnd = min(cx + R, g.n.x - 1);
+    const int z0 = max(cz - R, 0), z1 = min(cz + R, g.n.z - 1);
+    const int ay0 = max(cy - R, 0), ay1 = min(cy + R, g.n.y - 1);
+    for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
+    {
+        for (int ay = ay0; ay <= ay1; ++ay)
+        {
+            // cells (ax, ay, z0..z1) are adjacent in the cell order, so their
+            // particles form one contiguous span of the sorted arrays
+            const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
+            const int32_t s0 = cellStart[c0 + z0], s1 = cellStart[c0 + z1 + 1];
+            if (!MRMD_IN_BOUNDS(s0, nPos + 1) || !MRMD_IN_BOUNDS(s1, nPos + 1)) continue;
+            span(ax, ay, c0, z0, z1, s0, s1);
+        }
+    }
+}
+
+// The candidate test of the list builds: every decision is the FP64
+// predicate.  An FP32 prefilter settles the clear cases (outside [rsqLo,
+// rsqHi]) and the FP64 positions decide the rest.  FULL: every j != i within
+// r; otherwise Cabana's half-neighbour rule (x_j lexicographically above x_i).
+// Returns true when j (the candidate q, id in q.w) is kept; d2f: its FP32
+// distance squared.
+template <bool FULL>
+__device__ __forceinline__ bool candidate_kept(const double4* __restrict__ pos, const double4& pi, int64_t i,
+                                               float xi, float yi, float zi, const float4& q, double rsq,
+                                               float rsqLo, float rsqHi, int64_t nPos, float& d2f)
+{
+    const int32_t j = __float_as_int(q.w);
+    if (j == (int32_t)i || !MRMD_IN_BOUNDS(j, nPos)) return false;
+    // lexicographic (x, y, z): float order is exact unless equal
+    if (!FULL && q.x < xi) return false;
+    const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+    d2f = dx * dx + dy * dy + dz * dz;
+    if (d2f > rsqHi) return false;
+    if ((FULL || q.x > xi) && d2f < rsqLo) return true;
+    const double4 pj = pos[j];
+    const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+    return (d2 <= rsq) && (FULL || lex_above(pi, pj));
+}
+
+// The candidate scan of the list builds for particle i in cell ci: keep(j,
+// d2f) is called for every kept neighbour in scan order.
 template <bool FULL, class Keep>
 __device__ __forceinline__ void scan_candidates(const double4* __restrict__ pos, const int32_t* __restrict__ cellStart,
                                                 const float4* __restrict__ spos, const CellGrid& g, int64_t i,
@@ -61,57 +110,25 @@ __device__ __forceinline__ void scan_candidates(const double4* __restrict__ pos,
 {
     const double4 pi = pos[i];
     const float xi = (float)(pi.x - g.mn.x), yi = (float)(pi.y - g.mn.y), zi = (float)(pi.z - g.mn.z);
-    const int cz = ci % g.n.z;
-    const int cy = (ci / g.n.z) % g.n.y;
-    const int cx = ci / (g.n.z * g.n.y);
-    const int R = g.reach;
-    const int axEnd = min(cx + R, g.n.x - 1);
-    const int az0 = max(cz - R, 0), az1 = min(cz + R, g.n.z - 1);
     auto candidate = [&](const float4& q) {
-        const int32_t j = __float_as_int(q.w);
-        if (j == (int32_t)i || !MRMD_IN_BOUNDS(j, nPos)) return;
-        // lexicographic (x, y, z): float order is exact unless equal
-        if (!FULL && q.x < xi) return;
-        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-        const float d2f = dx * dx + dy * dy + dz * dz;
-        if (d2f > rsqHi) return;
-        bool kept;
-        if ((FULL || q.x > xi) && d2f < rsqLo)
-        {
-            kept = true;
-        }
-        else
-        {
-            const double4 pj = pos[j];
-            const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-            kept = (d2 <= rsq) && (FULL || lex_above(pi, pj));
-        }
-        if (kept) keep(j, d2f);
+        float d2f;
+        if (candidate_kept<FULL>(pos, pi, i, xi, yi, zi, q, rsq, rsqLo, rsqHi, nPos, d2f))
+            keep(__float_as_int(q.w), d2f);
     };
-    for (int ax = FULL ? max(cx - R, 0) : cx; ax <= axEnd; ++ax)
-    {
-        for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
+    for_each_span<FULL>(cellStart, g, ci, nPos, [&](int, int, int32_t, int, int, int32_t s0, int32_t s1) {
+        // four candidates loaded per iteration: the loop is bound by the
+        // latency of these loads, not by the arithmetic
+        int32_t s = s0;
+        for (; s + 3 < s1; s += 4)
         {
-            // cells (ax, ay, az0..az1) are adjacent in the cell order, so
-            // their particles form one contiguous span of `spos`
-            const int32_t c0 = (ax * g.n.y + ay) * g.n.z;
-            const int32_t s0 = cellStart[c0 + az0], s1 = cellStart[c0 + az1 + 1];
-            if (!MRMD_IN_BOUNDS(s0, nPos + 1) || !MRMD_IN_BOUNDS(s1, nPos + 1)) continue;
-            // four candidates loaded per iteration: the loop is bound by the
-            // latency of these loads, not by the arithmetic
-            int32_t s = s0;
-            for (; s + 3 < s1; s += 4)
-            {
-                const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
-                candidate(q0);
-                candidate(q1);
-                candidate(q2);
-                candidate(q3);
-            }
-            for (; s < s1; ++s) candidate(spos[s]);
+            const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
+            candidate(q0);
+            candidate(q1);
+            candidate(q2);
+            candidate(q3);
         }
-    }
+        for (; s < s1; ++s) candidate(spos[s]);
+    });
 }
 
 // Particles binned by cell: sorted[] holds particle ids in cell order
@@ -144,12 +161,21 @@ struct TileList;
 // Full list split by distance at build time: pairs closer than rnear (FP32
 // distance) in nearList, the rest within rlist in farList; the cell list of
 // nearList is used.  Each pair appears in exactly one of the two lists.
-// With `tiles` (begin = 0), the lists' tile form (lj_tile.cuh) is built
-// right after them, before the one synchronisation of the build.
+// With `tiles` (begin = 0), the lists are built in their tile form
+// (lj_tile.cuh) only, in one pass (tile_list_launch); when a tile does not
+// fit that pass, the int32 rows are built and their tile form made from them.
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
                      int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid,
                      TileList* tiles = nullptr);
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl);
+// The tile form of the split full list over rows [0, rows) built in one
+// pass from the cell list `cl` (tile_list.cu), without the int32 rows: the
+// near/far counts and tl's members and chunks.  flags as build_split_list's;
+// flags[4] != 0 when a tile did not fit its tables (the caller then builds
+// the int32 rows and their tile form).
+int tile_list_launch(mrmd_ctx* ctx, TileList* tl, int64_t rows, int64_t nPos, const CellList& cl, double rsq, float rsqLo, float rsqHi, float nearSqF, mrmd_nlist* nearList,
+                     mrmd_nlist* farList, const double* pos4, int32_t* flags);
+
 // MRMD_ERR_ARG unless the list's rows [begin, begin + rows) are particles
 // below numLocal and every neighbour index it can hold (the candidates it
 // was built over) is below nAll.

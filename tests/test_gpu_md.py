@@ -133,15 +133,7 @@ def test_mixed_cutoff_decision_at_scale(M):
     assert mix.stats()["pairs"] > 1.9 * ref.stats()["pairs"]
 
 
-def nve_drift_per_1000tau(rec, n, dt=0.005):
-    """Slope of a least-squares line through (E_pot + E_kin) / N of every
-    step, in epsilon per atom per 1000 tau."""
-    e = (rec[:, 0] + rec[:, 2]) / n
-    t = np.arange(len(e)) * dt
-    return float(np.polyfit(t, e, 1)[0]) * 1000.0
-
-
-def test_mixed_vs_fp64_forces_and_drift(M):
+def test_mixed_vs_fp64_forces(M):
     pos, L = fcc(8)  # 2048 atoms
     vel = mb_velocities(len(pos), 0.728, 3)
     ref = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64)
@@ -159,19 +151,27 @@ def test_mixed_vs_fp64_forces_and_drift(M):
     err = np.linalg.norm(fm - fr, axis=1).max() / rms
     assert err < 1e-6, err
     assert per_atom_rel_err(fm, fr, 0.1) < 1e-6
-    # NVE energy drift over 100 tau (20,000 steps) of both forms from the same
-    # equilibrated state, from the device-summed per-step energies.  Limit:
-    # 5e-4 epsilon per atom per 1000 tau for each form, and the mixed form's
-    # drift within 5e-4 of the FP64 form's (the drift of this protocol comes
-    # from the force jump at rc and the fixed rebuild interval, not from the
-    # pair arithmetic)
-    n = len(pos)
-    drift = {}
-    for name, prec in (("fp64", M.PREC_FP64), ("mixed", M.PREC_MIXED)):
-        s = M.LJSystem(p, v, [0, 0, 0], [L] * 3, precision=prec, observe=True)
-        drift[name] = nve_drift_per_1000tau(s.run_observed(20000), n)
-    assert abs(drift["fp64"]) <= 5e-4 and abs(drift["mixed"]) <= 5e-4, drift
-    assert abs(drift["mixed"] - drift["fp64"]) <= 5e-4, drift
+
+
+def test_nve_drift_both_forms(M):
+    """NVE energy drift of both forms: the slope of a least-squares line
+    through (E_pot + E_kin) / N of every step, from the device-summed per-step
+    energies, in epsilon per atom per 1000 tau.  Protocol of the benchmark's
+    drift figure at a fifth of its length: 32,000 atoms (fcc 20^3, rho
+    0.8442), 2,000 FP64 steps from the lattice at T 0.728, then 40,000 steps
+    (200 tau) of each form from that state, for velocity seeds 7, 8 and 9.
+    The energy of this protocol is a random walk (kicks from the force jump at
+    rc), so a slope fitted over 200 tau scatters by ~1.5e-4 between seeds
+    (sd of the mean of three ~0.9e-4); the means measured on a GB300 are
+    ~1e-4 for both forms.  Limits: |mean| <= 5e-4 for each form, and the
+    mixed mean within 5e-4 of the FP64 mean."""
+    import bench
+
+    ctx = M.default_context()
+    r = bench.nve_drift(M, ctx, ["fp64", "mixed"], cells=20, equil=2000, steps=40000, seeds=(7, 8, 9))
+    d64, dmx = r["fp64"]["drift"], r["mixed"]["drift"]
+    assert abs(d64) <= 5e-4 and abs(dmx) <= 5e-4, r
+    assert abs(dmx - d64) <= 5e-4, r
 
 
 @pytest.mark.parametrize("split_radius,bound", [(0.0, 1e-6), (1.8, 5e-7), (2.8, 5e-8)])
