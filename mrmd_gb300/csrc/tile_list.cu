@@ -2,13 +2,15 @@
 // pass from the cell list, without the int32 rows.
 //
 // One block per tile of TILE_ROWS rows, one thread per row.
-// - Span table.  The columns (ax, ay) of the stencils of the tile's cells, cut
-//   into z blocks of ZB cells, each entry with the hull of the z ranges the
-//   tile's cells ask of it, in a shared hash table.  An entry's hull is one
-//   contiguous span of the cell-sorted particles; numbering the spans one
-//   after another gives every candidate of the tile a position (slot = s +
-//   delta of its entry).  The z blocks keep two far-apart parts of a tile (a
-//   tile across a high Z-order boundary) in separate entries.
+// - Span table.  One entry per column (ax, ay) of the stencils of the tile's
+//   cells and z block (16 cells) of the asking cell, with the hull of the z
+//   ranges those cells ask of the column, in a shared hash table.  An entry's
+//   hull (at most 20 cells) is one contiguous span of the cell-sorted
+//   particles; numbering the spans one after another gives every candidate
+//   of the tile a position (slot = s + delta of its entry).  The z blocks keep
+//   two far-apart parts of a tile (a tile across a high Z-order boundary) in
+//   separate entries; a particle in the overlap of two entries of a column
+//   can become two members, each row using the one of its own entry.
 // - Scan.  Each row walks its stencil (for_each_span) with the list builds'
 //   exact FP64 pair decision; a kept neighbour marks its candidate position as
 //   used and is appended to the row's near or far chunks as that position
@@ -34,7 +36,7 @@ namespace
 constexpr int COL_BITS = 9;
 constexpr int COL_HT = 1 << COL_BITS;  // span table slots per tile (a sorted tile uses ~100-200)
 constexpr int ZB_BITS = 4;             // z blocks of 16 cells
-constexpr int CAND_CAP = 4096;         // candidate positions per tile (a sorted tile has ~2,000-3,000)
+constexpr int CAND_CAP = 8192;         // candidate positions per tile (a sorted tile has ~2,000-3,500)
 
 __device__ __forceinline__ uint32_t col_hash(int32_t key)
 {
@@ -211,17 +213,16 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_tile_list(
         const int z0 = max(cz - R, 0), z1 = min(cz + R, g.n.z - 1);
         for (int ax = max(cx - R, 0); ax <= min(cx + R, g.n.x - 1); ++ax)
             for (int ay = max(cy - R, 0); ay <= min(cy + R, g.n.y - 1); ++ay)
-                for (int zb = z0 >> ZB_BITS; zb <= z1 >> ZB_BITS; ++zb)
+            {
+                const int h = col_insert(colKey, (ax * g.n.y + ay) * nzb + (cz >> ZB_BITS));
+                if (h < 0)
                 {
-                    const int h = col_insert(colKey, (ax * g.n.y + ay) * nzb + zb);
-                    if (h < 0)
-                    {
-                        badS = 1;
-                        continue;
-                    }
-                    atomicMin(&colLo[h], max(z0, zb << ZB_BITS));
-                    atomicMax(&colHi[h], min(z1, ((zb + 1) << ZB_BITS) - 1));
+                    badS = 1;
+                    continue;
                 }
+                atomicMin(&colLo[h], z0);
+                atomicMax(&colHi[h], z1);
+            }
     }
     __syncthreads();
 
@@ -273,34 +274,28 @@ __global__ void __launch_bounds__(TILE_ROWS, 4) k_tile_list(
         auto candidate = [&](const float4& q, int32_t slot) {
             float d2f;
             if (!candidate_kept<true>(pos, pi, row, xi, yi, zi, q, rsq, rsqLo, rsqHi, nPos, d2f)) return;
-            if ((uint32_t)slot >= (uint32_t)nCand) return;  // unreachable: the span lies in its entries' hulls
+            if ((uint32_t)slot >= (uint32_t)nCand) return;  // unreachable: the span lies in its entry's hull
             used[slot] = __float_as_int(q.w);
             if (d2f >= nearSqF)
                 chunk_push(af, (uint32_t)slot, farChunks, row, chF);
             else
                 chunk_push(an, (uint32_t)slot, nearChunks, row, chN);
         };
-        for_each_span<true>(cellStart, g, ci, nPos,
-                            [&](int ax, int ay, int32_t c0, int z0, int z1, int32_t s0, int32_t s1) {
-            // the span's first z block and, when it reaches into the next
-            // block (from particle sm on), that block's entry
-            const int32_t col = (ax * g.n.y + ay) * nzb;
-            const int zb0 = z0 >> ZB_BITS, zb1 = z1 >> ZB_BITS;
-            const int h0 = col_find(colKey, col + zb0);
-            const int h1 = zb1 != zb0 ? col_find(colKey, col + zb1) : h0;
-            if (h0 < 0 || h1 < 0) return;  // unreachable: the table holds every entry of the row's stencil
-            const int32_t d0 = colDelta[h0], d1 = colDelta[h1];
-            const int32_t sm = zb1 != zb0 ? cellStart[c0 + (zb1 << ZB_BITS)] : s1;
+        const int zbRow = (ci % g.n.z) >> ZB_BITS;
+        for_each_span<true>(cellStart, g, ci, nPos, [&](int ax, int ay, int32_t, int, int, int32_t s0, int32_t s1) {
+            const int h = col_find(colKey, (ax * g.n.y + ay) * nzb + zbRow);
+            if (h < 0) return;  // unreachable: the table holds every entry of the row's stencil
+            const int32_t delta = colDelta[h];
             int32_t s = s0;
             for (; s + 3 < s1; s += 4)
             {
                 const float4 q0 = spos[s], q1 = spos[s + 1], q2 = spos[s + 2], q3 = spos[s + 3];
-                candidate(q0, s + (s < sm ? d0 : d1));
-                candidate(q1, s + 1 + (s + 1 < sm ? d0 : d1));
-                candidate(q2, s + 2 + (s + 2 < sm ? d0 : d1));
-                candidate(q3, s + 3 + (s + 3 < sm ? d0 : d1));
+                candidate(q0, s + delta);
+                candidate(q1, s + 1 + delta);
+                candidate(q2, s + 2 + delta);
+                candidate(q3, s + 3 + delta);
             }
-            for (; s < s1; ++s) candidate(spos[s], s + (s < sm ? d0 : d1));
+            for (; s < s1; ++s) candidate(spos[s], s + delta);
         });
         chunk_flush(an, nearChunks, row, chN);
         chunk_flush(af, farChunks, row, chF);

@@ -2,6 +2,7 @@
 
     python -m mrmd_gb300.profile_run [--cells 40] [--steps 20] [--warmup 5]
                                      [--form mixed|fp64] [--gather] [--kernel-reps 10]
+                                     [--sort 4]
 
 Builds the fcc LJ fluid of the benchmark (cells^3 unit cells, rho 0.8442,
 T 0.728), runs `warmup` steps, then `steps` steps, then launches the pair
@@ -33,6 +34,7 @@ def main() -> None:
     ap.add_argument("--form", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--gather", action="store_true", help="mixed form: gather records instead of tiles")
     ap.add_argument("--kernel-reps", type=int, default=10)
+    ap.add_argument("--sort", type=int, default=4, help="re-sort the atoms at every k-th rebuild")
     args = ap.parse_args()
 
     import torch
@@ -47,7 +49,8 @@ def main() -> None:
     vel = rng.normal(0.0, np.sqrt(0.728), (n, 3))
     vel -= vel.mean(0)
     prec = M.PREC_MIXED if args.form == "mixed" else M.PREC_FP64
-    s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, gather_neighbours=args.gather, ctx=ctx)
+    s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=prec, gather_neighbours=args.gather,
+                   sort_atoms=args.sort, ctx=ctx)
     s.run(args.warmup, energies=False)
 
     def timed(fn):
