@@ -655,6 +655,14 @@ int mrmd_batch_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out10);
  * slots per entry (1 or 32); pairs / (entries * slots) is the fraction of
  * the pair kernel's lanes that evaluate a listed pair. */
 int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3);
+/* The list of the last rebuild of one replica as canonical keys a * 2^32 + b
+ * of unordered pairs of the replica's molecules (a < b, indices in the
+ * replica's input order; ghosts mapped to their source), one key per pair
+ * the force kernel evaluates (per-molecule rows: one per entry; cluster
+ * layout: one per set mask bit), sorted.  keys may be NULL to query *count;
+ * otherwise cap >= *count keys are written.  For tests and diagnostics. */
+int mrmd_batch_pair_keys(mrmd_ctx* ctx, mrmd_batch* b, int64_t replica, int64_t* keys, int64_t cap,
+                         int64_t* count);
 
 /* ------------------------------------------------- differentiation -- */
 /* Gradient of a trajectory loss of one AdResS system (the batched engine with

@@ -1058,6 +1058,18 @@ class BatchSystem:
                 "recoveries", "list_capacity", "ghost_capacity", "flags"]
         return {k: int(v) for k, v in zip(keys, out)}
 
+    def pair_keys(self, replica: int):
+        """Sorted canonical keys a * 2^32 + b (a < b, molecule indices in the
+        replica's input order) of every pair the force kernel evaluates in the
+        current list of one replica."""
+        cnt = C.c_int64()
+        self.ctx.check(self.ctx.lib.mrmd_batch_pair_keys(self.ctx.h, self.h, int(replica), None, 0, C.byref(cnt)),
+                       "batch_pair_keys")
+        keys = np.zeros(max(cnt.value, 1), dtype=np.int64)
+        self.ctx.check(self.ctx.lib.mrmd_batch_pair_keys(self.ctx.h, self.h, int(replica), _ip(keys), len(keys),
+                                                         C.byref(cnt)), "batch_pair_keys")
+        return keys[: cnt.value]
+
     def list_stats(self):
         """The list of the last rebuild: pairs, entries, pair slots per entry and
         the fraction of the pair kernel's lanes that evaluate a listed pair."""

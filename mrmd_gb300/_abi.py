@@ -278,6 +278,7 @@ SIGNATURES = {
     "mrmd_md_nlist": (P(NListS), [_v]),
     "mrmd_md_tile_stats": (_i, [_v, c_int64_p]),
     "mrmd_md_pair_keys": (_i, [_v, _v, c_int64_p, _i64, c_int64_p]),
+    "mrmd_batch_pair_keys": (_i, [_v, _v, _i64, c_int64_p, _i64, c_int64_p]),
 }
 
 _lib = None

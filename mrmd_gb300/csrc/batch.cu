@@ -27,6 +27,7 @@
 //    block per replica.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "adress_impl.cuh"
@@ -2001,6 +2002,94 @@ int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3)
     out3[0] = pairs;
     out3[1] = pairs;
     out3[2] = 1;
+    return MRMD_OK;
+}
+
+int mrmd_batch_pair_keys(mrmd_ctx* ctx, mrmd_batch* b, int64_t replica, int64_t* keys, int64_t cap,
+                         int64_t* count)
+{
+    if (!ctx || !b || !count || replica < 0 || replica >= b->R) return MRMD_ERR_ARG;
+    MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const BDev& B = b->B;
+    const int64_t N = b->N;
+    MRMD_TRY(d2h(ctx, b->hSc, B.sc, sizeof(Scalars)));
+    const int64_t nGhost = b->hSc->numGhost;
+    if (nGhost < 0 || nGhost > B.gCap) return set_error(ctx, MRMD_ERR_STATE, "ghost count outside the capacity");
+    std::vector<int32_t> orig((size_t)N), slotRep((size_t)N), gSrc((size_t)std::max<int64_t>(nGhost, 1));
+    MRMD_TRY(d2h(ctx, orig.data(), B.orig, sizeof(int32_t) * (size_t)N));
+    MRMD_TRY(d2h(ctx, slotRep.data(), B.slotRep, sizeof(int32_t) * (size_t)N));
+    if (nGhost > 0) MRMD_TRY(d2h(ctx, gSrc.data(), B.gSrc, sizeof(int32_t) * (size_t)nGhost));
+    const int64_t off = b->offsets[(size_t)replica];
+    std::vector<int64_t> out;
+    bool bad = false;
+    // slot j (a ghost maps to its source) -> key of the unordered pair with local i
+    auto add = [&](int64_t i, int64_t j) {
+        if (j >= N) j = j - N < nGhost ? gSrc[(size_t)(j - N)] : -1;
+        if (j < 0 || j >= N)
+        {
+            bad = true;
+            return;
+        }
+        const int64_t a = orig[(size_t)i] - off, c = orig[(size_t)j] - off;
+        out.push_back(std::min(a, c) * (int64_t(1) << 32) + std::max(a, c));
+    };
+    if (b->cfg.tuning.listLayout == LAYOUT_CLUSTER)
+    {
+        const int64_t nc = B.numClusters, capC = B.listCapC;
+        std::vector<int2> cl((size_t)std::max<int64_t>(nc, 1));
+        std::vector<int32_t> cnt((size_t)std::max<int64_t>(nc, 1));
+        std::vector<int4> cli((size_t)std::max<int64_t>(nc * capC, 1));
+        std::vector<float4> sp((size_t)(N + nGhost));
+        MRMD_TRY(d2h(ctx, cl.data(), B.clusters, sizeof(int2) * (size_t)nc));
+        MRMD_TRY(d2h(ctx, cnt.data(), B.countsC, sizeof(int32_t) * (size_t)nc));
+        MRMD_TRY(d2h(ctx, cli.data(), B.clist, sizeof(int4) * (size_t)(nc * capC)));
+        MRMD_TRY(d2h(ctx, sp.data(), B.spos, sizeof(float4) * sp.size()));
+        for (int64_t c = 0; c < nc; ++c)
+        {
+            if (cl[(size_t)c].x < 0 || cl[(size_t)c].x >= N || slotRep[(size_t)cl[(size_t)c].x] != replica) continue;
+            for (int32_t e = 0; e < cnt[(size_t)c]; ++e)
+            {
+                const int4 v = cli[(size_t)(c * capC + e)];
+                for (int bit = 0; bit < 32; ++bit)
+                {
+                    if (!(((uint32_t)v.y >> bit) & 1u)) continue;
+                    const int64_t i = cl[(size_t)c].x + (bit >> 2), s = (int64_t)v.x + (bit & (CLUSTER_J - 1));
+                    if (i >= N || s < 0 || s >= N + nGhost)
+                    {
+                        bad = true;
+                        continue;
+                    }
+                    int32_t j;
+                    std::memcpy(&j, &sp[(size_t)s].w, sizeof(j));
+                    add(i, j);
+                }
+            }
+        }
+    }
+    else
+    {
+        const int64_t tiles = div_up(N, 32);
+        for (int w = 0; w < (B.split ? 2 : 1); ++w)
+        {
+            const int64_t lc = w == 0 ? B.listCap : B.listCapF;
+            std::vector<int32_t> cnt((size_t)N), nb((size_t)std::max<int64_t>(tiles * 32 * lc, 1));
+            MRMD_TRY(d2h(ctx, cnt.data(), w == 0 ? B.counts : B.countsF, sizeof(int32_t) * (size_t)N));
+            MRMD_TRY(d2h(ctx, nb.data(), w == 0 ? B.nbrs : B.nbrsF, sizeof(int32_t) * (size_t)(tiles * 32 * lc)));
+            for (int64_t i = 0; i < N; ++i)
+            {
+                if (slotRep[(size_t)i] != replica) continue;
+                for (int64_t k = 0; k < cnt[(size_t)i] && k < lc; ++k)
+                    add(i, nb[(size_t)((i >> 5) * (lc << 5) + (k << 5) + (i & 31))] & 0x7fffffff);
+            }
+        }
+    }
+    if (bad) return set_error(ctx, MRMD_ERR_STATE, "list entry outside the locals and ghosts");
+    std::sort(out.begin(), out.end());
+    *count = (int64_t)out.size();
+    if (!keys) return MRMD_OK;
+    if (cap < (int64_t)out.size()) return set_error(ctx, MRMD_ERR_CAPACITY, "pair key capacity %lld < %lld",
+                                                     (long long)cap, (long long)out.size());
+    std::copy(out.begin(), out.end(), keys);
     return MRMD_OK;
 }
 

@@ -208,6 +208,57 @@ def test_cluster_layout_lists_the_same_pairs(M):
     assert a.list_stats()["pairs"] == b.list_stats()["pairs"]
 
 
+@pytest.mark.parametrize("layout,prec", [(0, "fp64"), (1, "mixed"), (2, "fp64"), (2, "mixed")])
+def test_batch_lists_are_the_oracle_pair_set(M, orc, layout, prec):
+    """Each replica's list of the batch engine (per-molecule rows, near/far
+    rows, 8 x 4 cluster pairs), mapped to unordered pairs of the replica's
+    molecules, against the oracle's half list of the same positions.
+    Replica 0's slab reaches past its box, so no pair is pruned and the two
+    pair sets are equal bit for bit.  Replica 1 has a narrow slab: pairs of two
+    molecules that stay coarse grained until the next rebuild (|x - c| beyond
+    r_at/2 + d_hy + skin + 1e-3, decided in FP32) are left out.  There the list
+    is a subset of the oracle's, holds every pair with a molecule 1e-4 inside
+    that bound, and no pair with both molecules r_list + 1e-4 beyond it.  No
+    pair appears more than twice (the full list's two rows)."""
+    rc, skin, hy = P["rc"], P["skin"], P["hy"]
+    specs = [([20.0, 12.0, 12.0], 16.0, 700, 11), ([44.0, 12.0, 14.0], 6.0, 1300, 12)]
+    reps, pos, vel = [], [], []
+    for box, at, n, seed in specs:
+        reps.append(replica(M, n, box, at, 500 + seed))
+        p_, v_ = random_system(n, box, seed)
+        pos.append(p_)
+        vel.append(v_)
+    precision = M.PREC_MIXED if prec == "mixed" else M.PREC_FP64
+    b = batch(M, reps, np.concatenate(pos), np.concatenate(vel), precision=precision, list_layout=layout,
+              sort_every=1)
+    b.run(1)  # the first step rebuilds at its drifted positions and keeps them
+    state = b.state()[0]
+    off = 0
+    for r, (box, at, n, _) in enumerate(specs):
+        p_ = state[off:off + n]
+        off += n
+        sd = orc.subdomain([0, 0, 0], box, rc + skin)
+        ao = orc.Atoms.from_positions(p_, capacity=8 * n)
+        corr = orc.create_ghosts(ao, sd)
+        co, no = orc.build_half_list(ao.pos, ao.n, 0, ao.numLocal, rc + skin, sd.minGhostCorner,
+                                     sd.maxGhostCorner, 1.0, 256)
+        ko = orc.canonical_pairs(co, no, corr, ao.numLocal)
+        kb_all = b.pair_keys(r)
+        kb, mult = np.unique(kb_all, return_counts=True)
+        assert mult.max() <= 2
+        if r == 0:
+            np.testing.assert_array_equal(kb, ko)
+            continue
+        assert np.isin(kb, ko).all()
+        deep = at / 2 + hy + skin + 1e-3
+        a_, c_ = ko >> 32, ko & 0xffffffff
+        dmin = np.minimum(np.abs(p_[a_, 0] - box[0] / 2), np.abs(p_[c_, 0] - box[0] / 2))
+        inb = np.isin(ko, kb)
+        assert inb[dmin < deep - 1e-4].all()
+        pruned = dmin > deep + rc + skin + 1e-4
+        assert pruned.sum() > 100 and not inb[pruned].any()
+
+
 def test_layout_switch_and_bad_cluster_tuning(M):
     """Switching layouts between runs keeps the trajectory on the FP64 path
     (to rounding), and the cluster layout takes 4 lanes per row only."""
