@@ -526,7 +526,11 @@ int mrmd_md_pair_keys(mrmd_ctx* ctx, mrmd_md* md, int64_t* keys, int64_t cap, in
  * (UpdateMolecules.hpp:24-70), ContributeMoleculeForceToAtoms
  * (ContributeMoleculeForceToAtoms.cpp:23-48), MultiResGhostLayer and
  * ThermodynamicForce sample/apply/update (ThermodynamicForce.cpp:74-96),
- * for single-site molecules; the reference has no driver for this step. */
+ * for single-site molecules; the reference has no driver for this step.
+ * With unit masses (mass NULL or all 1) the step runs on the batched engine
+ * with one replica (mrmd_batch_*: molecule pairs that stay coarse grained
+ * until the next rebuild are left out of its full list, the mixed form
+ * evaluates far pairs in FP32); other masses run the composed actions. */
 typedef struct mrmd_adress mrmd_adress;
 typedef struct {
     double boxMin[3];
@@ -548,6 +552,8 @@ typedef struct {
     double tfBinWidth, tfTargetDensity, tfModulation, tfSmoothingSigma, tfSmoothingRange;
     int64_t tfSampleInterval, tfUpdateInterval;
     int64_t maxNeighbors;
+    int32_t composed;         /* 1: run the composed actions even with unit masses */
+    int32_t reserved0;
 } mrmd_adress_config;
 
 int mrmd_adress_create(mrmd_ctx* ctx, mrmd_adress** out, const mrmd_adress_config* cfg, int64_t n,
@@ -558,7 +564,8 @@ int mrmd_adress_run(mrmd_ctx* ctx, mrmd_adress* s, int64_t nsteps, double* energ
 int mrmd_adress_get_state(mrmd_ctx* ctx, mrmd_adress* s, double* pos3, double* vel3, double* force3);
 int mrmd_adress_get_tf(mrmd_ctx* ctx, mrmd_adress* s, double* force, double* density, int64_t* numBins);
 int mrmd_adress_set_tf(mrmd_ctx* ctx, mrmd_adress* s, const double* force);
-/* [0] steps, [1] rebuilds, [2] molecule list pairs, [3] ghost molecules */
+/* [0] steps, [1] rebuilds, [2] molecule list pairs (half list of the composed
+ * actions; full-list entries of the batched engine), [3] ghost molecules */
 int mrmd_adress_stats(const mrmd_adress* s, int64_t* out4);
 
 /* ------------------------------------------ batched AdResS replicas -- */

@@ -822,7 +822,9 @@ class LJSystem:
 
 
 class AdResSSystem:
-    """Fused AdResS LJ <-> ideal-gas stepper for single-site molecules (mrmd_adress_*)."""
+    """Fused AdResS LJ <-> ideal-gas stepper for single-site molecules (mrmd_adress_*).
+    With unit masses the step runs on the batched engine with one replica;
+    composed=True (or other masses) runs the composed actions instead."""
 
     def __init__(self, pos, vel, box_min, box_max, slab_center, atomistic_diameter,
                  hybrid_diameter, nu=1, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
@@ -830,7 +832,7 @@ class AdResSSystem:
                  rebuild_interval=10, gamma=1.0, temperature=1.0, seed=1234, tf=True,
                  tf_bin_width=1.2, tf_target_density=0.5, tf_modulation=1.0, tf_sigma=2.4,
                  tf_range=3.0, tf_sample_interval=1, tf_update_interval=1000, use_graph=True,
-                 max_neighbors=0, mass=None, ctx: Context | None = None):
+                 max_neighbors=0, mass=None, composed=False, ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -853,6 +855,7 @@ class AdResSSystem:
         c.tfSmoothingSigma, c.tfSmoothingRange = tf_sigma, tf_range
         c.tfSampleInterval, c.tfUpdateInterval = int(tf_sample_interval), int(tf_update_interval)
         c.maxNeighbors = int(max_neighbors)
+        c.composed = int(bool(composed))
         self.cfg = c
         h = C.c_void_p()
         m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())

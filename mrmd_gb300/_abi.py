@@ -109,7 +109,7 @@ class AdResSConfigS(C.Structure):
                 ("tfTargetDensity", C.c_double), ("tfModulation", C.c_double),
                 ("tfSmoothingSigma", C.c_double), ("tfSmoothingRange", C.c_double),
                 ("tfSampleInterval", C.c_int64), ("tfUpdateInterval", C.c_int64),
-                ("maxNeighbors", C.c_int64)]
+                ("maxNeighbors", C.c_int64), ("composed", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class ReplicaS(C.Structure):

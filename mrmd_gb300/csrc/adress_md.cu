@@ -12,9 +12,16 @@
 //   ThermodynamicForce::sample every S steps, ::update every U steps.
 // The steps between rebuilds are captured once per rebuild and replayed as
 // one CUDA graph.
+//
+// With unit masses (single-site molecules of the AdResS workload) the same
+// step runs on the batched engine with one replica instead (batch.cu: full
+// list without the pairs of molecules that stay coarse grained, FP32 far
+// pairs in the mixed form, four launches per step in CUDA graphs); the
+// composed actions above serve other masses.
 #include <cmath>
 #include <vector>
 
+#include "batch_impl.cuh"
 #include "common.cuh"
 #include "lj_mixed.cuh"
 #include "nlist_impl.cuh"
@@ -44,6 +51,8 @@ struct mrmd_adress
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t graphSteps = 0, graphLaunches = 0;
+    mrmd_batch* batch = nullptr;  // unit masses: the batched engine runs the step
+    mrmd_ctx* ctx = nullptr;      // the context the system was created on
 };
 
 namespace
@@ -167,8 +176,62 @@ int mrmd_adress_create(mrmd_ctx* ctx, mrmd_adress** out, const mrmd_adress_confi
     MRMD_CHECK_ARG(!cfg->tfEnabled || (cfg->tfSampleInterval >= 1 && cfg->tfUpdateInterval >= 1), ctx,
                    "bad thermodynamic-force intervals");
     *out = nullptr;
+    bool unitMass = cfg->composed == 0;
+    for (int64_t i = 0; mass && i < n && unitMass; ++i) unitMass = mass[i] == 1.0;
+    if (unitMass)
+    {
+        mrmd_batch_config bc{};
+        bc.rc = cfg->rc;
+        bc.skin = cfg->skin;
+        bc.sigma = cfg->sigma;
+        bc.epsilon = cfg->epsilon;
+        bc.cappingDistance = cfg->cappingDistance;
+        bc.shifted = cfg->shifted;
+        bc.precision = cfg->precision;
+        bc.dt = cfg->dt;
+        bc.hybridDiameter = cfg->hybridDiameter;
+        bc.nu = cfg->nu;
+        bc.gamma = cfg->gamma;
+        bc.temperature = cfg->temperature;
+        bc.tfEnabled = cfg->tfEnabled;
+        bc.tfBinWidth = cfg->tfBinWidth;
+        bc.tfTargetDensity = cfg->tfTargetDensity;
+        bc.tfModulation = cfg->tfModulation;
+        bc.tfSmoothingSigma = cfg->tfSmoothingSigma;
+        bc.tfSmoothingRange = cfg->tfSmoothingRange;
+        bc.tfSampleInterval = cfg->tfSampleInterval;
+        bc.tfUpdateInterval = cfg->tfUpdateInterval;
+        bc.initialMaxNeighbors = cfg->maxNeighbors > 0 ? cfg->maxNeighbors : 0;
+        // cell sort every 5th rebuild; graphs of 5 rebuild intervals
+        bc.tuning.threadsPerRow = 1;
+        bc.tuning.blockSize = 128;
+        bc.tuning.rebuildInterval = cfg->rebuildInterval;
+        bc.tuning.sortEvery = 5;
+        bc.tuning.graphSteps = cfg->useGraph ? 5 * cfg->rebuildInterval : 0;
+        bc.tuning.listLayout = 0;
+        mrmd_replica_desc rd{};
+        rd.numMolecules = n;
+        for (int d = 0; d < 3; ++d)
+        {
+            rd.boxMin[d] = cfg->boxMin[d];
+            rd.boxMax[d] = cfg->boxMax[d];
+            rd.slabCenter[d] = cfg->slabCenter[d];
+        }
+        rd.atomisticDiameter = cfg->atomisticDiameter;
+        rd.seed = cfg->seed;
+        mrmd_batch* b = nullptr;
+        MRMD_TRY(mrmd_batch_create(ctx, &b, &bc, 1, &rd, pos3, vel3));
+        mrmd_adress* s = new mrmd_adress();
+        s->cfg = *cfg;
+        s->n = n;
+        s->batch = b;
+        s->ctx = ctx;
+        *out = s;
+        return MRMD_OK;
+    }
     mrmd_adress* s = new mrmd_adress();
     s->cfg = *cfg;
+    s->ctx = ctx;
     if (s->cfg.maxNeighbors <= 0) s->cfg.maxNeighbors = 64;
     s->n = n;
     const double rlist = cfg->rc + cfg->skin;
@@ -224,6 +287,12 @@ int mrmd_adress_create(mrmd_ctx* ctx, mrmd_adress** out, const mrmd_adress_confi
 int mrmd_adress_destroy(mrmd_ctx* ctx, mrmd_adress* s)
 {
     if (!s) return MRMD_OK;
+    if (s->batch)
+    {
+        const int rc = mrmd_batch_destroy(ctx, s->batch);
+        delete s;
+        return rc;
+    }
     if (ctx) cudaStreamSynchronize(ctx->stream);
     ad_drop_graph(s);
     mrmd_atoms_free(ctx, &s->atoms);
@@ -242,6 +311,7 @@ int mrmd_adress_destroy(mrmd_ctx* ctx, mrmd_adress* s)
 int mrmd_adress_run(mrmd_ctx* ctx, mrmd_adress* s, int64_t nsteps, double* energies)
 {
     if (!ctx || !s || nsteps < 0) return MRMD_ERR_ARG;
+    if (s->batch) return mrmd_batch_run(ctx, s->batch, nsteps, energies);
     if (nsteps == 0) return MRMD_OK;
     if (nsteps + 1 > s->energyCap)
     {
@@ -304,12 +374,22 @@ int mrmd_adress_run(mrmd_ctx* ctx, mrmd_adress* s, int64_t nsteps, double* energ
 int mrmd_adress_get_state(mrmd_ctx* ctx, mrmd_adress* s, double* pos3, double* vel3, double* force3)
 {
     if (!ctx || !s) return MRMD_ERR_ARG;
+    if (s->batch) return mrmd_batch_get_state(ctx, s->batch, pos3, vel3, force3);
     return mrmd_atoms_download(ctx, &s->atoms, s->n, pos3, vel3, force3, nullptr, nullptr, nullptr, nullptr);
 }
 
 int mrmd_adress_get_tf(mrmd_ctx* ctx, mrmd_adress* s, double* force, double* density, int64_t* numBins)
 {
-    if (!ctx || !s || !s->tf) return MRMD_ERR_ARG;
+    if (!ctx || !s) return MRMD_ERR_ARG;
+    if (s->batch)
+    {
+        if (!s->cfg.tfEnabled) return MRMD_ERR_ARG;
+        int64_t offsets[2] = {0, 0};
+        MRMD_TRY(mrmd_batch_get_tf(ctx, s->batch, force, density, offsets));
+        if (numBins) *numBins = offsets[1];
+        return MRMD_OK;
+    }
+    if (!s->tf) return MRMD_ERR_ARG;
     if (numBins) mrmd_tf_shape(s->tf, numBins, nullptr, nullptr);
     if (force) MRMD_TRY(mrmd_tf_get_force(ctx, s->tf, force));
     if (density) MRMD_TRY(mrmd_tf_get_density(ctx, s->tf, density, nullptr));
@@ -318,13 +398,25 @@ int mrmd_adress_get_tf(mrmd_ctx* ctx, mrmd_adress* s, double* force, double* den
 
 int mrmd_adress_set_tf(mrmd_ctx* ctx, mrmd_adress* s, const double* force)
 {
-    if (!ctx || !s || !s->tf || !force) return MRMD_ERR_ARG;
+    if (!ctx || !s || !force) return MRMD_ERR_ARG;
+    if (s->batch) return s->cfg.tfEnabled ? mrmd_batch_set_tf(ctx, s->batch, force) : MRMD_ERR_ARG;
+    if (!s->tf) return MRMD_ERR_ARG;
     return mrmd_tf_set_force(ctx, s->tf, force);
 }
 
 int mrmd_adress_stats(const mrmd_adress* s, int64_t* out4)
 {
     if (!s || !out4) return MRMD_ERR_ARG;
+    if (s->batch)
+    {
+        int64_t b10[10];
+        MRMD_TRY(mrmd_batch_stats(s->ctx, s->batch, b10));
+        out4[0] = b10[0];
+        out4[1] = b10[1];
+        out4[2] = b10[2];
+        out4[3] = b10[3];
+        return MRMD_OK;
+    }
     out4[0] = s->steps;
     out4[1] = s->rebuilds;
     out4[2] = s->list.totalPairs;

@@ -46,7 +46,8 @@ namespace
 {
 // ------------------------------------------------------------------ pre --
 // B(dt/2) A(dt/2) O(dt) A(dt/2) (VelocityVerletLangevinThermostat.hpp:64-113)
-// with noise keyed by (replica seed, step, index inside the replica); on a
+// with noise keyed by (replica seed, step, the molecule's input index inside
+// the replica: the noise follows the molecule through cell sorts); on a
 // rebuild step the molecule is then wrapped into its box by the
 // MultiResRealAtomsExchange rule (MultiResRealAtomsExchange.cpp:23-73).
 template <bool MIXED>
@@ -67,7 +68,7 @@ __global__ void k_b_pre(BDev B, int rebuild)
         kick_fma(v, f, B.dtHalfOverMass);
         drift_fma(x, v, dtHalf);
         double g[3];
-        normal3(R.seed, st, (uint64_t)(i - R.lbase), g);
+        normal3(R.seed, st, (uint64_t)(B.orig[i] - R.lbase), g);
         v.x = fma(B.ouSigma, g[0], v.x * B.ouDamping);
         v.y = fma(B.ouSigma, g[1], v.y * B.ouDamping);
         v.z = fma(B.ouSigma, g[2], v.z * B.ouDamping);

@@ -25,23 +25,25 @@ def system(n, box, seed):
     return random_system(n, box, seed)
 
 
-def gpu_system(M, pos, vel, box, p, precision, graph=True):
+def gpu_system(M, pos, vel, box, p, precision, graph=True, composed=False):
     return M.AdResSSystem(pos, vel, [0, 0, 0], box, [box[0] / 2, box[1] / 2, box[2] / 2], p["at"], p["hy"],
                           p["nu"], rc=p["rc"], skin=p["skin"], sigma=p["sigma"], epsilon=p["epsilon"],
                           capping_distance=p["cap"], precision=precision, dt=p["dt"], rebuild_interval=p["K"],
                           gamma=p["gamma"], temperature=p["T"], seed=p["seed"], tf=True, tf_bin_width=p["binw"],
                           tf_target_density=p["rho"], tf_modulation=p["mod"], tf_sigma=p["tfs"],
                           tf_range=p["tfr"], tf_sample_interval=p["S"], tf_update_interval=p["U"],
-                          use_graph=graph)
+                          use_graph=graph, composed=composed)
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_adress_trajectory_matches_oracle(M, orc, graph):
+@pytest.mark.parametrize("graph,composed", [(False, False), (True, False), (False, True), (True, True)])
+def test_adress_trajectory_matches_oracle(M, orc, graph, composed):
+    """Both engines of the stepper (the batched engine with one replica, the
+    default for unit masses, and the composed actions) against the oracle."""
     box = [36.0, 10.0, 10.0]
     pos, vel = system(1800, box, 5)
     steps = 13
     po, vo, eo, fo, _ = oracle_loop(orc, pos, vel, box, steps, P)
-    s = gpu_system(M, pos, vel, box, P, M.PREC_FP64, graph)
+    s = gpu_system(M, pos, vel, box, P, M.PREC_FP64, graph, composed)
     eg = s.run(steps)
     pg, vg, _ = s.state()
     # Langevin noise and the Slab weights go through exp/log/cos/sin, which may
@@ -55,11 +57,12 @@ def test_adress_trajectory_matches_oracle(M, orc, graph):
     assert st["steps"] == steps and st["rebuilds"] == 3 and st["ghost_molecules"] > 0
 
 
-def test_adress_mixed_close_to_fp64(M):
+@pytest.mark.parametrize("composed", [False, True])
+def test_adress_mixed_close_to_fp64(M, composed):
     box = [36.0, 10.0, 10.0]
     pos, vel = system(1800, box, 6)
-    a = gpu_system(M, pos, vel, box, P, M.PREC_FP64)
-    b = gpu_system(M, pos, vel, box, P, M.PREC_MIXED)
+    a = gpu_system(M, pos, vel, box, P, M.PREC_FP64, composed=composed)
+    b = gpu_system(M, pos, vel, box, P, M.PREC_MIXED, composed=composed)
     ea = a.run(6)
     eb = b.run(6)
     pa, va, _ = a.state()
