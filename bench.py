@@ -18,6 +18,7 @@ only: the hot path has no exchange step) and rank 0 prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -75,9 +76,13 @@ def load_traffic(kernel):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms in the
+    background.  The sampler is running (its first line written) before the
+    `with` body starts; time_run() marks the timed window and summary() keeps
+    the samples inside it (the nearest one when the window is shorter than
+    the sampling interval)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -85,6 +90,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = None
+        self.window = None
 
     def __enter__(self):
         try:
@@ -92,11 +98,17 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
+
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -109,26 +121,31 @@ class ClockSampler:
     def summary(self):
         if self.proc is None or not self.path or not os.path.exists(self.path):
             return None
-        sm, mx, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
                 c = [x.strip() for x in line.split(",")]
-                if len(c) < 9:
+                if len(c) < 10:
                     continue
                 try:
-                    sm.append(float(c[1]))
-                    mx.append(float(c[2]))
+                    ts = datetime.datetime.strptime(c[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    rows.append((ts, float(c[2]), float(c[3]),
+                                 {n for n, v in zip(names, c[6:10]) if v.lower().startswith("active")}))
                 except ValueError:
                     continue
-                for name, val in zip(names, c[5:9]):
-                    if val.lower().startswith("active"):
-                        reasons.add(name)
         os.unlink(self.path)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
-                "samples": len(sm), "reasons": sorted(reasons)}
+        inside = rows
+        if self.window is not None:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 <= r[0] <= t1]
+            if not inside:
+                inside = [min(rows, key=lambda r: abs(r[0] - 0.5 * (t0 + t1)))]
+        reasons = set().union(*(r[3] for r in inside))
+        return {"sm_mhz": float(np.median([r[1] for r in inside])), "sm_max_mhz": float(max(r[2] for r in inside)),
+                "samples": len(inside), "reasons": sorted(reasons)}
 
 
 def run_cpu(pos, vel, L, steps, warmup, budget_s, threads):
@@ -243,18 +260,24 @@ def replica_throughput(units_per_rank, steps, world, seconds):
     return units_per_rank * steps * world / seconds
 
 
-def time_run(torch, M, sysm, steps, stream):
+def time_run(torch, M, sysm, steps, stream, clk=None):
+    """CUDA-event time of `steps` steps on the stepper's stream (ms), wall
+    time (s), energies and kernel launches; clk (a running ClockSampler)
+    gets the timed window."""
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     sysm.ctx.sync()
     l0 = sysm.ctx.launches
+    w0 = time.time()
     t0 = time.perf_counter()
     ev0.record(stream)
     e = sysm.run(steps)
     ev1.record(stream)
     ev1.synchronize()
     wall = time.perf_counter() - t0
+    if clk is not None:
+        clk.mark(w0, time.time())
     return ev0.elapsed_time(ev1), wall, e, sysm.ctx.launches - l0
 
 
@@ -296,30 +319,32 @@ def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005, seeds
                     drift_per_seed=per[f], fluct=float(np.mean(fluct[f]))) for f in forms}
 
 
-def adress_batch_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
-    """The AdResS workload (scaled to `molecules` at density 0.5) on the batched
-    engine with one replica, both forms: ms per step, atom-steps/s and the
-    force error of the mixed form against FP64 on the first step's identical
-    positions."""
+def adress_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
+    """The AdResS workload (scaled to `molecules` at density 0.5) through the
+    drop-in stepper (AdResSSystem, mrmd_adress_*: the batched engine with one
+    replica for these unit-mass molecules), both forms: ms per step,
+    atom-steps/s and the force error of the mixed form against FP64 on the
+    first step's identical positions."""
     c = adress_config(molecules)
     pos, vel = adress_initial(100, c)
     n = len(pos)
     out, forces = {}, {}
     for form in forms:
         prec = M.PREC_MIXED if form == "mixed" else M.PREC_FP64
-        rep = M.Replica(n, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], 1234)
-        b = M.BatchSystem([rep], pos, vel, hybrid_diameter=c["hy"], nu=c["nu"], rc=c["rc"], skin=c["skin"],
-                          capping_distance=c["cap"], precision=prec, dt=c["dt"], gamma=c["gamma"],
-                          temperature=c["T"], tf=True, tf_bin_width=c["binw"], tf_target_density=c["rho"],
-                          tf_modulation=c["mod"], tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
-                          tf_update_interval=c["U"], rebuild_interval=c["K"], sort_every=5, graph_steps=50, ctx=ctx)
+        b = M.AdResSSystem(pos, vel, [0, 0, 0], list(c["box"]), list(c["center"]), c["at"], c["hy"], c["nu"],
+                           rc=c["rc"], skin=c["skin"], capping_distance=c["cap"], precision=prec, dt=c["dt"],
+                           rebuild_interval=c["K"], gamma=c["gamma"], temperature=c["T"], seed=1234, tf=True,
+                           tf_bin_width=c["binw"], tf_target_density=c["rho"], tf_modulation=c["mod"],
+                           tf_sigma=c["tfs"], tf_range=c["tfr"], tf_sample_interval=c["S"],
+                           tf_update_interval=c["U"], ctx=ctx)
         b.run(1, energies=False)
         forces[form] = b.state()[2]
         b.run(warmup - 1, energies=False)
         ms, wall, e, launches = time_run(torch, M, b, steps, stream)
         out[form] = {"ms_per_step": ms / steps, "atom_steps_per_s": n * steps / (ms * 1e-3)}
         b.close()
-    res = {"molecules": n, "forms": out, "engine": "batched engine, one replica, CUDA graphs of 50 steps"}
+    res = {"molecules": n, "forms": out,
+           "engine": "AdResSSystem (mrmd_adress_*): batched engine with one replica, CUDA graphs of 50 steps"}
     if {"fp64", "mixed"} <= out.keys():
         res["mixed_over_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
         fa, fb = forces["fp64"], forces["mixed"]
@@ -463,7 +488,7 @@ def adress_main(args, rank, world, local_rank):
                            tf_update_interval=c["U"], ctx=ctx)
         s.run(args.warmup)
         with ClockSampler(local_rank) as clk:
-            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream)
+            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream, clk)
         res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
                          stats=s.stats())
         s.close()
@@ -480,7 +505,7 @@ def adress_main(args, rank, world, local_rank):
         forces[form] = b.state()[2]
         b.run(max(args.warmup, 50) - 1, energies=False)
         with ClockSampler(local_rank) as clk:
-            ms, wall, e, launches = time_run(torch, M, b, args.steps, stream)
+            ms, wall, e, launches = time_run(torch, M, b, args.steps, stream, clk)
         st = b.stats()
         res[form + "_batch_engine"] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches,
                                            clocks=clk.summary(), stats={"pairs": st["pairs"],
@@ -573,7 +598,7 @@ def batch_main(args, rank, world, local_rank):
         tuned, trials = (s.tuning, []) if args.no_autotune else s.autotune(trial_steps=BATCH["graph"])
         s.run(args.warmup)
         with ClockSampler(local_rank) as clk:
-            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream)
+            ms, wall, e, launches = time_run(torch, M, s, args.steps, stream, clk)
         res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),
                          stats=s.stats(), lstats=s.list_stats(), tuning=tuned,
                          trials=[dict(t, ms_per_step=m) for t, m in trials])
@@ -813,7 +838,7 @@ def precision_main(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--workload", choices=["lj", "adress", "batch", "diff", "precision"], default="lj")
@@ -882,7 +907,7 @@ def main():
         sysm.run(args.warmup, energies=False)
         barrier()
         with ClockSampler(local_rank) as clk:
-            ms, wall, e, launches = time_run(torch, M, sysm, args.steps, stream)
+            ms, wall, e, launches = time_run(torch, M, sysm, args.steps, stream, clk)
         ms = max_over_ranks(ms, dist, "cuda")
         res[form] = dict(ms=ms, wall=wall, launches=launches,
                          value=replica_throughput(n, args.steps, world, ms * 1e-3),
@@ -923,8 +948,8 @@ def main():
     adress = None
     if rank == 0 and world == 1 and not args.no_adress:
         adress = {"workload": ADRESS_WORKLOAD,
-                  "34560": adress_batch_leg(M, ctx, torch, stream, None, list(res)),
-                  "4000000": adress_batch_leg(M, ctx, torch, stream, 4_000_000, list(res))}
+                  "34560": adress_leg(M, ctx, torch, stream, None, list(res)),
+                  "4000000": adress_leg(M, ctx, torch, stream, 4_000_000, list(res))}
 
     nbar = st["pairs"] / n
     # Algorithmic bytes of the pair force per atom: the half-list FP64 layout,
