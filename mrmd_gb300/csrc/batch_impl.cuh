@@ -188,21 +188,8 @@ __device__ __forceinline__ void set_coord(double4& p, int d, double v)
         p.z = v;
 }
 
-// velocity-Verlet kick and drift with fused multiply-adds (the reference's
-// v += dt/2m F and x += dt v, each rounded once)
-__device__ __forceinline__ void kick_fma(double4& v, const double4& f, double dtfm)
-{
-    v.x = fma(dtfm, f.x, v.x);
-    v.y = fma(dtfm, f.y, v.y);
-    v.z = fma(dtfm, f.z, v.z);
-}
-
-__device__ __forceinline__ void drift_fma(double4& x, const double4& v, double dt)
-{
-    x.x = fma(dt, v.x, x.x);
-    x.y = fma(dt, v.y, x.y);
-    x.z = fma(dt, v.z, x.z);
-}
+// velocity-Verlet kick and drift: kick_fma / drift_fma (integrate_impl.cuh),
+// the reference's v += dt/2m F and x += dt v, each rounded once
 
 // lambda, modulated lambda and grad lambda (x) of one slot, plus the mixed
 // form's split coordinates (UpdateMolecules.hpp:39-69 for a single site).

@@ -25,6 +25,21 @@ __device__ __forceinline__ void drift(double4& x, const double4& v, double dt)
     x.z = __dadd_rn(x.z, __dmul_rn(dt, v.z));
 }
 
+// The same updates with one rounding each (fused multiply-add).
+__device__ __forceinline__ void kick_fma(double4& v, const double4& f, double dtfm)
+{
+    v.x = __fma_rn(dtfm, f.x, v.x);
+    v.y = __fma_rn(dtfm, f.y, v.y);
+    v.z = __fma_rn(dtfm, f.z, v.z);
+}
+
+__device__ __forceinline__ void drift_fma(double4& x, const double4& v, double dt)
+{
+    x.x = __fma_rn(dt, v.x, x.x);
+    x.y = __fma_rn(dt, v.y, x.y);
+    x.z = __fma_rn(dt, v.z, x.z);
+}
+
 // util::dot3 of (x0 - x)   (VelocityVerlet.cpp:55-59)
 __device__ __forceinline__ double disp_sqr(const double4& x0, const double4& x)
 {

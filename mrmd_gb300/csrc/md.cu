@@ -73,14 +73,31 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
         double4 v = vel[i], x = pos[i];
         const double4 f = force[i];
         const double dtfm = dtfmOf[i];
-        if (postKick) kick(v, f, dtfm);  // VelocityVerlet::postForceIntegrate of the previous step
-        if (OBS) observe_add(o, v, mass[i]);
-        kick(v, f, dtfm);                // preForceIntegrate
-        drift(x, v, dt);
+        if (SPLIT)
+        {
+            // mixed form: each update rounded once (fused multiply-add); the
+            // kernel is bound by GB300's FP64 pipe, and the split below
+            // needs it too
+            if (postKick) kick_fma(v, f, dtfm);
+            if (OBS) observe_add(o, v, mass[i]);
+            kick_fma(v, f, dtfm);
+            drift_fma(x, v, dt);
+        }
+        else
+        {
+            if (postKick) kick(v, f, dtfm);  // VelocityVerlet::postForceIntegrate of the previous step
+            if (OBS) observe_add(o, v, mass[i]);
+            kick(v, f, dtfm);                // preForceIntegrate
+            drift(x, v, dt);
+        }
         pos[i] = x;
         vel[i] = v;
-        force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-        if (SPLIT) split_store(x, sp, recA, recB, i);
+        // the mixed form's pair kernel overwrites every local force (no
+        // accumulation, ghosts unused): only the FP64 form needs the reset
+        if (SPLIT)
+            split_store(x, sp, recA, recB, i);
+        else
+            force[i] = make_double4(0.0, 0.0, 0.0, 0.0);
     }
     if (OBS) grid_sum<4>(o, partial, ticket, rec + 2);
 }
@@ -306,7 +323,9 @@ int md_forces(mrmd_ctx* ctx, mrmd_md* md, double* ev, bool splitDone = false)
 
 // Kick / drift / force reset of one step; prevRec (may be null) receives the
 // observables of the previous step when the stepper records them.
-// split: also write the split coordinates of the new local positions.
+// split (mixed form, steps without rebuild): write the split coordinates of
+// the new local positions instead of resetting the forces, which the tile
+// pair kernel overwrites.
 int md_kick_drift(mrmd_ctx* ctx, mrmd_md* md, bool postKick, double* prevRec, bool split = false)
 {
     mrmd_atoms* a = &md->atoms;
