@@ -596,7 +596,9 @@ def batch_main(args, rank, world, local_rank):
         forces[form] = s.state()[2]
         s.run(BATCH["graph"] - 1)
         tuned, trials = (s.tuning, []) if args.no_autotune else s.autotune(trial_steps=BATCH["graph"])
-        s.run(args.warmup)
+        # the random start relaxes over the first few hundred steps; its list
+        # rows grow meanwhile (capacity recoveries replay whole graphs)
+        s.run(max(args.warmup, 300))
         with ClockSampler(local_rank) as clk:
             ms, wall, e, launches = time_run(torch, M, s, args.steps, stream, clk)
         res[form] = dict(ms=ms, value=n * args.steps / (ms * 1e-3), launches=launches, clocks=clk.summary(),

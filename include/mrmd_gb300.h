@@ -603,7 +603,11 @@ typedef struct {
                                  threadsPerRow 4 (mixed form: pairs beyond 1.4 sigma in
                                  FP32); its clusters are compact only for molecules in
                                  cell order (sortEvery > 0, or given in cell order) */
-    int32_t reserved0;
+    int32_t persistent;       /* 1: inside CUDA graphs, the steps between two rebuilds run
+                                 as one persistent cooperative launch (its phases
+                                 separated by grid barriers with a time limit; a barrier
+                                 that times out makes mrmd_batch_run return
+                                 MRMD_ERR_TIMEOUT) */
 } mrmd_batch_tuning;
 
 typedef struct {
@@ -644,8 +648,9 @@ int mrmd_batch_set_compensation(mrmd_ctx* ctx, mrmd_batch* b, const double* mean
 int mrmd_batch_get_tuning(const mrmd_batch* b, mrmd_batch_tuning* t);
 int mrmd_batch_set_tuning(mrmd_ctx* ctx, mrmd_batch* b, const mrmd_batch_tuning* t);
 /* Time each candidate tuning (list layout, lanes per row, block size, rebuild
- * interval) on trialSteps steps from the current state (restored after every trial)
- * and set the fastest.  A rebuild interval longer than the configured one is
+ * interval; then the fastest of those with the persistent step kernel, when
+ * the tuning has CUDA graphs) on trialSteps steps from the current state
+ * (restored after every trial) and set the fastest.  A rebuild interval longer than the configured one is
  * accepted only if no molecule moved skin/2 away from its position at the
  * last rebuild during the trial.  msPerStep (may be NULL) receives
  * [numCandidates] timings (negative = rejected), candidates (may be NULL) the
@@ -670,6 +675,11 @@ int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3);
  * otherwise cap >= *count keys are written.  For tests and diagnostics. */
 int mrmd_batch_pair_keys(mrmd_ctx* ctx, mrmd_batch* b, int64_t replica, int64_t* keys, int64_t cap,
                          int64_t* count);
+/* The grid barrier of the persistent step kernel on its own: `rounds`
+ * barriers of one cooperative launch; block skipBlock (>= 0) never arrives,
+ * so the others give up after limitMs and the call returns MRMD_ERR_TIMEOUT
+ * (-1: every block arrives, MRMD_OK).  For tests of the time limit. */
+int mrmd_grid_sync_selftest(mrmd_ctx* ctx, int32_t rounds, int32_t skipBlock, double limitMs);
 
 /* ------------------------------------------------- differentiation -- */
 /* Gradient of a trajectory loss of one AdResS system (the batched engine with

@@ -926,7 +926,7 @@ class Replica:
 def _tuning_dict(t):
     return dict(threads_per_row=int(t.threadsPerRow), block_size=int(t.blockSize),
                 rebuild_interval=int(t.rebuildInterval), sort_every=int(t.sortEvery),
-                graph_steps=int(t.graphSteps), list_layout=int(t.listLayout))
+                graph_steps=int(t.graphSteps), list_layout=int(t.listLayout), persistent=int(t.persistent))
 
 
 def _tuning_struct(d):
@@ -937,7 +937,15 @@ def _tuning_struct(d):
     t.sortEvery = int(d["sort_every"])
     t.graphSteps = int(d["graph_steps"])
     t.listLayout = int(d.get("list_layout", 0))
+    t.persistent = int(d.get("persistent", 0))
     return t
+
+
+def grid_sync_selftest(rounds=100, skip_block=-1, limit_ms=50.0, ctx: Context | None = None):
+    """The persistent step kernel's grid barrier on its own (mrmd_grid_sync_selftest):
+    returns the status, MRMD_ERR_TIMEOUT when a block never arrived (skip_block >= 0)."""
+    ctx = ctx or default_context()
+    return int(ctx.lib.mrmd_grid_sync_selftest(ctx.h, int(rounds), int(skip_block), float(limit_ms)))
 
 
 class BatchSystem:
@@ -956,7 +964,8 @@ class BatchSystem:
                  tf_modulation=1.0, tf_sigma=2.4, tf_range=3.0, tf_sample_interval=1,
                  tf_update_interval=1000, comp_sampling_interval=0, comp_update_interval=0, comp_frozen=False,
                  threads_per_row=1, block_size=128, rebuild_interval=10, sort_every=5, graph_steps=50,
-                 list_layout=0, initial_max_neighbors=0, initial_ghost_capacity=0, ctx: Context | None = None):
+                 list_layout=0, initial_max_neighbors=0, initial_ghost_capacity=0, persistent=False,
+                 ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -983,7 +992,8 @@ class BatchSystem:
         c.initialMaxNeighbors, c.initialGhostCapacity = int(initial_max_neighbors), int(initial_ghost_capacity)
         c.tuning = _tuning_struct(dict(threads_per_row=threads_per_row, block_size=block_size,
                                        rebuild_interval=rebuild_interval, sort_every=sort_every,
-                                       graph_steps=graph_steps, list_layout=list_layout))
+                                       graph_steps=graph_steps, list_layout=list_layout,
+                                       persistent=int(bool(persistent))))
         self.cfg = c
         reps = (_abi.ReplicaS * len(self.replicas))(*[r._struct() for r in self.replicas])
         h = C.c_void_p()

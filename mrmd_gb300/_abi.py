@@ -120,7 +120,7 @@ class ReplicaS(C.Structure):
 class BatchTuningS(C.Structure):
     _fields_ = [("threadsPerRow", C.c_int32), ("blockSize", C.c_int32), ("rebuildInterval", C.c_int64),
                 ("sortEvery", C.c_int64), ("graphSteps", C.c_int64), ("listLayout", C.c_int32),
-                ("reserved0", C.c_int32)]
+                ("persistent", C.c_int32)]
 
 
 class BatchConfigS(C.Structure):
@@ -279,6 +279,7 @@ SIGNATURES = {
     "mrmd_md_tile_stats": (_i, [_v, c_int64_p]),
     "mrmd_md_pair_keys": (_i, [_v, _v, c_int64_p, _i64, c_int64_p]),
     "mrmd_batch_pair_keys": (_i, [_v, _v, _i64, c_int64_p, _i64, c_int64_p]),
+    "mrmd_grid_sync_selftest": (_i, [_v, C.c_int32, C.c_int32, C.c_double]),
 }
 
 _lib = None

@@ -50,15 +50,16 @@ namespace
 // the replica: the noise follows the molecule through cell sorts); on a
 // rebuild step the molecule is then wrapped into its box by the
 // MultiResRealAtomsExchange rule (MultiResRealAtomsExchange.cpp:23-73).
+// The body over molecules tid, tid + stride, ... (every thread of the grid
+// calls it: the displacement maximum ends in a warp reduction).
 template <bool MIXED>
-__global__ void k_b_pre(BDev B, int rebuild)
+__device__ __forceinline__ void pre_body(const BDev& B, int rebuild, int64_t tid, int64_t stride)
 {
     const unsigned long long st = B.sc->step;
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (tid < B.R) B.energyRing[(int64_t)B.sc->ringSlot * B.R + tid] = 0.0;
+    for (int64_t r = tid; r < B.R; r += stride) B.energyRing[(int64_t)B.sc->ringSlot * B.R + r] = 0.0;
     float m2 = 0.0f;
     const double dtHalf = 0.5 * B.dt;
-    for (int64_t i = tid; i < B.N; i += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t i = tid; i < B.N; i += stride)
     {
         const RepDev& R = B.reps[B.slotRep[i]];
         double4 x = B.pos[i], v = B.vel[i];
@@ -84,13 +85,13 @@ __global__ void k_b_pre(BDev B, int rebuild)
             float4 h, l;
             slot_derived<MIXED>(B, R, i, x, &h, &l);
             const float dx = (h.x - r0.x) + l.x, dy = (h.y - r0.y) + l.y, dz = (h.z - r0.z) + l.z;
-            m2 = fmaxf(m2, dx * dx + dy * dy + dz * dz);
+            m2 = fmaxf(m2, __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))));
             continue;
         }
         {
             const float dx = (float)(x.x - R.gmn[0]) - r0.x, dy = (float)(x.y - R.gmn[1]) - r0.y,
                         dz = (float)(x.z - R.gmn[2]) - r0.z;
-            m2 = fmaxf(m2, dx * dx + dy * dy + dz * dz);
+            m2 = fmaxf(m2, __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))));
         }
         if (rebuild)
         {
@@ -109,6 +110,12 @@ __global__ void k_b_pre(BDev B, int rebuild)
     }
     for (int o = 16; o > 0; o >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
     if ((threadIdx.x & 31) == 0) mrmd_dev::atomic_max_nonneg(&B.sc->dispStep, (double)m2);
+}
+
+template <bool MIXED>
+__global__ void k_b_pre(BDev B, int rebuild)
+{
+    pre_body<MIXED>(B, rebuild, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // weights and split coordinates of the locals at their current positions
@@ -298,10 +305,10 @@ __global__ void k_b_ghost_write(BDev B)
 
 // ghost position = real position +- L (UpdateGhostAtoms.cpp:31-68)
 template <bool MIXED>
-__global__ void k_b_ghost_update(BDev B)
+__device__ __forceinline__ void ghost_update_body(const BDev& B, int64_t tid, int64_t stride)
 {
     const int32_t n = num_slots(B, 1) - B.N;
-    for (int32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x)
+    for (int64_t g = tid; g < n; g += stride)
     {
         const int32_t i = B.gSrc[g];
         const uint32_t code = B.gShift[g];
@@ -319,6 +326,12 @@ __global__ void k_b_ghost_update(BDev B)
         B.pos[s] = p;
         slot_derived<MIXED>(B, R, s, p);
     }
+}
+
+template <bool MIXED>
+__global__ void k_b_ghost_update(BDev B)
+{
+    ghost_update_body<MIXED>(B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // ------------------------------------------------------------ list build --
@@ -769,17 +782,19 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             if (ownMod <= 0.0 && partMod <= 0.0) return;  // both coarse grained: ideal gas
             const double4 pj = B.pos[j];
             const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const double distSqr = dx * dx + dy * dy + dz * dz;
+            // explicit roundings (the oracle's order): the same bits in every
+            // kernel that inlines this body
+            const double distSqr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             if (distSqr > B.rcSqr) return;
             const bool hyPair = is_hy(ownMod) || is_hy(partMod);
             double ff, e;
             lj_eval_fp64(B.lj, distSqr, ff, e);
             const double weighting = 0.5 * (ownMod + partMod);
             const double ffactor = ff * weighting;
-            dfx += dx * ffactor;
-            dfy += dy * ffactor;
-            dfz += dz * ffactor;
-            energy += e * weighting;
+            dfx = fma(dx, ffactor, dfx);
+            dfy = fma(dy, ffactor, dfy);
+            dfz = fma(dz, ffactor, dfz);
+            energy = fma(e, weighting, energy);
             if (hyPair)
             {
                 const double Vij = 0.5 * e;
@@ -790,7 +805,7 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
                 }
                 else
                 {
-                    imgFx += -Vij * ownGx;
+                    imgFx = fma(-Vij, ownGx, imgFx);
                     if (sampling && is_hy(ownMod))
                     {
                         const int b = comp_bin(ownLam);
@@ -899,13 +914,14 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
 // (ThermodynamicForce.hpp:98-122), density sample (AxialDensityProfile.cpp:
 // 36-47) and the velocity-Verlet post kick (VelocityVerlet.cpp:69-90).
 // CL: one warp per i-cluster, 4 lanes per row (TPR = 4).
+// One thread's share of the force for global thread index gtid (a warp's
+// 32 lanes take 32 consecutive indices, aligned to 32).
 template <bool MIXED, int TPR, bool CL>
-__global__ void k_b_force(BDev B)
+__device__ __forceinline__ void force_body(const BDev& B, int64_t gtid)
 {
     static_assert(!CL || TPR == CLUSTER_J, "the cluster layout has CLUSTER_J lanes per row");
     const bool sampling = B.sc->sampleComp != 0;
     const bool tfSample = B.sc->sampleTf != 0;
-    const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int32_t i = (int32_t)(gtid / TPR);
     const int sub = (int)(gtid % TPR);
     bool valid = i < B.N;
@@ -926,7 +942,7 @@ __global__ void k_b_force(BDev B)
         const RepDev& R = B.reps[r];
         const double4 la = B.lam[i];
         // molecule force: drift (-V_ij grad lambda) and compensation
-        double fmx = -o.vsum * la.z + o.imgFx;
+        double fmx = fma(-o.vsum, la.z, o.imgFx);
         if (MIXED && (o.vImgM != 0.0 || o.vImgP != 0.0))
         {
             // pairs acting through i's images: drift force -V grad lambda of the
@@ -938,7 +954,7 @@ __global__ void k_b_force(BDev B)
                 if (v == 0.0) continue;
                 double l, m, g;
                 image_weights(B, R, i, side, l, m, g);
-                fmx += -v * g;
+                fmx = fma(-v, g, fmx);
                 if (sampling && is_hy(m))
                 {
                     const int b = comp_bin(l);
@@ -953,7 +969,7 @@ __global__ void k_b_force(BDev B)
             const int b = comp_bin(la.x);
             if (b != -1)
             {
-                fmx += B.compMean[r * COMP_BINS + b] * la.z;
+                fmx = fma(B.compMean[r * COMP_BINS + b], la.z, fmx);
                 if (sampling)
                 {
                     atomicAdd(B.compCounter + r * COMP_BINS + b, 1ull);
@@ -1013,6 +1029,14 @@ __global__ void k_b_force(BDev B)
     }
 }
 
+// 80 registers: six blocks of 128 threads per SM (86 registers gave five
+// and an 8% slower step)
+template <bool MIXED, int TPR, bool CL>
+__global__ void __maxnreg__(80) k_b_force(BDev B)
+{
+    force_body<MIXED, TPR, CL>(B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // pairs (mask bits) and cluster pairs of the cluster layout's rows
 __global__ void k_b_cluster_stats(BDev B, unsigned long long* out)
 {
@@ -1027,26 +1051,28 @@ __global__ void k_b_cluster_stats(BDev B, unsigned long long* out)
 }
 
 // ------------------------------------------------------------------ tail --
-// One block per replica: the drift-compensation mean update
-// (LJ_IdealGas.cpp:21-50, 253-255) and the ThermodynamicForce update; the
-// last block advances the step counters and the displacement bookkeeping.
-__global__ void k_b_tail(BDev B, int rebuild)
+// The step decisions the tail reads (thread 0, before the counters advance).
+struct TailShared
 {
-    __shared__ unsigned long long sStep, sRun, sSamples;
-    __shared__ int sCompUpdate, sTfUpdate;
-    if (threadIdx.x == 0)
-    {
-        sStep = B.sc->step;
-        sRun = B.sc->run;
-        sSamples = B.sc->tfSamples + (unsigned long long)(B.sc->sampleTf != 0);  // including this step's sample
-        sCompUpdate = B.compUpdate > 0 && (sRun % (unsigned long long)B.compUpdate) == 0;
-        sTfUpdate = B.tfEnabled && ((sStep + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && sSamples > 0;
-    }
-    __syncthreads();
-    const unsigned long long st = sStep, run = sRun;
-    const int r = blockIdx.x;
+    unsigned long long step, run, samples;
+    int compUpdate, tfUpdate;
+};
+
+__device__ __forceinline__ void tail_read(const BDev& B, TailShared& t)
+{
+    t.step = B.sc->step;
+    t.run = B.sc->run;
+    t.samples = B.sc->tfSamples + (unsigned long long)(B.sc->sampleTf != 0);  // including this step's sample
+    t.compUpdate = B.compUpdate > 0 && (t.run % (unsigned long long)B.compUpdate) == 0;
+    t.tfUpdate = B.tfEnabled && ((t.step + 1) % (unsigned long long)B.tfUpdateInterval) == 0 && t.samples > 0;
+}
+
+// Replica r's drift-compensation mean update (LJ_IdealGas.cpp:21-50, 253-255)
+// and ThermodynamicForce update, by one block.
+__device__ __forceinline__ void tail_replica(const BDev& B, int r, const TailShared& t)
+{
     const RepDev& R = B.reps[r];
-    if (sCompUpdate)
+    if (t.compUpdate)
     {
         for (int k = threadIdx.x; k < COMP_BINS; k += blockDim.x)
         {
@@ -1059,38 +1085,67 @@ __global__ void k_b_tail(BDev B, int rebuild)
             B.compCounter[q] = 0;
         }
     }
-    if (sTfUpdate)
+    if (t.tfUpdate)
     {
-        const unsigned long long samples = sSamples;
+        double* d = B.tfWork + R.tfBase;
+        for (int k = threadIdx.x; k < R.tfBins; k += blockDim.x)
         {
-            double* d = B.tfWork + R.tfBase;
-            for (int k = threadIdx.x; k < R.tfBins; k += blockDim.x)
-            {
-                d[k] = (double)B.tfDensity[R.tfBase + k];
-                B.tfDensity[R.tfBase + k] = 0ull;
-            }
-            __syncthreads();
-            UpdateArgs A{};
-            A.density = d;
-            A.force = B.tfForce + R.tfBase;
-            A.smooth = B.tfWork + B.totalBins + R.tfBase;
-            A.grad = B.tfWork + 2 * (int64_t)B.totalBins + R.tfBase;
-            A.forceFactor = B.tfFF;
-            A.numBins = R.tfBins;
-            A.numTypes = 1;
-            A.binSize = R.tfBinSize;
-            A.inverseBinSize = R.tfInvBin;
-            A.min = R.tfMin;
-            A.normalization = 1.0 / (R.tfBinVolume * (double)samples);
-            A.sigma = B.tfSigma;
-            A.range = B.tfRange;
-            A.enforceSymmetry = 0;
-            A.periodic = 1;
-            A.usePred = 0;
-            tf_update_block(A);
+            d[k] = (double)B.tfDensity[R.tfBase + k];
+            B.tfDensity[R.tfBase + k] = 0ull;
         }
+        __syncthreads();
+        UpdateArgs A{};
+        A.density = d;
+        A.force = B.tfForce + R.tfBase;
+        A.smooth = B.tfWork + B.totalBins + R.tfBase;
+        A.grad = B.tfWork + 2 * (int64_t)B.totalBins + R.tfBase;
+        A.forceFactor = B.tfFF;
+        A.numBins = R.tfBins;
+        A.numTypes = 1;
+        A.binSize = R.tfBinSize;
+        A.inverseBinSize = R.tfInvBin;
+        A.min = R.tfMin;
+        A.normalization = 1.0 / (R.tfBinVolume * (double)t.samples);
+        A.sigma = B.tfSigma;
+        A.range = B.tfRange;
+        A.enforceSymmetry = 0;
+        A.periodic = 1;
+        A.usePred = 0;
+        tf_update_block(A);
     }
-    // last block: counters
+}
+
+// The step counters and the displacement bookkeeping (one thread, after
+// every replica's tail).
+__device__ __forceinline__ void tail_counters(const BDev& B, int rebuild, const TailShared& t)
+{
+    Scalars* s = B.sc;
+    s->tfSamples = t.tfUpdate ? 0ull : t.samples;
+    // on a rebuild step the pre-force displacement is measured against
+    // the previous list, which this step no longer uses
+    if (rebuild)
+    {
+        s->maxDisp = 0.0;
+    }
+    else
+    {
+        const double d = sqrt(s->dispStep);
+        s->maxDisp = fmax(s->maxDisp, d);
+        if (d >= B.halfSkin) s->flags |= FLAG_UNSAFE_INTERVAL;
+    }
+    s->dispStep = 0.0;
+    s->run = t.run + 1;
+    s->step = t.step + 1;
+    set_step_flags(*s, t.step + 1, t.run + 1, B.ring, B.compSampling, B.tfEnabled, B.tfSampleInterval);
+}
+
+// One block per replica; the last block to finish advances the counters.
+__global__ void k_b_tail(BDev B, int rebuild)
+{
+    __shared__ TailShared t;
+    if (threadIdx.x == 0) tail_read(B, t);
+    __syncthreads();
+    tail_replica(B, blockIdx.x, t);
     __syncthreads();
     __threadfence();
     if (threadIdx.x == 0)
@@ -1099,27 +1154,116 @@ __global__ void k_b_tail(BDev B, int rebuild)
         if (ticket == gridDim.x - 1)
         {
             __threadfence();
-            Scalars* s = B.sc;
-            s->tfSamples = sTfUpdate ? 0ull : sSamples;
-            // on a rebuild step the pre-force displacement is measured against
-            // the previous list, which this step no longer uses
-            if (rebuild)
-            {
-                s->maxDisp = 0.0;
-            }
-            else
-            {
-                const double d = sqrt(s->dispStep);
-                s->maxDisp = fmax(s->maxDisp, d);
-                if (d >= B.halfSkin) s->flags |= FLAG_UNSAFE_INTERVAL;
-            }
-            s->dispStep = 0.0;
-            s->run = run + 1;
-            s->step = st + 1;
-            set_step_flags(*s, st + 1, run + 1, B.ring, B.compSampling, B.tfEnabled, B.tfSampleInterval);
-            s->done = 0u;
+            tail_counters(B, rebuild, t);
+            B.sc->done = 0u;
         }
     }
+}
+
+// ------------------------------------------------------ persistent steps --
+// A grid-wide barrier with a wall-clock limit: the blocks of a cooperative
+// launch (all resident) arrive on a counter; the last one resets it and
+// advances the generation the others wait on.  A wait longer than limitNs,
+// or an error raised by another block, ends with `error` set and false
+// returned: the caller returns, and the host reads the error.
+struct GridBar
+{
+    unsigned* count;
+    unsigned* gen;
+    int32_t* error;
+    unsigned long long limitNs;
+};
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// every thread of every block; skip (tests only): this block never arrives
+__device__ bool grid_sync(const GridBar& gb, bool skip = false)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        volatile unsigned* gen = gb.gen;
+        volatile int32_t* err = gb.error;
+        const unsigned g = *gen;
+        __threadfence();
+        bool released = false;
+        if (!skip && atomicAdd(gb.count, 1u) == gridDim.x - 1)
+        {
+            *gb.count = 0u;
+            __threadfence();
+            atomicAdd(gb.gen, 1u);
+            released = true;
+        }
+        bool good = *err == 0;
+        if (!released && good)
+        {
+            const unsigned long long t0 = global_ns();
+            while (*gen == g)
+            {
+                if (*err != 0)
+                {
+                    good = false;
+                    break;
+                }
+                if (global_ns() - t0 > gb.limitNs)
+                {
+                    atomicExch(gb.error, 1);
+                    good = false;
+                    break;
+                }
+                __nanosleep(200);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// `count` steps without rebuild in one cooperative launch: the four phases
+// of step() (pre, ghost update, force, tail) separated by grid barriers,
+// the same arithmetic per molecule, ghost, row and replica.
+template <bool MIXED, int TPR, bool CL>
+__global__ void __maxnreg__(80) k_b_steps(BDev B, int count, GridBar gb)
+{
+    __shared__ TailShared t;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t threads = CL ? (int64_t)B.numClusters * 32 : (int64_t)B.N * TPR;
+    for (int k = 0; k < count; ++k)
+    {
+        pre_body<MIXED>(B, 0, tid, stride);
+        if (!grid_sync(gb)) return;
+        ghost_update_body<MIXED>(B, tid, stride);
+        if (!grid_sync(gb)) return;
+        for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < threads; base += stride)
+            force_body<MIXED, TPR, CL>(B, base + threadIdx.x);
+        if (!grid_sync(gb)) return;
+        if (threadIdx.x == 0) tail_read(B, t);
+        __syncthreads();
+        for (int r = blockIdx.x; r < B.R; r += gridDim.x)
+        {
+            tail_replica(B, r, t);
+            __syncthreads();
+        }
+        if (!grid_sync(gb)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) tail_counters(B, 0, t);
+        if (!grid_sync(gb)) return;
+    }
+}
+
+// `rounds` barriers; block `skipBlock` (>= 0, tests only) never arrives.
+__global__ void k_grid_sync_test(GridBar gb, int rounds, int skipBlock)
+{
+    for (int k = 0; k < rounds; ++k)
+        if (!grid_sync(gb, (int)blockIdx.x == skipBlock)) return;
 }
 }  // namespace
 
@@ -1415,6 +1559,65 @@ int snapshot(mrmd_ctx* ctx, mrmd_batch* b, Snap& sn, bool save)
     return MRMD_OK;
 }
 
+// Wall-clock limit of one grid-barrier wait of the persistent step kernel:
+// far above any phase of a step (milliseconds), short enough to give the
+// GPU back quickly when a block never arrives.
+constexpr unsigned long long SYNC_LIMIT_NS = 2000000000ull;
+
+// A cooperative launch of the kernel with every block resident (blocks per
+// SM from the occupancy calculator), captured like any launch.
+template <typename... A>
+int cooperative_launch(mrmd_ctx* ctx, void (*kernel)(A...), int blockSize, const char* what, A... args)
+{
+    int perSM = 0;
+    MRMD_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, blockSize, 0));
+    if (perSM < 1) return set_error(ctx, MRMD_ERR_CAPACITY, "%s: no block of %d threads fits an SM", what, blockSize);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(perSM * ctx->numSMs));
+    cfg.blockDim = dim3((unsigned)blockSize);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    MRMD_CUDA(ctx, cudaLaunchKernelEx(&cfg, kernel, args...));
+    return after_launch(ctx, what);
+}
+
+template <bool M, int TPR, bool CL = false>
+int persistent_t(mrmd_ctx* ctx, mrmd_batch* b, int count)
+{
+    // a fresh barrier (count, generation); the error word is cleared by the
+    // host before each graph launch and read after it
+    MRMD_CUDA(ctx, cudaMemsetAsync(b->dSync, 0, 2 * sizeof(unsigned), ctx->stream));
+    const GridBar gb{b->dSync, b->dSync + 1, reinterpret_cast<int32_t*>(b->dSync + 2), SYNC_LIMIT_NS};
+    return cooperative_launch(ctx, k_b_steps<M, TPR, CL>, b->cfg.tuning.blockSize, "batch persistent steps", b->B,
+                              count, gb);
+}
+
+template <bool M>
+int persistent_m(mrmd_ctx* ctx, mrmd_batch* b, int count)
+{
+    if (b->cfg.tuning.listLayout == LAYOUT_CLUSTER) return persistent_t<M, CLUSTER_J, true>(ctx, b, count);
+    switch (b->cfg.tuning.threadsPerRow)
+    {
+        case 1: return persistent_t<M, 1>(ctx, b, count);
+        case 2: return persistent_t<M, 2>(ctx, b, count);
+        case 4: return persistent_t<M, 4>(ctx, b, count);
+        case 8: return persistent_t<M, 8>(ctx, b, count);
+        default: return set_error(ctx, MRMD_ERR_ARG, "threadsPerRow must be 1, 2, 4 or 8");
+    }
+}
+
+// `count` steps without rebuild in one persistent launch
+int persistent_steps(mrmd_ctx* ctx, mrmd_batch* b, int count)
+{
+    return b->cfg.precision == MRMD_PREC_MIXED ? persistent_m<true>(ctx, b, count)
+                                               : persistent_m<false>(ctx, b, count);
+}
+
 int capture(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
 {
     drop_graph(b);
@@ -1422,7 +1625,21 @@ int capture(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
     MRMD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t l0 = ctx->launches, r0 = b->rebuilds;
     int rc = MRMD_OK;
-    for (int64_t k = 0; k < P && rc == MRMD_OK; ++k) rc = step(ctx, b, st0 + k, false);
+    if (b->cfg.tuning.persistent)
+    {
+        // each rebuild step on its own, then the steps up to the next rebuild
+        // in one cooperative launch (P is a multiple of the rebuild interval)
+        const int64_t K = b->cfg.tuning.rebuildInterval;
+        for (int64_t k = 0; k < P && rc == MRMD_OK; k += K)
+        {
+            rc = step(ctx, b, st0 + k, false);
+            if (rc == MRMD_OK && K > 1) rc = persistent_steps(ctx, b, (int)(K - 1));
+        }
+    }
+    else
+    {
+        for (int64_t k = 0; k < P && rc == MRMD_OK; ++k) rc = step(ctx, b, st0 + k, false);
+    }
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     b->graphKernels = ctx->launches - l0;
@@ -1459,12 +1676,18 @@ int run_graph(mrmd_ctx* ctx, mrmd_batch* b, int64_t st0)
     {
         if (!b->exec) MRMD_TRY(capture(ctx, b, st0));
         MRMD_CUDA(ctx, cudaMemsetAsync(&B.sc->overflow, 0, sizeof(uint32_t), ctx->stream));
+        MRMD_CUDA(ctx, cudaMemsetAsync(b->dSync + 2, 0, sizeof(unsigned), ctx->stream));
         MRMD_TRY(snapshot(ctx, b, b->sn, true));
         MRMD_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
         ctx->launches += b->graphKernels;
         b->graphLaunches++;
         MRMD_CUDA(ctx, cudaMemcpyAsync(b->hSc, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+        unsigned syncError = 0;
+        MRMD_CUDA(ctx, cudaMemcpyAsync(&syncError, b->dSync + 2, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
         MRMD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (syncError)
+            return set_error(ctx, MRMD_ERR_TIMEOUT, "a grid barrier of the persistent step kernel timed out");
         const uint32_t f = b->hSc->overflow;
         const int64_t P = b->cfg.tuning.graphSteps;
         if (!f)
@@ -1507,6 +1730,7 @@ int validate_tuning(mrmd_ctx* ctx, const mrmd_batch_tuning& t)
     MRMD_CHECK_ARG(t.listLayout >= LAYOUT_ROWS && t.listLayout <= LAYOUT_CLUSTER, ctx, "listLayout must be 0, 1 or 2");
     MRMD_CHECK_ARG(t.listLayout != LAYOUT_CLUSTER || t.threadsPerRow == CLUSTER_J, ctx,
                    "the cluster layout (listLayout 2) takes threadsPerRow 4");
+    MRMD_CHECK_ARG(t.persistent == 0 || t.persistent == 1, ctx, "persistent must be 0 or 1");
     const int64_t period = t.rebuildInterval * (t.sortEvery > 0 ? t.sortEvery : 1);
     MRMD_CHECK_ARG(t.graphSteps == 0 || t.graphSteps % period == 0, ctx,
                    "graphSteps must be a multiple of rebuildInterval * sortEvery");
@@ -1539,7 +1763,7 @@ void free_all(mrmd_batch* b)
                     B.lam, B.lamt, B.lamtf, B.hi, B.lo, B.cellOf, B.cellStart, B.cursor, B.unordered, B.sorted,
                     B.spos, B.counts, B.nbrs, B.countsF, B.nbrsF, B.clusters, B.countsC, B.clist, B.sPos, B.sVel, B.sMass, B.sOrig, B.tfForce,
                     B.tfDensity, B.tfWork, B.compEnergy, B.compCounter, B.compMean, B.energyRing, B.sc,
-                    b->dReps, b->dTfFF};
+                    b->dReps, b->dTfFF, b->dSync};
     for (void* p : ptrs) dfree(p);
     snap_free(b->sn);
     if (b->hSc) cudaFreeHost(b->hSc);
@@ -1725,6 +1949,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
     alloc(B.compCounter, nc);
     alloc(B.compMean, nc);
     alloc(B.sc, 1);
+    alloc(b->dSync, 4);
     alloc(b->dReps, b->R);
     alloc(b->dTfFF, 1);
     {
@@ -2006,6 +2231,23 @@ int mrmd_batch_list_stats(mrmd_ctx* ctx, mrmd_batch* b, int64_t* out3)
     return MRMD_OK;
 }
 
+int mrmd_grid_sync_selftest(mrmd_ctx* ctx, int32_t rounds, int32_t skipBlock, double limitMs)
+{
+    if (!ctx || rounds < 0 || !(limitMs > 0.0)) return MRMD_ERR_ARG;
+    unsigned* d = nullptr;
+    MRMD_TRY(dmalloc(ctx, reinterpret_cast<void**>(&d), 4 * sizeof(unsigned)));
+    int rc = check_cuda(ctx, cudaMemsetAsync(d, 0, 4 * sizeof(unsigned), ctx->stream), "memset");
+    const GridBar gb{d, d + 1, reinterpret_cast<int32_t*>(d + 2), (unsigned long long)(limitMs * 1e6)};
+    if (rc == MRMD_OK)
+        rc = cooperative_launch(ctx, k_grid_sync_test, 128, "grid sync selftest", gb, (int)rounds, (int)skipBlock);
+    unsigned err = 0;
+    if (rc == MRMD_OK) rc = d2h(ctx, &err, d + 2, sizeof(unsigned));
+    cudaStreamSynchronize(ctx->stream);
+    dfree(d);
+    MRMD_TRY(rc);
+    return err ? set_error(ctx, MRMD_ERR_TIMEOUT, "grid barrier wait gave up after %.1f ms", limitMs) : MRMD_OK;
+}
+
 int mrmd_batch_pair_keys(mrmd_ctx* ctx, mrmd_batch* b, int64_t replica, int64_t* keys, int64_t cap,
                          int64_t* count)
 {
@@ -2177,6 +2419,10 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
                     if (t.graphSteps > 0) t.graphSteps = ((t0.graphSteps + period - 1) / period) * period;
                     cand.push_back(t);
                 }
+    // last candidate: the best of the others with the persistent step kernel
+    // (filled in after they ran)
+    if (t0.graphSteps > 0) cand.push_back(t0);
+    const size_t numRegular = t0.graphSteps > 0 ? cand.size() - 1 : cand.size();
     const int oldSync = ctx->sync;
     ctx->sync = 0;
     Snap keep;
@@ -2190,6 +2436,12 @@ int mrmd_batch_autotune(mrmd_ctx* ctx, mrmd_batch* b, int64_t trialSteps, mrmd_b
     int bestIdx = -1;
     for (size_t c = 0; c < cand.size() && rc == MRMD_OK; ++c)
     {
+        if (c == numRegular)
+        {
+            if (bestIdx < 0) break;
+            cand[c] = cand[(size_t)bestIdx];
+            cand[c].persistent = 1;
+        }
         b->cfg.tuning = cand[c];
         rc = apply_layout(ctx, b);
         if (rc != MRMD_OK) break;

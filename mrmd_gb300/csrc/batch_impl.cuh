@@ -257,6 +257,7 @@ struct mrmd_batch
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t graphKernels = 0;
+    unsigned* dSync = nullptr;  // persistent steps: barrier count, generation, error word
     int64_t steps = 0, rebuilds = 0, graphLaunches = 0, recoveries = 0;
     bool needRebuild = true;  // ghosts and list do not match the locals (new tuning, restored state)
 };

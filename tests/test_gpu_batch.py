@@ -259,6 +259,39 @@ def test_batch_lists_are_the_oracle_pair_set(M, orc, layout, prec):
         assert pruned.sum() > 100 and not inb[pruned].any()
 
 
+@pytest.mark.parametrize("prec,layout,tpr", [("fp64", 0, 2), ("mixed", 1, 1), ("mixed", 2, 4)])
+def test_persistent_steps_bitwise_equal(M, prec, layout, tpr):
+    """The steps between rebuilds as one persistent cooperative launch (grid
+    barriers between the phases) against one launch per phase, inside the same
+    CUDA graphs: positions, velocities and forces bitwise equal (every
+    molecule, ghost, row and replica does the same arithmetic), energies to
+    the order of the per-replica atomic sums, the same TF tables."""
+    reps, pos, vel = replica_set(M)
+    precision = M.PREC_MIXED if prec == "mixed" else M.PREC_FP64
+    tune = dict(threads_per_row=tpr, block_size=128, rebuild_interval=5, sort_every=2, graph_steps=10,
+                list_layout=layout)
+    a = batch(M, reps, pos, vel, precision=precision, **tune)
+    b = batch(M, reps, pos, vel, precision=precision, persistent=True, **tune)
+    assert b.tuning["persistent"] == 1 and a.tuning["persistent"] == 0
+    ea = a.run(30)
+    eb = b.run(30)
+    for x, y in zip(a.state(), b.state()):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_allclose(eb, ea, rtol=1e-12, atol=1e-9)
+    for ta, tb in zip(a.thermodynamic_force()[0], b.thermodynamic_force()[0]):
+        np.testing.assert_array_equal(ta, tb)
+    assert b.stats()["steps"] == 30
+
+
+def test_grid_barrier_time_limit(M):
+    """The persistent kernel's grid barrier gives up after its time limit:
+    with one block that never arrives the others stop waiting after 50 ms and
+    the call returns MRMD_ERR_TIMEOUT; the context keeps working."""
+    assert M.grid_sync_selftest(rounds=1000) == 0
+    assert M.grid_sync_selftest(rounds=10, skip_block=0, limit_ms=50.0) == -5
+    assert M.grid_sync_selftest(rounds=1000) == 0
+
+
 def test_layout_switch_and_bad_cluster_tuning(M):
     """Switching layouts between runs keeps the trajectory on the FP64 path
     (to rounding), and the cluster layout takes 4 lanes per row only."""
