@@ -300,6 +300,7 @@ def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005, seeds
     pos, L = fcc(cells)
     per = {f: [] for f in forms}
     fluct = {f: [] for f in forms}
+    mom = {f: [] for f in forms}
     for seed in seeds:
         vel = mb_velocities(len(pos), 0.728, seed)
         eq = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_FP64, ctx=ctx)
@@ -315,8 +316,12 @@ def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005, seeds
             t = np.arange(steps) * dt
             per[form].append(float(np.polyfit(t, et, 1)[0]) * 1000.0)
             fluct[form].append(float(et.std()))
+            # largest component of the velocity sum (the reference's
+            # getSystemMomentum) reached during the run, per atom
+            mom[form].append(float(np.abs(rec[:, 3:6]).max()) / len(p))
     return {f: dict(drift=float(np.mean(per[f])), drift_sd=float(np.std(per[f], ddof=1)) if len(per[f]) > 1 else None,
-                    drift_per_seed=per[f], fluct=float(np.mean(fluct[f]))) for f in forms}
+                    drift_per_seed=per[f], fluct=float(np.mean(fluct[f])), momentum_max=float(np.max(mom[f])))
+            for f in forms}
 
 
 def adress_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
@@ -1016,6 +1021,7 @@ def main():
                                  "nve_drift_sd_over_seeds": drift.get(f, {}).get("drift_sd"),
                                  "nve_drift_per_seed": drift.get(f, {}).get("drift_per_seed"),
                                  "nve_energy_fluctuation_per_atom": drift.get(f, {}).get("fluct"),
+                                 "nve_momentum_max_per_atom": drift.get(f, {}).get("momentum_max"),
                                  "kernel_launches": res[f]["launches"]} for f in res},
                    "tiles": tiles, "adress": adress,
                    "mixed_over_fp64": (res["mixed"]["value"] / res["fp64"]["value"]) if {"mixed", "fp64"} <= res.keys() else None,
