@@ -274,9 +274,11 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
     const double rlist = md->cfg.rc + md->cfg.skin;
     if (full)
     {
-        // near rows: closer than r_split + skin / 2 at the rebuild.  A far pair
-        // that comes within r_split later is still evaluated in double-float
-        // (the pair kernel decides per pair); the margin only keeps that rare.
+        // near rows: closer than r_split + skin / 2 at the rebuild, always in
+        // double-float.  A far pair that comes within r_split later is still
+        // evaluated in double-float (the pair kernel decides per pair).  A
+        // margin of skin / 4 ran the pair kernel 0.9% faster but raised the
+        // dilute-lattice error from 1.4e-6 to 2.1e-6 per atom (floored).
         if (md->farList.maxNeighbors == 0) md->farList.maxNeighbors = md->cfg.maxNeighbors;
         MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
                                   md->rsplit + 0.5 * md->cfg.skin, md->grid,
