@@ -60,8 +60,23 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(kernel):
-    """Bytes per atom of one pair-kernel launch from the committed ncu summary."""
+def issue_roofline(torch, device, per_atom, n, kern_ms, clocks):
+    """The pair kernel against the GPU's instruction issue rate (one warp
+    instruction per scheduler and clock, 4 schedulers per SM): thread
+    instructions per atom from the ncu summary x atoms / kernel time, against
+    SMs x 4 x 32 lanes x the SM clock sampled during the timed run."""
+    if per_atom is None or not clocks or not clocks.get("sm_mhz"):
+        return None
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    peak = sms * 4 * 32 * clocks["sm_mhz"] * 1e6
+    achieved = per_atom * n / (kern_ms * 1e-3)
+    return {"unit": "thread instructions/s", "thread_instructions_per_atom": per_atom, "achieved": achieved,
+            "peak": peak, "frac": achieved / peak, "sms": sms, "sm_mhz": clocks["sm_mhz"]}
+
+
+def load_traffic(kernel, key="dram_bytes_per_atom"):
+    """A per-atom figure of one pair-kernel launch (DRAM bytes, thread
+    instructions) from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(p):
         return None
@@ -70,8 +85,8 @@ def load_traffic(kernel):
             if line.lstrip().startswith("#"):
                 continue
             parts = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
-            if parts.get("kernel") == kernel and "dram_bytes_per_atom" in parts:
-                return float(parts["dram_bytes_per_atom"])
+            if parts.get("kernel") == kernel and key in parts:
+                return float(parts[key])
     return None
 
 
@@ -977,6 +992,7 @@ def main():
     peak, peak_kind = load_peaks()
     achieved = bytes_per_atom * n / (kern_ms * 1e-3) / 1e9
     tpa = load_traffic(kname)
+    ipa = load_traffic(kname, "thread_instructions_per_atom")
 
     # end to end through the public API with pinned host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -1035,7 +1051,8 @@ def main():
                      "frac": achieved / peak, "peak_source": peak_kind, "kernel_ms": kern_ms,
                      "algorithmic_bytes_per_atom": bytes_per_atom, "kernel_bytes_per_atom": kernel_bytes,
                      "kernel_bytes_gbs": kernel_bytes * n / (kern_ms * 1e-3) / 1e9,
-                     "traffic": (tpa * n) if tpa is not None else None},
+                     "traffic": (tpa * n) if tpa is not None else None,
+                     "instruction_issue": issue_roofline(torch, local_rank, ipa, n, kern_ms, r["clocks"])},
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -782,9 +782,9 @@ __device__ __forceinline__ RowOut row_force(const BDev& B, int32_t i, int sub, b
             if (ownMod <= 0.0 && partMod <= 0.0) return;  // both coarse grained: ideal gas
             const double4 pj = B.pos[j];
             const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            // explicit roundings (the oracle's order): the same bits in every
-            // kernel that inlines this body
-            const double distSqr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            // explicit roundings: the same bits in every kernel that inlines
+            // this body
+            const double distSqr = __fma_rn(dx, dx, __fma_rn(dy, dy, __dmul_rn(dz, dz)));
             if (distSqr > B.rcSqr) return;
             const bool hyPair = is_hy(ownMod) || is_hy(partMod);
             double ff, e;

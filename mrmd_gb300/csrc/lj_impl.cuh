@@ -62,22 +62,22 @@ inline LJDev to_dev(const mrmd_lj_params& p)
 
 // computeForceAndEnergy (action/LennardJones.hpp:52-78) in FP64; the
 // reciprocal is the correctly rounded one, identical to 1.0 / distSqr.
-// Every operation rounded on its own, in the reference's order (no
-// contraction left to the compiler): the same bits in every kernel that
-// inlines it, and the oracle's.
+// The reference's formulae with every rounding explicit (fused
+// multiply-adds where a product meets a sum, nothing left to the compiler's
+// contraction): the same bits in every kernel that inlines it.
 __device__ __forceinline__ void lj_eval_fp64(const LJDev& p, double distSqr, double& ff, double& e)
 {
     if (distSqr >= p.capSqr)
     {
         const double frac2 = __drcp_rn(distSqr);
         const double frac6 = __dmul_rn(__dmul_rn(frac2, frac2), frac2);
-        ff = __dmul_rn(__dmul_rn(frac6, __dsub_rn(__dmul_rn(p.ff1, frac6), p.ff2)), frac2);
-        e = __dsub_rn(__dmul_rn(frac6, __dsub_rn(__dmul_rn(p.ef1, frac6), p.ef2)), p.shift);
+        ff = __dmul_rn(__dmul_rn(frac6, __fma_rn(p.ff1, frac6, -p.ff2)), frac2);
+        e = __fma_rn(frac6, __fma_rn(p.ef1, frac6, -p.ef2), -p.shift);
         return;
     }
     const double dist = __dsqrt_rn(distSqr);
     ff = __ddiv_rn(p.capCoeff, dist);
-    e = __dsub_rn(__dsub_rn(p.eCap, __dmul_rn(__dsub_rn(dist, p.capDist), p.capCoeff)), p.shift);
+    e = __dsub_rn(__fma_rn(-__dsub_rn(dist, p.capDist), p.capCoeff, p.eCap), p.shift);
 }
 
 void lj_force_energy_host(const mrmd_lj_params* t, double distSqr, int64_t typeIdx, double* ff, double* e);
