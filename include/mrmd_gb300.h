@@ -473,6 +473,10 @@ typedef struct {
     double splitRadius;      /* mixed form: pairs beyond it are evaluated in FP32, closer
                                 ones in double-float; 0 = 1.5 sigma (at least 1.05 x the
                                 capping distance); >= rc: every pair in double-float */
+    int32_t tileBuild;       /* mixed form: 0 = the tile list in one pass from the cell list
+                                (the int32 rows and their tile form when a tile does not fit);
+                                1 = always the int32 rows, then their tile form */
+    int32_t reserved0;
 } mrmd_md_config;
 
 int mrmd_md_create(mrmd_ctx* ctx, mrmd_md** out, const mrmd_md_config* cfg, int64_t n,

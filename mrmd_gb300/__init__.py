@@ -713,12 +713,15 @@ class LJSystem:
 
     sort_atoms: permute the atoms into Z-order of their cells at every k-th
     list rebuild (True = every rebuild, 0 = never; the order decays slowly,
-    so every 4th rebuild is the default)."""
+    so every 4th rebuild is the default).  tile_build (mixed form):
+    "one_pass" builds the tile list from the cell list, "two_kernel" the int32
+    rows and then their tile form (the same lists)."""
 
     def __init__(self, pos, vel, box_min, box_max, rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0,
                  capping_distance=0.0, shifted=True, precision=PREC_FP64, dt=0.005,
                  rebuild_interval=10, use_graph=True, sort_atoms=4, max_neighbors=0, mass=None,
-                 observe=False, split_radius=0.0, gather_neighbours=False, ctx: Context | None = None):
+                 observe=False, split_radius=0.0, gather_neighbours=False, tile_build="one_pass",
+                 ctx: Context | None = None):
         self.ctx = ctx or default_context()
         pos = _f64(pos)
         vel = _f64(vel)
@@ -738,6 +741,9 @@ class LJSystem:
         cfg.observe = int(bool(observe))
         cfg.splitRadius = float(split_radius)
         cfg.gatherNeighbours = int(bool(gather_neighbours))
+        if tile_build not in ("one_pass", "two_kernel"):
+            raise ValueError("tile_build must be 'one_pass' or 'two_kernel'")
+        cfg.tileBuild = 1 if tile_build == "two_kernel" else 0
         self.cfg = cfg
         h = C.c_void_p()
         m = None if mass is None else _f64(np.broadcast_to(mass, (self.n,)).copy())

@@ -95,7 +95,8 @@ class MDConfigS(C.Structure):
                 ("cappingDistance", C.c_double), ("shifted", C.c_int32),
                 ("precision", C.c_int32), ("dt", C.c_double), ("rebuildInterval", C.c_int64),
                 ("useGraph", C.c_int32), ("sortAtoms", C.c_int32), ("maxNeighbors", C.c_int64),
-                ("observe", C.c_int32), ("gatherNeighbours", C.c_int32), ("splitRadius", C.c_double)]
+                ("observe", C.c_int32), ("gatherNeighbours", C.c_int32), ("splitRadius", C.c_double),
+                ("tileBuild", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class AdResSConfigS(C.Structure):

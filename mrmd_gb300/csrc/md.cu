@@ -282,7 +282,7 @@ int md_rebuild(mrmd_ctx* ctx, mrmd_md* md)
         if (md->farList.maxNeighbors == 0) md->farList.maxNeighbors = md->cfg.maxNeighbors;
         MRMD_TRY(build_split_list(ctx, &md->list, &md->farList, a->pos, nAll, 0, a->numLocal, rlist,
                                   md->rsplit + 0.5 * md->cfg.skin, md->grid,
-                                  md->cfg.gatherNeighbours ? nullptr : &md->tiles));
+                                  md->cfg.gatherNeighbours ? nullptr : &md->tiles, md->cfg.tileBuild == 0));
         MRMD_TRY(list_total_pairs(ctx, &md->farList));
         md->tp = make_tile_params(md->lj->p0, md->lj->rcSqr, md->rsplit, md->farList.maxNeighbors);
     }

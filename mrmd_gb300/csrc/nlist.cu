@@ -339,7 +339,8 @@ __global__ void k_count_sum(const int32_t* __restrict__ counts, int64_t n, unsig
 }
 
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
-                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid, TileList* tiles)
+                     int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid, TileList* tiles,
+                     bool onePass)
 {
     if (tiles && begin != 0) return set_error(ctx, MRMD_ERR_ARG, "tile lists need rows from particle 0");
     CellList* cl = static_cast<CellList*>(nearList->cells);
@@ -373,7 +374,12 @@ int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, c
         };
         if (rows > 0)
         {
-            if (tiles)
+            if (tiles && !onePass)
+            {
+                MRMD_TRY(int32_rows());
+                MRMD_TRY(tile_build_launch(ctx, tiles, rows, nPos, nearList, farList, maxCount));
+            }
+            else if (tiles)
                 MRMD_TRY(tile_list_launch(ctx, tiles, rows, nPos, *cl, rsq, rsqLo, rsqHi, nearSqF, nearList,
                                           farList, pos4, maxCount));
             else

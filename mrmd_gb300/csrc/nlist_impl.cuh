@@ -164,9 +164,10 @@ struct TileList;
 // With `tiles` (begin = 0), the lists are built in their tile form
 // (lj_tile.cuh) only, in one pass (tile_list_launch); when a tile does not
 // fit that pass, the int32 rows are built and their tile form made from them.
+// onePass = false: always the int32 rows and then their tile form.
 int build_split_list(mrmd_ctx* ctx, mrmd_nlist* nearList, mrmd_nlist* farList, const double* pos4, int64_t nPos,
                      int64_t begin, int64_t end, double rlist, double rnear, const CellGrid& grid,
-                     TileList* tiles = nullptr);
+                     TileList* tiles = nullptr, bool onePass = true);
 int list_total_pairs(mrmd_ctx* ctx, mrmd_nlist* nl);
 // The tile form of the split full list over rows [0, rows) built in one
 // pass from the cell list `cl` (tile_list.cu), without the int32 rows: the

@@ -236,6 +236,47 @@ def test_elongated_box_linear_sort_fallback(M):
     assert np.all(np.isfinite(e))
 
 
+def test_one_pass_and_two_kernel_tile_builds_agree(M):
+    """The tile list built in one pass from the cell list and the one made
+    from the int32 rows (tile_build="two_kernel"): the same pairs in the same
+    rows and order, so the forces and a short trajectory are bitwise equal."""
+    pos, L = fcc(16)  # 16,384 atoms
+    vel = mb_velocities(len(pos), 0.728, 9)
+    a = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED)
+    b = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED, tile_build="two_kernel")
+    a.run(35)
+    b.run(35)
+    assert a.tile_stats()["tiled"] and b.tile_stats()["tiled"]
+    assert a.tile_stats()["two_pass_builds"] == 0
+    for x, y in zip(a.state(), b.state()):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(a.pair_keys(), b.pair_keys())
+
+
+def test_unsorted_atoms_take_the_two_kernel_tile_build(M):
+    """Atoms never cell-sorted and given in random order: a tile's rows are
+    scattered through the box, so the one-pass tile build overflows its span
+    table and the rebuild makes the int32 rows and their tile form instead.
+    The tile form it makes holds the same pairs in the same order (forces
+    bitwise equal to the gather form, which reads the int32 rows directly)."""
+    pos, L = fcc(12)  # 6,912 atoms
+    rng = np.random.default_rng(11)
+    perm = rng.permutation(len(pos))
+    pos = pos[perm] + rng.normal(0, 0.05, pos.shape)
+    vel = mb_velocities(len(pos), 0.728, 5)
+    t = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED, sort_atoms=0)
+    g = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, precision=M.PREC_MIXED, sort_atoms=0, gather_neighbours=True)
+    t.eval_forces()
+    g.eval_forces()
+    st = t.tile_stats()
+    assert st["two_pass_builds"] >= 1 and st["unfit_tiles"] > 0
+    np.testing.assert_array_equal(t.state()[2], g.state()[2])
+    np.testing.assert_array_equal(t.pair_keys(), g.pair_keys())
+    t.run(20)
+    g.run(20)
+    np.testing.assert_array_equal(t.state()[0], g.state()[0])
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_nonfinite_state_reported_by_the_stepper(M, precision):
     """An infinite velocity, set on the host, makes a position infinite after
