@@ -77,3 +77,51 @@ def test_bounds_build_reports_a_bad_ghost_index():
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "reported: MRMD_ERR_BOUNDS" in r.stdout and r.stdout.strip().endswith("ok"), r.stdout
+
+
+CLEAN = textwrap.dedent(r"""
+    import sys
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, ROOT + "/tests")
+    import mrmd_gb300 as M
+    from test_gpu_md import fcc, mb_velocities
+    ctx = M.default_context()
+    if ctx.lib.mrmd_bounds_checked() != 1:
+        print("not the bounds-checked library")
+        sys.exit(3)
+    pos, L = fcc(12)
+    vel = mb_velocities(len(pos), 0.728, 3)
+    for kw in (dict(precision=M.PREC_MIXED), dict(precision=M.PREC_MIXED, tile_build="two_kernel"),
+               dict(precision=M.PREC_MIXED, gather_neighbours=True), dict(precision=M.PREC_FP64)):
+        s = M.LJSystem(pos, vel, [0, 0, 0], [L] * 3, **kw)
+        e = s.run(45)
+        assert np.all(np.isfinite(e))
+        s.close()
+    from adress_loop import random_system
+    box = [36.0, 10.0, 10.0]
+    p, v = random_system(1800, box, 5)
+    for layout, prec in ((0, M.PREC_FP64), (1, M.PREC_MIXED), (2, M.PREC_MIXED)):
+        b = M.BatchSystem([M.Replica(1800, [0, 0, 0], box, [18.0, 5.0, 5.0], 10.0, 77)], p, v, hybrid_diameter=5.0,
+                          capping_distance=0.7842, precision=prec, list_layout=layout,
+                          threads_per_row=4 if layout == 2 else 1, rebuild_interval=5, sort_every=2,
+                          graph_steps=10, persistent=layout == 1)
+        b.run(30)
+        b.close()
+    print("clean")
+""")
+
+
+def test_bounds_build_runs_the_steppers_clean():
+    """The fused LJ stepper (both forms; the one-pass and two-kernel tile
+    builds and the gather form) and the batched engine (three layouts, the
+    persistent step kernel) under the bounds-checked library: every index
+    stays inside its array."""
+    from mrmd_gb300 import build as B
+
+    B.build(bounds_check=True)
+    env = dict(os.environ, MRMD_GB300_BOUNDS_CHECK="1")
+    r = subprocess.run([sys.executable, "-c", f"ROOT = {ROOT!r}\n" + CLEAN], env=env, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0 and r.stdout.strip().endswith("clean"), r.stdout + r.stderr
+
