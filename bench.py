@@ -339,7 +339,7 @@ def nve_drift(M, ctx, forms, cells=20, equil=2000, steps=200000, dt=0.005, seeds
             for f in forms}
 
 
-def adress_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
+def adress_leg(M, ctx, torch, stream, molecules, forms, warmup=300, steps=100):
     """The AdResS workload (scaled to `molecules` at density 0.5) through the
     drop-in stepper (AdResSSystem, mrmd_adress_*: the batched engine with one
     replica for these unit-mass molecules), both forms: ms per step,
@@ -359,12 +359,15 @@ def adress_leg(M, ctx, torch, stream, molecules, forms, warmup=50, steps=50):
                            tf_update_interval=c["U"], ctx=ctx)
         b.run(1, energies=False)
         forces[form] = b.state()[2]
+        # the random start relaxes over the first few hundred steps; its list
+        # rows grow meanwhile (capacity recoveries replay whole graphs)
         b.run(warmup - 1, energies=False)
         ms, wall, e, launches = time_run(torch, M, b, steps, stream)
         out[form] = {"ms_per_step": ms / steps, "atom_steps_per_s": n * steps / (ms * 1e-3)}
         b.close()
-    res = {"molecules": n, "forms": out,
-           "engine": "AdResSSystem (mrmd_adress_*): batched engine with one replica, CUDA graphs of 50 steps"}
+    res = {"molecules": n, "forms": out, "warmup_steps": warmup, "timed_steps": steps,
+           "engine": ("AdResSSystem (mrmd_adress_*): batched engine with one replica, CUDA graphs of 50 steps"
+                      + (", the steps between rebuilds as one persistent launch" if n >= 1000000 else ""))}
     if {"fp64", "mixed"} <= out.keys():
         res["mixed_over_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
         fa, fb = forces["fp64"], forces["mixed"]

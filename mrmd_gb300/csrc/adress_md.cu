@@ -202,13 +202,17 @@ int mrmd_adress_create(mrmd_ctx* ctx, mrmd_adress** out, const mrmd_adress_confi
         bc.tfSampleInterval = cfg->tfSampleInterval;
         bc.tfUpdateInterval = cfg->tfUpdateInterval;
         bc.initialMaxNeighbors = cfg->maxNeighbors > 0 ? cfg->maxNeighbors : 0;
-        // cell sort every 5th rebuild; graphs of 5 rebuild intervals
+        // cell sort every 5th rebuild; graphs of 5 rebuild intervals; from a
+        // million molecules the steps between rebuilds as one persistent
+        // launch (4,000,000 molecules: 2.01 against 2.33 ms per step mixed,
+        // 5.13 against 5.25 FP64; 34,560: 6% slower)
         bc.tuning.threadsPerRow = 1;
         bc.tuning.blockSize = 128;
         bc.tuning.rebuildInterval = cfg->rebuildInterval;
         bc.tuning.sortEvery = 5;
         bc.tuning.graphSteps = cfg->useGraph ? 5 * cfg->rebuildInterval : 0;
         bc.tuning.listLayout = 0;
+        bc.tuning.persistent = cfg->useGraph && n >= 1000000 ? 1 : 0;
         mrmd_replica_desc rd{};
         rd.numMolecules = n;
         for (int d = 0; d < 3; ++d)
