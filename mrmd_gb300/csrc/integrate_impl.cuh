@@ -33,6 +33,14 @@ __device__ __forceinline__ void kick_fma(double4& v, const double4& f, double dt
     v.z = __fma_rn(dtfm, f.z, v.z);
 }
 
+// 2 d, exactly, on the integer pipe (d finite and not negative zero)
+__device__ __forceinline__ double twice(double d)
+{
+    const long long b = __double_as_longlong(d);
+    const long long e = b & 0x7ff0000000000000ll;
+    return __longlong_as_double(b + (e ? (1ll << 52) : (b & 0x000fffffffffffffll)));
+}
+
 __device__ __forceinline__ void drift_fma(double4& x, const double4& v, double dt)
 {
     x.x = __fma_rn(dt, v.x, x.x);

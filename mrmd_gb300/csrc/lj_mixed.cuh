@@ -12,6 +12,7 @@ struct SplitParams
     double invScale;  // 2^-q
     double magic;     // 1.5 * 2^(52 - q)
     float invScaleF;  // 2^-q
+    double3 shift;    // magic - origin (the tile split; origin a multiple of 2^-q)
 };
 
 // origin = grid corner; extent bounds |x - origin| for every coordinate.

@@ -36,9 +36,18 @@ bool tile_split_params(const double* origin, double extent, double rlist, SplitP
     int e = 0;
     std::frexp(1.0625 * rlist / 2048.0, &e);  // value in [2^(e-1), 2^e)
     const double Q = std::ldexp(1.0, e);      // smallest power of two above it
-    if (!(extent < Q * 16777216.0)) return false;
+    if (!(extent + Q < Q * 16777216.0)) return false;
     *out = make_split(1.0 / Q, Q);
-    out->origin = make_double3(origin[0], origin[1], origin[2]);
+    // the records are differences: any origin on the Q grid serves, and
+    // magic - origin is then exact (|origin| < 2^40 Q)
+    double o[3];
+    for (int d = 0; d < 3; ++d)
+    {
+        o[d] = std::floor(origin[d] / Q) * Q;
+        if (!(std::fabs(o[d]) < Q * 1099511627776.0)) return false;
+    }
+    out->origin = make_double3(o[0], o[1], o[2]);
+    out->shift = make_double3(out->magic - o[0], out->magic - o[1], out->magic - o[2]);
     return true;
 }
 
