@@ -4,6 +4,7 @@
 // Host and device (the host form is tested against the C cast).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -80,5 +81,85 @@ __host__ __device__ inline float f64_to_f32_rn(double d)
         }
     }
     return f32_from_bits(sign | bits);
+}
+
+__host__ __device__ inline uint32_t f32_bits(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t b;
+    std::memcpy(&b, &f, sizeof(b));
+    return b;
+#endif
+}
+
+__host__ __device__ inline double f64_from_bits(uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+#endif
+}
+
+// The double of a float (exact, subnormals and NaN payloads included), with
+// integer operations only.
+__host__ __device__ inline double f32_to_f64(float f)
+{
+    const uint32_t b = f32_bits(f);
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    const uint32_t e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    uint64_t bits;
+    if (e == 0xffu)
+        bits = 0x7ff0000000000000ull | ((uint64_t)m << 29);
+    else if (e != 0)
+        bits = ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    else if (m == 0)
+        bits = 0;
+    else
+    {
+        // subnormal: m 2^-149 with the leading one of m at bit p
+#ifdef __CUDA_ARCH__
+        const int p = 31 - __clz((int)m);
+#else
+        const int p = 31 - __builtin_clz(m);
+#endif
+        bits = ((uint64_t)(p + 874) << 52) | ((uint64_t)(m ^ (1u << p)) << (52 - p));
+    }
+    return f64_from_bits(sign | bits);
+}
+
+#ifdef __CUDA_ARCH__
+#define MRMD_FADD(a, b) __fadd_rn(a, b)
+#define MRMD_FSUB(a, b) __fsub_rn(a, b)
+#define MRMD_FMUL(a, b) __fmul_rn(a, b)
+#else
+#define MRMD_FADD(a, b) ((float)(a) + (float)(b))
+#define MRMD_FSUB(a, b) ((float)(a) - (float)(b))
+#define MRMD_FMUL(a, b) ((float)(a) * (float)(b))
+#endif
+
+// floor(fl(fl(x - mn) * rdx)) (FP64 operations) from an FP32 estimate, when
+// the estimate's error interval holds no integer: *ok false otherwise
+// (and for NaN / infinite / huge x), where the caller evaluates the FP64
+// formula.  mnf, rdxf: mn and rdx rounded to FP32.  The estimate's error is
+// below (|x| + |mn| + 3 |x - mn|) rdx 2^-24 (the roundings of x, mn, rdx,
+// the difference and the product; the FP64 value's own error is ~2^-52
+// relative); the interval is four times that.
+__host__ __device__ inline float floor_of_scaled(double x, float mnf, float rdxf, bool* ok)
+{
+    const float xf = f64_to_f32_rn(x);
+    const float d = MRMD_FSUB(xf, mnf);
+    const float tf = MRMD_FMUL(d, rdxf);
+    const float ax = xf < 0.f ? -xf : xf, am = mnf < 0.f ? -mnf : mnf, ad = d < 0.f ? -d : d;
+    const float at = tf < 0.f ? -tf : tf;
+    const float err = MRMD_FMUL(MRMD_FADD(MRMD_FMUL(MRMD_FADD(MRMD_FADD(ax, am), MRMD_FADD(ad, ad)), rdxf), at),
+                                2.384185791015625e-7f);  // 2^-22
+    const float lo = std::floor(MRMD_FSUB(tf, err)), hi = std::floor(MRMD_FADD(tf, err));
+    *ok = lo == hi;  // false for NaN
+    return lo;
 }
 }  // namespace mrmd_impl

@@ -43,6 +43,8 @@ CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, i
     }
     g.mn = make_double3(mn[0], mn[1], mn[2]);
     g.rdx = make_double3(rdx[0], rdx[1], rdx[2]);
+    g.mnf = make_float3((float)mn[0], (float)mn[1], (float)mn[2]);
+    g.rdxf = make_float3((float)rdx[0], (float)rdx[1], (float)rdx[2]);
     g.n = make_int3(n[0], n[1], n[2]);
     g.ncell = (int64_t)n[0] * n[1] * n[2];
     g.extent = extent;
@@ -72,12 +74,16 @@ __global__ void k_cell_count(const double4* __restrict__ pos, int64_t n, CellGri
     {
         int32_t c;
         const double4 p = pos[i];
-        if (nonfinite && !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) *nonfinite = 1;
+        // finite: exponent field below all ones (integer test, no FP64 compare)
+        const uint32_t ex = (uint32_t)(__double_as_longlong(p.x) >> 52) & 0x7ffu;
+        const uint32_t ey = (uint32_t)(__double_as_longlong(p.y) >> 52) & 0x7ffu;
+        const uint32_t ez = (uint32_t)(__double_as_longlong(p.z) >> 52) & 0x7ffu;
+        if (nonfinite && (ex == 0x7ffu || ey == 0x7ffu || ez == 0x7ffu)) *nonfinite = 1;
         if (morton)
         {
-            const uint32_t cx = (uint32_t)cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x);
-            const uint32_t cy = (uint32_t)cell_coord(p.y, g.mn.y, g.rdx.y, g.n.y);
-            const uint32_t cz = (uint32_t)cell_coord(p.z, g.mn.z, g.rdx.z, g.n.z);
+            const uint32_t cx = (uint32_t)cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x, g.mnf.x, g.rdxf.x);
+            const uint32_t cy = (uint32_t)cell_coord(p.y, g.mn.y, g.rdx.y, g.n.y, g.mnf.y, g.rdxf.y);
+            const uint32_t cz = (uint32_t)cell_coord(p.z, g.mn.z, g.rdx.z, g.n.z, g.mnf.z, g.rdxf.z);
             c = (int32_t)((spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz));
         }
         else

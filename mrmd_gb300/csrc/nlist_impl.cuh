@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "f32_round.cuh"
 
 namespace mrmd_impl
 {
@@ -16,6 +17,7 @@ struct CellGrid
     int64_t ncell;
     double extent;  // max |coordinate| relative bound used for FP32 error bands
     int reach;      // list builds search cells within +-reach per axis
+    float3 mnf, rdxf;  // mn, rdx rounded to FP32 (the binning's FP32 estimate)
 };
 
 // n = max(1, floor(L * reach / delta)) cells per axis, edge L/n >= delta / reach,
@@ -25,18 +27,30 @@ CellGrid make_grid(const double* gridMin, const double* gridMax, double delta, i
 // cell = clamp(floor((x - min) * rdx), 0, n - 1) per axis, id (ix*ny + iy)*nz + iz.
 // A NaN coordinate goes to cell 0: the comparisons are written so that NaN
 // fails `t >= 0` (a double-to-int conversion of NaN is not a valid cell).
-__device__ __forceinline__ int32_t cell_coord(double x, double mn, double rdx, int n)
+// Not inlined: the callers reach it only when the FP32 estimate is open.
+static __device__ __noinline__ int32_t cell_coord_fp64(double x, double mn, double rdx, int n)
 {
     const double t = floor(__dmul_rn(__dsub_rn(x, mn), rdx));
     int c = t >= 0.0 ? (t > (double)(n - 1) ? n - 1 : (int)t) : 0;
     return c;
 }
 
+// The same cell as cell_coord_fp64, from the FP32 estimate where it is
+// certain (all but a few in ten thousand coordinates): GB300's FP64 pipe
+// made the binning kernel FP64 bound.
+__device__ __forceinline__ int32_t cell_coord(double x, double mn, double rdx, int n, float mnf, float rdxf)
+{
+    bool ok;
+    const float t = floor_of_scaled(x, mnf, rdxf, &ok);
+    if (!ok) return cell_coord_fp64(x, mn, rdx, n);
+    return t >= 0.f ? (t > (float)(n - 1) ? n - 1 : (int)t) : 0;
+}
+
 __device__ __forceinline__ int32_t cell_of(const double4& p, const CellGrid& g)
 {
-    const int32_t cx = cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x);
-    const int32_t cy = cell_coord(p.y, g.mn.y, g.rdx.y, g.n.y);
-    const int32_t cz = cell_coord(p.z, g.mn.z, g.rdx.z, g.n.z);
+    const int32_t cx = cell_coord(p.x, g.mn.x, g.rdx.x, g.n.x, g.mnf.x, g.rdxf.x);
+    const int32_t cy = cell_coord(p.y, g.mn.y, g.rdx.y, g.n.y, g.mnf.y, g.rdxf.y);
+    const int32_t cz = cell_coord(p.z, g.mn.z, g.rdx.z, g.n.z, g.mnf.z, g.rdxf.z);
     return (cx * g.n.y + cy) * g.n.z + cz;
 }
 
