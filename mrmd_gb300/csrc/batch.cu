@@ -79,12 +79,14 @@ __device__ __forceinline__ void pre_body(const BDev& B, int rebuild, int64_t tid
         const float4 r0 = B.ref[i];
         if (MIXED && !rebuild)
         {
-            // the split coordinates are relative to the same origin as r0
+            // r0 is relative to gmn, the split coordinates to the split
+            // origin, soff below it
             B.pos[i] = x;
             B.vel[i] = v;
             float4 h, l;
             slot_derived<MIXED>(B, R, i, x, &h, &l);
-            const float dx = (h.x - r0.x) + l.x, dy = (h.y - r0.y) + l.y, dz = (h.z - r0.z) + l.z;
+            const float dx = ((h.x - r0.x) + l.x) - R.soff[0], dy = ((h.y - r0.y) + l.y) - R.soff[1],
+                        dz = ((h.z - r0.z) + l.z) - R.soff[2];
             m2 = fmaxf(m2, __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))));
             continue;
         }
@@ -1833,6 +1835,17 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
         const SplitParams sp = split_params(sd.minGhostCorner, ext * 1.25 + 8.0);
         R.splitScale = sp.scale;
         R.splitInv = sp.invScale;
+        for (int a = 0; a < 3; ++a)
+        {
+            // the split origin on the 2^-q grid (the pair kernels use only
+            // differences of split coordinates), so that magic - origin is exact
+            const double o = std::floor(R.gmn[a] / sp.invScale) * sp.invScale;
+            if (!(std::fabs(o) < sp.invScale * 1099511627776.0))
+                rc = set_error(ctx, MRMD_ERR_ARG, "replica %lld too far from the origin for the mixed form",
+                               (long long)r);
+            R.sshift[a] = sp.magic - o;
+            R.soff[a] = (float)(R.gmn[a] - o);
+        }
         mrmd_slab slab{};
         slab.center[0] = d.slabCenter[0];
         slab.center[1] = d.slabCenter[1];

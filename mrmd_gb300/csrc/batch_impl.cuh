@@ -49,7 +49,9 @@ struct RepDev
     double gmn[3], grdx[3];  // ghost-inclusive cell grid
     int32_t gn[3];
     int32_t cellBase;
-    double splitScale, splitInv;  // mixed form: coordinates split relative to gmn
+    double splitScale, splitInv;  // mixed form: the split's quantum 2^-q
+    double sshift[3];             // magic - the split origin (gmn rounded down to the 2^-q grid)
+    float soff[3];                // gmn - the split origin, [0, 2^-q)
     SlabDev slab;
     int32_t consistent;  // slab weights of every image equal those of its real molecule
     int32_t lbase, n;
@@ -203,13 +205,15 @@ __device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int
     B.lamt[s] = m;
     if (MIXED)
     {
-        const float h = (float)m;
-        B.lamtf[s] = make_float2(h, (float)(m - (double)h));
-        const SplitParams sp = make_split(R.splitScale, R.splitInv);
+        // the conversions on the integer pipe (the same values as the FP64
+        // conversions: this kernel is bound by the FP64 pipe)
+        const float h = f64_to_f32_rn(m);
+        B.lamtf[s] = make_float2(h, f64_to_f32_rn(__dsub_rn(m, f32_to_f64(h))));
+        const float invQ = (float)R.splitInv;
         float4 hv, lv;
-        split_one(x.x - R.gmn[0], sp, hv.x, lv.x);
-        split_one(x.y - R.gmn[1], sp, hv.y, lv.y);
-        split_one(x.z - R.gmn[2], sp, hv.z, lv.z);
+        split_one_shifted(x.x, R.sshift[0], invQ, hv.x, lv.x);
+        split_one_shifted(x.y, R.sshift[1], invQ, hv.y, lv.y);
+        split_one_shifted(x.z, R.sshift[2], invQ, hv.z, lv.z);
         hv.w = 0.0f;
         lv.w = 0.0f;
         B.hi[s] = hv;

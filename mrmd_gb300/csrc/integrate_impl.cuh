@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "f32_round.cuh"
 
 namespace mrmd_impl
 {
@@ -149,9 +150,11 @@ __device__ __forceinline__ void normal3(uint64_t seed, uint64_t step, uint64_t a
     float ca, sa, cb, sb;
     bm_sincos(u[1], ca, sa);
     bm_sincos(u[3], cb, sb);
-    g[0] = (double)__fmul_rn(ra, ca);
-    g[1] = (double)__fmul_rn(ra, sa);
-    g[2] = (double)__fmul_rn(rb, cb);
+    // exact widening on the integer pipe (the FP64 pipe bounds the kernels
+    // that draw the noise)
+    g[0] = f32_to_f64(__fmul_rn(ra, ca));
+    g[1] = f32_to_f64(__fmul_rn(ra, sa));
+    g[2] = f32_to_f64(__fmul_rn(rb, cb));
 }
 
 // Ornstein-Uhlenbeck coefficients of one mass (UpdateSteps.hpp:56-79):

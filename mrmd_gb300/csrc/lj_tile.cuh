@@ -23,7 +23,6 @@
 
 #include <cstdint>
 
-#include "f32_round.cuh"
 #include "lj_impl.cuh"
 #include "lj_mixed.cuh"
 
@@ -41,27 +40,13 @@ constexpr int TILE_CAP = 3072;
 // otherwise.
 bool tile_split_params(const double* origin, double extent, double rlist, SplitParams* out);
 
-// One coordinate: hi = k Q, the multiple of Q nearest to c = x - origin
-// (ties to even k), and lo = c - hi rounded to FP32.  With the origin a
-// multiple of Q, t = x + (magic - origin) rounds c to the Q grid in one
-// addition (t has ulp Q, and k is the low word of its bits); t - (magic -
-// origin) = k Q + origin exactly, and x - (k Q + origin) is exact too (at
-// most Q / 2 in magnitude).  Three FP64 additions; the FP32 rounding of lo
-// runs on the integer pipe.
-__device__ __forceinline__ void tile_split_one(double x, double shift, float invScaleF, float& h, float& l)
-{
-    const double t = __dadd_rn(x, shift);
-    h = __int2float_rn(__double2loint(t)) * invScaleF;  // exact: |k| < 2^24, power-of-two scale
-    l = f64_to_f32_rn(__dsub_rn(x, __dsub_rn(t, shift)));
-}
-
 // (A, B) records of one position.
 __device__ __forceinline__ void tile_split(const double4& x, const SplitParams& sp, float4& a, float2& b)
 {
     float lx, ly, lz;
-    tile_split_one(x.x, sp.shift.x, sp.invScaleF, a.x, lx);
-    tile_split_one(x.y, sp.shift.y, sp.invScaleF, a.y, ly);
-    tile_split_one(x.z, sp.shift.z, sp.invScaleF, a.z, lz);
+    split_one_shifted(x.x, sp.shift.x, sp.invScaleF, a.x, lx);
+    split_one_shifted(x.y, sp.shift.y, sp.invScaleF, a.y, ly);
+    split_one_shifted(x.z, sp.shift.z, sp.invScaleF, a.z, lz);
     a.w = lx;
     b = make_float2(ly, lz);
 }
