@@ -74,15 +74,15 @@ def test_adress_mixed_close_to_fp64(M, composed):
     assert np.abs(pa - pb).max() < 1e-7
 
 
-# BASELINE config 2 physics: 34,560 single-site molecules in 120 x 24 x 24,
+# The 34,560-molecule AdResS workload: single-site molecules in 120 x 24 x 24,
 # density 0.5, capped LJ (cap 1000 <-> r_cap 0.7842), atomistic slab 30,
 # hybrid 10, Langevin T 1 gamma 1, thermodynamic force on 100 bins sampled
 # every step and updated every 1,000 steps
-CONFIG2 = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=10, gamma=1.0, T=1.0, seed=77,
+ADRESS_34560 = dict(rc=2.5, skin=0.3, sigma=1.0, epsilon=1.0, cap=0.7842, dt=0.005, K=10, gamma=1.0, T=1.0, seed=77,
                at=30.0, hy=10.0, nu=1, binw=1.2, rho=0.5, mod=1.0, tfs=2.4, tfr=3.0, S=1, U=1000)
 
 
-def test_config2_thermodynamic_force_over_update_cycles(M, orc):
+def test_adress_34560_thermodynamic_force_over_update_cycles(M, orc):
     """Three thermodynamic-force update cycles (ThermodynamicForce.hpp:124-152,
     every 1,000 steps) of the 34,560-molecule system, then 990 steps into the
     fourth, on the GPU (FP64 form) and in the oracle loop from the same start
@@ -99,7 +99,7 @@ def test_config2_thermodynamic_force_over_update_cycles(M, orc):
     correlated bins is uncertain to about 25%) and max over bins <= 4.5 s
     (4.5 standard deviations).  Both for the table after the third update
     and for the density profile of the fourth cycle (counts per sample)."""
-    p = CONFIG2
+    p = ADRESS_34560
     box = [120.0, 24.0, 24.0]
     pos, vel = system(34560, box, 11)
     steps = 3 * p["U"] + 990
