@@ -1835,6 +1835,11 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
         const SplitParams sp = split_params(sd.minGhostCorner, ext * 1.25 + 8.0);
         R.splitScale = sp.scale;
         R.splitInv = sp.invScale;
+        {
+            int e = 0;
+            std::frexp(sp.invScale, &e);  // 2^-q = 0.5 * 2^e
+            R.sq = 1 - e;
+        }
         for (int a = 0; a < 3; ++a)
         {
             // the split origin on the 2^-q grid (the pair kernels use only
@@ -1843,7 +1848,7 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
             if (!(std::fabs(o) < sp.invScale * 1099511627776.0))
                 rc = set_error(ctx, MRMD_ERR_ARG, "replica %lld too far from the origin for the mixed form",
                                (long long)r);
-            R.sshift[a] = sp.magic - o;
+            R.sko[a] = (long long)(o / sp.invScale);
             R.soff[a] = (float)(R.gmn[a] - o);
         }
         mrmd_slab slab{};

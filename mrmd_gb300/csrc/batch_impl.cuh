@@ -50,7 +50,8 @@ struct RepDev
     int32_t gn[3];
     int32_t cellBase;
     double splitScale, splitInv;  // mixed form: the split's quantum 2^-q
-    double sshift[3];             // magic - the split origin (gmn rounded down to the 2^-q grid)
+    long long sko[3];             // the split origin / 2^-q (gmn rounded down to the 2^-q grid)
+    int32_t sq;                   // q
     float soff[3];                // gmn - the split origin, [0, 2^-q)
     SlabDev slab;
     int32_t consistent;  // slab weights of every image equal those of its real molecule
@@ -211,9 +212,9 @@ __device__ __forceinline__ void slot_derived(const BDev& B, const RepDev& R, int
         B.lamtf[s] = make_float2(h, f64_to_f32_rn(__dsub_rn(m, f32_to_f64(h))));
         const float invQ = (float)R.splitInv;
         float4 hv, lv;
-        split_one_shifted(x.x, R.sshift[0], invQ, hv.x, lv.x);
-        split_one_shifted(x.y, R.sshift[1], invQ, hv.y, lv.y);
-        split_one_shifted(x.z, R.sshift[2], invQ, hv.z, lv.z);
+        split_bits(x.x, R.sko[0], R.sq, invQ, hv.x, lv.x);
+        split_bits(x.y, R.sko[1], R.sq, invQ, hv.y, lv.y);
+        split_bits(x.z, R.sko[2], R.sq, invQ, hv.z, lv.z);
         hv.w = 0.0f;
         lv.w = 0.0f;
         B.hi[s] = hv;

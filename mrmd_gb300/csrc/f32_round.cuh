@@ -132,6 +132,103 @@ __host__ __device__ inline double f32_to_f64(float f)
     return f64_from_bits(sign | bits);
 }
 
+// The float nearest to r 2^E (ties to even), r a signed integer, with
+// integer operations only.
+__host__ __device__ inline float scaled_i64_to_f32_rn(int64_t r, int E)
+{
+    if (r == 0) return 0.0f;
+    const uint32_t sign = r < 0 ? 0x80000000u : 0u;
+    const uint64_t a = r < 0 ? (uint64_t)0 - (uint64_t)r : (uint64_t)r;
+#ifdef __CUDA_ARCH__
+    const int p = 63 - __clzll((long long)a);
+#else
+    const int p = 63 - __builtin_clzll(a);
+#endif
+    const int be = p + E + 127;  // biased float exponent of r 2^E (normal case)
+    uint32_t bits;
+    if (be >= 255)
+        bits = 0x7f800000u;
+    else if (be >= 1)
+    {
+        uint64_t m;
+        if (p > 23)
+        {
+            const int s = p - 23;
+            m = a >> s;
+            const uint64_t rest = a & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+            m += (rest > half || (rest == half && (m & 1ull))) ? 1ull : 0ull;
+        }
+        else
+            m = a << (23 - p);
+        // m in [2^23, 2^24]: its leading one adds one to the exponent field
+        // (a rounding carry to 2^24 adds two and clears the fraction)
+        bits = ((uint32_t)(be - 1) << 23) + (uint32_t)m;
+        if (bits >= 0x7f800000u) bits = 0x7f800000u;
+    }
+    else
+    {
+        // subnormal float: units of 2^-149
+        const int s = -(E + 149);
+        uint64_t q;
+        if (s <= 0)
+            q = a << (-s);  // below 2^23 here
+        else if (s >= 64)
+            q = 0;
+        else
+        {
+            q = a >> s;
+            const uint64_t rest = a & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+            q += (rest > half || (rest == half && (q & 1ull))) ? 1ull : 0ull;
+        }
+        bits = (uint32_t)q;
+    }
+    return f32_from_bits(sign | bits);
+}
+
+// The coordinate split hi = k Q, lo = x - o - k Q rounded to FP32, with
+// k the integer nearest to (x - o) / Q (ties to even k), Q = 2^-q and the
+// origin o = Ko Q, from the bits of x with integer operations only.  For
+// finite x with |x / Q| < 2^61 and |k| < 2^24 it gives, bit for bit, what
+// the three FP64 additions of the magic-number form give (t = x + (magic -
+// o) rounds to the Q grid with ties to the even significand, that is, to
+// even k).
+__host__ __device__ inline void split_bits(double x, long long Ko, int q, float invScaleF, float& h, float& l)
+{
+    const uint64_t b = f64_bits(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const int64_t M = (int64_t)((b & 0xfffffffffffffull) | (e ? (1ull << 52) : 0ull));
+    const int E = (e ? e : 1) - 1075;  // x = X 2^E
+    const int64_t X = (b >> 63) ? -M : M;
+    const int sh = -(E + q);  // fractional bits of x / Q in X
+    int64_t kx, r;            // x / Q = kx + r 2^-sh
+    if (sh <= 0)
+    {
+        kx = (int64_t)((uint64_t)X << (-sh));
+        r = 0;
+    }
+    else if (sh >= 62)
+    {
+        kx = 0;  // |x / Q| < 2^-9
+        r = X;
+    }
+    else
+    {
+        const int64_t fl = X >> sh;  // floor (arithmetic shift)
+        const int64_t fr = X - (int64_t)((uint64_t)fl << sh);
+        const int64_t half = (int64_t)1 << (sh - 1);
+        const bool up = fr > half || (fr == half && ((fl - Ko) & 1));
+        kx = up ? fl + 1 : fl;
+        r = up ? fr - ((int64_t)1 << sh) : fr;
+    }
+    const int32_t k = (int32_t)(kx - Ko);
+#ifdef __CUDA_ARCH__
+    h = __fmul_rn(__int2float_rn(k), invScaleF);
+#else
+    h = (float)k * invScaleF;
+#endif
+    l = scaled_i64_to_f32_rn(r, E);
+}
+
 #ifdef __CUDA_ARCH__
 #define MRMD_FADD(a, b) __fadd_rn(a, b)
 #define MRMD_FSUB(a, b) __fsub_rn(a, b)

@@ -14,6 +14,8 @@ struct SplitParams
     double magic;     // 1.5 * 2^(52 - q)
     float invScaleF;  // 2^-q
     double3 shift;    // magic - origin (the tile split; origin a multiple of 2^-q)
+    longlong3 ko;     // origin / 2^-q (the tile split, split_bits)
+    int q;
 };
 
 // origin = grid corner; extent bounds |x - origin| for every coordinate.
@@ -30,20 +32,6 @@ __device__ __forceinline__ void split_one(double c, const SplitParams& sp, float
     const int k = __double2loint(t);
     h = __int2float_rn(k) * sp.invScaleF;  // exact: |k| < 2^24, power-of-two scale
     l = __double2float_rn(__dsub_rn(c, __dsub_rn(t, sp.magic)));
-}
-
-// The same split with the origin on the Q = 2^-q grid and folded into the
-// rounding constant: hi = k Q, the multiple of Q nearest to c = x - origin
-// (ties to even k), and lo = c - hi rounded to FP32.  t = x + shift (shift =
-// magic - origin) rounds c to the Q grid in one addition (t has ulp Q, and
-// k is the low word of its bits); t - shift = k Q + origin exactly, and so
-// is x - (k Q + origin) (at most Q / 2 in magnitude).  Three FP64 additions;
-// the FP32 rounding of lo runs on the integer pipe.
-__device__ __forceinline__ void split_one_shifted(double x, double shift, float invScaleF, float& h, float& l)
-{
-    const double t = __dadd_rn(x, shift);
-    h = __int2float_rn(__double2loint(t)) * invScaleF;  // exact: |k| < 2^24, power-of-two scale
-    l = f64_to_f32_rn(__dsub_rn(x, __dsub_rn(t, shift)));
 }
 
 // The split parameters for quantum 2^-q given by `invScale`.

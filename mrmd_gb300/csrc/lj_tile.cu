@@ -48,6 +48,8 @@ bool tile_split_params(const double* origin, double extent, double rlist, SplitP
     }
     out->origin = make_double3(o[0], o[1], o[2]);
     out->shift = make_double3(out->magic - o[0], out->magic - o[1], out->magic - o[2]);
+    out->ko = make_longlong3((long long)(o[0] / Q), (long long)(o[1] / Q), (long long)(o[2] / Q));
+    out->q = -e;  // Q = 2^e
     return true;
 }
 

@@ -40,13 +40,15 @@ constexpr int TILE_CAP = 3072;
 // otherwise.
 bool tile_split_params(const double* origin, double extent, double rlist, SplitParams* out);
 
-// (A, B) records of one position.
+// (A, B) records of one position: the split of each coordinate relative to
+// the origin (a multiple of Q) on the integer pipe (split_bits: the same bits
+// as rounding x + (magic - origin) to the Q grid in FP64; no FP64 operation).
 __device__ __forceinline__ void tile_split(const double4& x, const SplitParams& sp, float4& a, float2& b)
 {
     float lx, ly, lz;
-    split_one_shifted(x.x, sp.shift.x, sp.invScaleF, a.x, lx);
-    split_one_shifted(x.y, sp.shift.y, sp.invScaleF, a.y, ly);
-    split_one_shifted(x.z, sp.shift.z, sp.invScaleF, a.z, lz);
+    split_bits(x.x, sp.ko.x, sp.q, sp.invScaleF, a.x, lx);
+    split_bits(x.y, sp.ko.y, sp.q, sp.invScaleF, a.y, ly);
+    split_bits(x.z, sp.ko.z, sp.q, sp.invScaleF, a.z, lz);
     a.w = lx;
     b = make_float2(ly, lz);
 }

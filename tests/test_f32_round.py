@@ -6,6 +6,11 @@
   float, overflow);
 - the exact integer-pipe FP32 -> FP64 widening, against the C cast on every
   subnormal and one float in 97 of the rest;
+- the integer-pipe coordinate split (split_bits), against the FP64
+  magic-number form it replaces, bit for bit: hi from rounding x + (magic -
+  origin) to the quantum grid, lo from x - (t - (magic - origin)) rounded to
+  FP32 (random quanta and grid origins, exact ties, grid points, values near
+  the origin and tiny values);
 - the binning's FP32 floor estimate, which must give the FP64 cell formula's
   cell whenever it claims certainty (random grids and coordinates, many of
   them within 2^-50 of a cell boundary)."""
@@ -196,6 +201,84 @@ def test_f32_to_f64_matches_the_c_cast(tmp_path):
     exe = tmp_path / "widen_test"
     src.write_text(WIDEN)
     subprocess.run([gxx, "-O2", "-std=c++17", f"-I{CSRC}", str(src), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "mismatches 0" in r.stdout
+
+
+SPLIT = r"""
+#include "f32_round.cuh"
+#include <cmath>
+#include <cstdio>
+#include <random>
+using namespace mrmd_impl;
+static uint32_t fb(float f) { uint32_t b; std::memcpy(&b, &f, 4); return b; }
+// the FP64 form: three additions, k from the low word of t's bits
+static void fp64_form(double x, double shift, float invQ, float& h, float& l)
+{
+    volatile double t = x + shift;
+    const double tt = t;
+    uint64_t tb;
+    std::memcpy(&tb, &tt, 8);
+    h = (float)(int32_t)(uint32_t)tb * invQ;
+    volatile double y = t - shift;
+    volatile double d = x - y;
+    l = (float)d;
+}
+int main()
+{
+    std::mt19937_64 g(99);
+    std::uniform_real_distribution<double> U(0, 1);
+    long bad = 0, n = 0;
+    for (int trial = 0; trial < 4000; ++trial)
+    {
+        const int q = (int)(U(g) * 24) - 3;
+        const double Q = std::ldexp(1.0, -q);
+        const long long Ko = U(g) < 0.3 ? 0 : (long long)((U(g) - 0.5) * 2e6);
+        const double o = (double)Ko * Q;
+        const double shift = 6755399441055744.0 * Q - o;
+        const float invQ = (float)Q;
+        for (int k = 0; k < 500; ++k)
+        {
+            double x;
+            const double r = U(g);
+            if (r < 0.5)
+                x = o + (U(g) * 1.1 - 0.05) * Q * 16777216.0 * U(g);
+            else if (r < 0.7)
+                x = o + ((double)(long long)(U(g) * 1e6) + 0.5) * Q;
+            else if (r < 0.8)
+                x = o + (double)(long long)(U(g) * 1e6) * Q;
+            else if (r < 0.9)
+                x = o + (U(g) - 0.5) * Q * std::ldexp(1.0, -(int)(U(g) * 60));
+            else
+                x = (U(g) - 0.5) * std::ldexp(1.0, -(int)(U(g) * 80));
+            if (!(std::fabs(x - o) < Q * 16777000.0) || !(std::fabs(x / Q) < std::ldexp(1.0, 61))) continue;
+            float h1, l1, h2, l2;
+            fp64_form(x, shift, invQ, h1, l1);
+            split_bits(x, Ko, q, invQ, h2, l2);
+            ++n;
+            if (fb(h1) != fb(h2) || fb(l1) != fb(l2))
+            {
+                if (bad < 5) std::printf("bad x=%.17g q=%d Ko=%lld\n", x, q, Ko);
+                ++bad;
+            }
+        }
+    }
+    std::printf("checked %ld mismatches %ld\n", n, bad);
+    return bad != 0;
+}
+"""
+
+
+def test_integer_split_matches_the_fp64_form(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "split_test.cpp"
+    exe = tmp_path / "split_test"
+    src.write_text(SPLIT)
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", f"-I{CSRC}", str(src), "-o", str(exe)],
+                   check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "mismatches 0" in r.stdout
