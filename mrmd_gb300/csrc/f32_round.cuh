@@ -203,7 +203,9 @@ __host__ __device__ inline void split_bits(double x, long long Ko, int q, float 
     int64_t kx, r;            // x / Q = kx + r 2^-sh
     if (sh <= 0)
     {
-        kx = (int64_t)((uint64_t)X << (-sh));
+        // x a multiple of Q (a non-finite x, reported by the next rebuild's
+        // binning, lands here too: no shift of 62 bits or more)
+        kx = -sh < 62 ? (int64_t)((uint64_t)X << (-sh)) : 0;
         r = 0;
     }
     else if (sh >= 62)
