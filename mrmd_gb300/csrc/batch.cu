@@ -1843,7 +1843,8 @@ int mrmd_batch_create(mrmd_ctx* ctx, mrmd_batch** out, const mrmd_batch_config* 
         for (int a = 0; a < 3; ++a)
         {
             // the split origin on the 2^-q grid (the pair kernels use only
-            // differences of split coordinates), so that magic - origin is exact
+            // differences of split coordinates), taken by split_bits as an
+            // integer multiple of 2^-q
             const double o = std::floor(R.gmn[a] / sp.invScale) * sp.invScale;
             if (!(std::fabs(o) < sp.invScale * 1099511627776.0))
                 rc = set_error(ctx, MRMD_ERR_ARG, "replica %lld too far from the origin for the mixed form",

@@ -13,8 +13,7 @@ struct SplitParams
     double invScale;  // 2^-q
     double magic;     // 1.5 * 2^(52 - q)
     float invScaleF;  // 2^-q
-    double3 shift;    // magic - origin (the tile split; origin a multiple of 2^-q)
-    longlong3 ko;     // origin / 2^-q (the tile split, split_bits)
+    longlong3 ko;     // origin / 2^-q (the tile split, split_bits; origin a multiple of 2^-q)
     int q;
 };
 

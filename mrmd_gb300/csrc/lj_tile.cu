@@ -38,8 +38,8 @@ bool tile_split_params(const double* origin, double extent, double rlist, SplitP
     const double Q = std::ldexp(1.0, e);      // smallest power of two above it
     if (!(extent + Q < Q * 16777216.0)) return false;
     *out = make_split(1.0 / Q, Q);
-    // the records are differences: any origin on the Q grid serves, and
-    // magic - origin is then exact (|origin| < 2^40 Q)
+    // the records are differences: any origin on the Q grid serves
+    // (split_bits takes it as the integer origin / Q; |origin| < 2^40 Q)
     double o[3];
     for (int d = 0; d < 3; ++d)
     {
@@ -47,7 +47,6 @@ bool tile_split_params(const double* origin, double extent, double rlist, SplitP
         if (!(std::fabs(o[d]) < Q * 1099511627776.0)) return false;
     }
     out->origin = make_double3(o[0], o[1], o[2]);
-    out->shift = make_double3(out->magic - o[0], out->magic - o[1], out->magic - o[2]);
     out->ko = make_longlong3((long long)(o[0] / Q), (long long)(o[1] / Q), (long long)(o[2] / Q));
     out->q = -e;  // Q = 2^e
     return true;
