@@ -77,8 +77,9 @@ __global__ void k_fused_kick_drift(double4* __restrict__ pos, double4* __restric
         {
             // mixed form: each update rounded once (fused multiply-add), and
             // without a record the previous step's post-kick and this step's
-            // pre-kick are one: v + 2 (dt/2m) F.  GB300's FP64 pipe bounds
-            // this kernel: 15 FP64 operations per atom with the split below.
+            // pre-kick are one: v + 2 (dt/2m) F.  Kick and drift are the
+            // kernel's 6 FP64 operations per atom (GB300's FP64 pipe runs 2
+            // per SM and clock); the split below runs on the integer pipe.
             if (OBS)
             {
                 if (postKick) kick_fma(v, f, dtfm);
